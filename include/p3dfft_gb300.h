@@ -1,0 +1,85 @@
+/*
+ * GB300 extensions of the P3DFFT++ C interface (libp3dfft_gb300.so).
+ *
+ * The reference's C++ templates (transform3D<T1,T2>, transplan<T1,T2>) are header-only
+ * wrappers over these plain-C entry points, so every exported symbol takes only ints and
+ * pointers.  None of these has a counterpart in the reference's C wrappers unless stated.
+ */
+#ifndef P3DFFT_GB300_EXT_H
+#define P3DFFT_GB300_EXT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error side channel (the reference reports errors with printf / MPI_Abort) ---- */
+#define P3DFFT_OK 0
+#define P3DFFT_ERR_BAD_ARG 1
+#define P3DFFT_ERR_UNSUPPORTED 2
+#define P3DFFT_ERR_CUDA 3
+#define P3DFFT_ERR_NO_DEVICE 4
+#define P3DFFT_ERR_TOO_LARGE 5
+#define P3DFFT_ERR_PLAN 6
+/* last error code of this thread's calls into the library, cleared by p3dfft_clear_error */
+int p3dfft_last_error(void);
+const char *p3dfft_last_error_string(void);
+void p3dfft_clear_error(void);
+
+/* ---- execution controls ---- */
+/* CUDA stream used by every launch (default 0, the legacy default stream) */
+void p3dfft_gb300_set_stream(void *cuda_stream);
+/* 1 (default): exec returns after the result is in `out`; 0: device-pointer execs return
+ * once the work is queued on the stream (host-pointer execs always synchronise). */
+void p3dfft_gb300_set_sync(int sync);
+/* Arithmetic of FP64 stages: 0 = native FP64 (DFMA), 1 = float-float on the FP32 pipe
+ * (~48-bit significand, magnitudes 2^-100..2^126).  Default from P3DFFT_GB300_FP64_ARITH. */
+void p3dfft_gb300_set_fp64_arith(int mode);
+int p3dfft_gb300_get_fp64_arith(void);
+
+/* ---- planning / execution by explicit grid descriptions (1x1x1 processor grid) ----
+ * A grid is (gdims[3], mem_order[3], dim_conj_sym).  Returns a handle >= 0, or -1 with the
+ * error recorded.  Type IDs are the reference's (0..43, p3dfft::setup order). */
+int p3dfft_gb300_plan3d(const int types[3], const int gdims1[3], const int mo1[3], int dcs1,
+                        const int gdims2[3], const int mo2[3], int dcs2);
+/* idir < 0: plain transform; 0..2: fused spectral derivative along that logical dim. */
+int p3dfft_gb300_exec3d(int plan, const void *in, void *out, int idir, int OW);
+int p3dfft_gb300_destroy3d(int plan);
+/* dt1 / dt2 (1 real, 2 complex) and precision (4/8) of a 3D plan */
+int p3dfft_gb300_plan3d_types(int plan, int *dt1, int *dt2, int *prec);
+/* Stage list of a 3D plan: per stage 1+1+3+3+1+3+3+1 = 16 ints
+ * (type, dim, gdims1[3], mo1[3], dcs1, gdims2[3], mo2[3], dcs2).  Returns the stage count. */
+int p3dfft_gb300_plan3d_stages(int plan, int *info, int max_stages);
+
+int p3dfft_gb300_plan1d(int type, const int gdims1[3], const int mo1[3], int dcs1,
+                        const int gdims2[3], const int mo2[3], int dcs2, int dim);
+int p3dfft_gb300_exec1d(int plan, const void *in, void *out, int OW);
+int p3dfft_gb300_destroy1d(int plan);
+
+/* compute_deriv on a complex field of grid (gdims, mo, dcs); prec 4 or 8, idir 0-based */
+int p3dfft_gb300_compute_deriv(int prec, const void *in, void *out, const int gdims[3],
+                               const int mo[3], int dcs, int idir);
+
+/* ---- introspection and timers ---- */
+/* number of kernels this library launched since the last reset */
+long long p3dfft_gb300_kernel_count(void);
+void p3dfft_gb300_reset_kernel_count(void);
+/* per-phase device time in seconds, accumulated when timing is enabled:
+ * phase 0 trans_exec (no reorder), 1 reorder_trans (transform + layout change),
+ * 2 reorder_out (pure reorder), 3 trans_deriv (stages with fused derivative),
+ * 4 h2d, 5 d2h */
+void p3dfft_gb300_enable_timers(int on);
+double p3dfft_gb300_timer(int phase);
+void p3dfft_gb300_reset_timers(void);
+/* device-memory helpers for callers without a CUDA runtime of their own */
+void *p3dfft_gb300_device_alloc(long long bytes);
+void p3dfft_gb300_device_free(void *p);
+int p3dfft_gb300_memcpy_h2d(void *dst, const void *src, long long bytes);
+int p3dfft_gb300_memcpy_d2h(void *dst, const void *src, long long bytes);
+int p3dfft_gb300_synchronize(void);
+/* library version string */
+const char *p3dfft_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

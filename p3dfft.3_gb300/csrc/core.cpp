@@ -1,0 +1,1224 @@
+// Host runtime of the GB300 P3DFFT++ pipeline: type registry, grid model, 3D planner, stage
+// executor, HBM buffer management and the C / Fortran / C++ entry points.
+//
+// Reference correspondence:
+//   registry            p3dfft::setup            build/init.C:121-731
+//   grid model          ProcGrid / DataGrid      build/init.C:1631-1863 (1x1x1 grid)
+//   planner             transform3D ctor         build/templ.C:91-420, find_order 627-802,
+//                                                swap0 816-858, excl 872-882, final_seq 422-435
+//   1D plans            transplan::init_tr       build/templ.C:900-992
+//   executor            transform3D::exec_deriv  build/exec.C:101-223 (stage loop)
+//   C / Fortran ABI     build/wrap.C:85-796
+// The executor keeps plans, twiddle tables and scratch fields resident in HBM (the reference
+// allocates its temporaries on every call, exec.C:148-166) and runs one fused kernel per stage.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "p3dfft.h"
+
+// ------------------------------------------------------------------------------------------
+// Type-ID globals (values assigned by setup(), registration order of build/init.C:121-731)
+extern "C" {
+int P3DFFT_EMPTY_TYPE_SINGLE, P3DFFT_EMPTY_TYPE_DOUBLE, P3DFFT_EMPTY_TYPE_SINGLE_COMPLEX, P3DFFT_EMPTY_TYPE_DOUBLE_COMPLEX;
+int P3DFFT_R2CFFT_S, P3DFFT_R2CFFT_D, P3DFFT_C2RFFT_S, P3DFFT_C2RFFT_D, P3DFFT_CFFT_FORWARD_S, P3DFFT_CFFT_FORWARD_D,
+    P3DFFT_CFFT_BACKWARD_S, P3DFFT_CFFT_BACKWARD_D;
+int P3DFFT_DCT1_REAL_S, P3DFFT_DCT1_REAL_D, P3DFFT_DST1_REAL_S, P3DFFT_DST1_REAL_D, P3DFFT_DCT1_COMPLEX_S,
+    P3DFFT_DCT1_COMPLEX_D, P3DFFT_DST1_COMPLEX_S, P3DFFT_DST1_COMPLEX_D;
+int P3DFFT_DCT2_REAL_S, P3DFFT_DCT2_REAL_D, P3DFFT_DST2_REAL_S, P3DFFT_DST2_REAL_D, P3DFFT_DCT2_COMPLEX_S,
+    P3DFFT_DCT2_COMPLEX_D, P3DFFT_DST2_COMPLEX_S, P3DFFT_DST2_COMPLEX_D;
+int P3DFFT_DCT3_REAL_S, P3DFFT_DCT3_REAL_D, P3DFFT_DST3_REAL_S, P3DFFT_DST3_REAL_D, P3DFFT_DCT3_COMPLEX_S,
+    P3DFFT_DCT3_COMPLEX_D, P3DFFT_DST3_COMPLEX_S, P3DFFT_DST3_COMPLEX_D;
+int P3DFFT_DCT4_REAL_S, P3DFFT_DCT4_REAL_D, P3DFFT_DST4_REAL_S, P3DFFT_DST4_REAL_D, P3DFFT_DCT4_COMPLEX_S,
+    P3DFFT_DCT4_COMPLEX_D, P3DFFT_DST4_COMPLEX_S, P3DFFT_DST4_COMPLEX_D;
+}
+
+namespace p3dfft {
+int EMPTY_TYPE_SINGLE, EMPTY_TYPE_DOUBLE, EMPTY_TYPE_SINGLE_COMPLEX, EMPTY_TYPE_DOUBLE_COMPLEX;
+int R2CFFT_S, R2CFFT_D, C2RFFT_S, C2RFFT_D, CFFT_FORWARD_S, CFFT_FORWARD_D, CFFT_BACKWARD_S, CFFT_BACKWARD_D;
+int DCT1_REAL_S, DCT1_REAL_D, DST1_REAL_S, DST1_REAL_D, DCT1_COMPLEX_S, DCT1_COMPLEX_D, DST1_COMPLEX_S, DST1_COMPLEX_D;
+int DCT2_REAL_S, DCT2_REAL_D, DST2_REAL_S, DST2_REAL_D, DCT2_COMPLEX_S, DCT2_COMPLEX_D, DST2_COMPLEX_S, DST2_COMPLEX_D;
+int DCT3_REAL_S, DCT3_REAL_D, DST3_REAL_S, DST3_REAL_D, DCT3_COMPLEX_S, DCT3_COMPLEX_D, DST3_COMPLEX_S, DST3_COMPLEX_D;
+int DCT4_REAL_S, DCT4_REAL_D, DST4_REAL_S, DST4_REAL_D, DCT4_COMPLEX_S, DCT4_COMPLEX_D, DST4_COMPLEX_S, DST4_COMPLEX_D;
+timer timers;
+}  // namespace p3dfft
+
+namespace p3d {
+
+// ------------------------------------------------------------------------------------------
+// error side channel
+static thread_local int t_err = E_OK;
+static thread_local char t_msg[512] = "no error";
+
+static void set_err(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+static void set_err(int code, const char *fmt, ...) {
+  t_err = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(t_msg, sizeof(t_msg), fmt, ap);
+  va_end(ap);
+  if (getenv("P3DFFT_GB300_QUIET") == nullptr) fprintf(stderr, "P3DFFT++ (GB300) error: %s\n", t_msg);
+}
+
+// ------------------------------------------------------------------------------------------
+// type registry
+struct TypeInfo {
+  int dt1, dt2, prec, kind, r2r;
+  const char *name;
+};
+static TypeInfo g_types[44];
+static bool g_setup_done = false;
+
+static void build_registry() {
+  // IDs 0..3: EMPTY single / double / single complex / double complex (init.C:132-179)
+  const char *en[4] = {"Empty Type Single", "Empty Type Double", "Empty Type Single Complex", "Empty Type Double Complex"};
+  for (int i = 0; i < 4; i++) g_types[i] = TypeInfo{i >= 2 ? 2 : 1, i >= 2 ? 2 : 1, (i & 1) ? 8 : 4, K_EMPTY, 0, en[i]};
+  // 4..11: R2C S/D, C2R S/D, CFFT_FORWARD S/D, CFFT_BACKWARD S/D (init.C:216-311)
+  g_types[4] = TypeInfo{1, 2, 4, K_R2C, 0, "Real-to-complex Fourier Transform, single precision"};
+  g_types[5] = TypeInfo{1, 2, 8, K_R2C, 0, "Real-to-complex Fourier Transform double precision"};
+  g_types[6] = TypeInfo{2, 1, 4, K_C2R, 0, "Complex-to-real Fourier Transform, single precision"};
+  g_types[7] = TypeInfo{2, 1, 8, K_C2R, 0, "Complex-to-real Fourier Transform, double precision"};
+  g_types[8] = TypeInfo{2, 2, 4, K_C2C_FWD, 0, "Complex-to-complex Fourier Transform, forward, single precision"};
+  g_types[9] = TypeInfo{2, 2, 8, K_C2C_FWD, 0, "Complex-to-complex Fourier Transform, forward, double precision"};
+  g_types[10] = TypeInfo{2, 2, 4, K_C2C_BWD, 0, "Complex-to-complex Fourier Transform, backward, single precision"};
+  g_types[11] = TypeInfo{2, 2, 8, K_C2C_BWD, 0, "Complex-to-complex Fourier Transform, backward, double precision"};
+  // 12..43: DCT1 DST1 DCT2 DST2 DCT3 DST3 DCT4 DST4 x {REAL_S, REAL_D, COMPLEX_S, COMPLEX_D}
+  // (init.C:335-731).  The DCT4 IDs are registered with the DCT1 planners in the reference
+  // (init.C:640, 652, 664, 676), so they compute REDFT00; that registration is kept.
+  static const int fam_kind[8] = {REDFT00, RODFT00, REDFT10, RODFT10, REDFT01, RODFT01, REDFT00, RODFT11};
+  static const char *fam_name[8] = {"DCT1", "DST1", "DCT2", "DST2", "DCT3", "DST3", "DCT4", "DST4"};
+  for (int f = 0; f < 8; f++)
+    for (int v = 0; v < 4; v++) {
+      int id = 12 + 4 * f + v;
+      int dt = v >= 2 ? 2 : 1;
+      g_types[id] = TypeInfo{dt, dt, (v & 1) ? 8 : 4, K_R2R, fam_kind[f], fam_name[f]};
+    }
+}
+
+static void assign_globals() {
+  using namespace p3dfft;
+  int *cpp[44] = {&EMPTY_TYPE_SINGLE, &EMPTY_TYPE_DOUBLE, &EMPTY_TYPE_SINGLE_COMPLEX, &EMPTY_TYPE_DOUBLE_COMPLEX,
+                  &R2CFFT_S, &R2CFFT_D, &C2RFFT_S, &C2RFFT_D, &CFFT_FORWARD_S, &CFFT_FORWARD_D, &CFFT_BACKWARD_S,
+                  &CFFT_BACKWARD_D, &DCT1_REAL_S, &DCT1_REAL_D, &DCT1_COMPLEX_S, &DCT1_COMPLEX_D, &DST1_REAL_S,
+                  &DST1_REAL_D, &DST1_COMPLEX_S, &DST1_COMPLEX_D, &DCT2_REAL_S, &DCT2_REAL_D, &DCT2_COMPLEX_S,
+                  &DCT2_COMPLEX_D, &DST2_REAL_S, &DST2_REAL_D, &DST2_COMPLEX_S, &DST2_COMPLEX_D, &DCT3_REAL_S,
+                  &DCT3_REAL_D, &DCT3_COMPLEX_S, &DCT3_COMPLEX_D, &DST3_REAL_S, &DST3_REAL_D, &DST3_COMPLEX_S,
+                  &DST3_COMPLEX_D, &DCT4_REAL_S, &DCT4_REAL_D, &DCT4_COMPLEX_S, &DCT4_COMPLEX_D, &DST4_REAL_S,
+                  &DST4_REAL_D, &DST4_COMPLEX_S, &DST4_COMPLEX_D};
+  int *c[44] = {&P3DFFT_EMPTY_TYPE_SINGLE, &P3DFFT_EMPTY_TYPE_DOUBLE, &P3DFFT_EMPTY_TYPE_SINGLE_COMPLEX,
+                &P3DFFT_EMPTY_TYPE_DOUBLE_COMPLEX, &P3DFFT_R2CFFT_S, &P3DFFT_R2CFFT_D, &P3DFFT_C2RFFT_S,
+                &P3DFFT_C2RFFT_D, &P3DFFT_CFFT_FORWARD_S, &P3DFFT_CFFT_FORWARD_D, &P3DFFT_CFFT_BACKWARD_S,
+                &P3DFFT_CFFT_BACKWARD_D, &P3DFFT_DCT1_REAL_S, &P3DFFT_DCT1_REAL_D, &P3DFFT_DCT1_COMPLEX_S,
+                &P3DFFT_DCT1_COMPLEX_D, &P3DFFT_DST1_REAL_S, &P3DFFT_DST1_REAL_D, &P3DFFT_DST1_COMPLEX_S,
+                &P3DFFT_DST1_COMPLEX_D, &P3DFFT_DCT2_REAL_S, &P3DFFT_DCT2_REAL_D, &P3DFFT_DCT2_COMPLEX_S,
+                &P3DFFT_DCT2_COMPLEX_D, &P3DFFT_DST2_REAL_S, &P3DFFT_DST2_REAL_D, &P3DFFT_DST2_COMPLEX_S,
+                &P3DFFT_DST2_COMPLEX_D, &P3DFFT_DCT3_REAL_S, &P3DFFT_DCT3_REAL_D, &P3DFFT_DCT3_COMPLEX_S,
+                &P3DFFT_DCT3_COMPLEX_D, &P3DFFT_DST3_REAL_S, &P3DFFT_DST3_REAL_D, &P3DFFT_DST3_COMPLEX_S,
+                &P3DFFT_DST3_COMPLEX_D, &P3DFFT_DCT4_REAL_S, &P3DFFT_DCT4_REAL_D, &P3DFFT_DCT4_COMPLEX_S,
+                &P3DFFT_DCT4_COMPLEX_D, &P3DFFT_DST4_REAL_S, &P3DFFT_DST4_REAL_D, &P3DFFT_DST4_COMPLEX_S,
+                &P3DFFT_DST4_COMPLEX_D};
+  for (int i = 0; i < 44; i++) *cpp[i] = *c[i] = i;
+}
+
+// ------------------------------------------------------------------------------------------
+// runtime state
+struct GridDesc {
+  int gdims[3];
+  int mo[3];
+  int dcs;
+};
+struct Stage {
+  int type;
+  int dim;
+  GridDesc g1, g2;
+};
+struct Buffers {
+  void *scratch[2] = {nullptr, nullptr};
+  size_t scratch_bytes = 0;
+  void *stage_in = nullptr, *stage_out = nullptr;
+  size_t stage_in_bytes = 0, stage_out_bytes = 0;
+  void release() {
+    for (int i = 0; i < 2; i++)
+      if (scratch[i]) cudaFree(scratch[i]);
+    if (stage_in) cudaFree(stage_in);
+    if (stage_out) cudaFree(stage_out);
+    scratch[0] = scratch[1] = stage_in = stage_out = nullptr;
+    scratch_bytes = stage_in_bytes = stage_out_bytes = 0;
+  }
+};
+struct Plan {
+  std::vector<Stage> st;
+  int L[3] = {0, 1, 2};
+  int dt1 = 1, dt2 = 1, prec = 8;
+  GridDesc g1, g2;
+  Buffers buf;
+  bool live = true;
+};
+
+static std::mutex g_mu;
+static std::vector<Plan *> g_plans3, g_plans1;
+struct Type3 {
+  int types[3];
+  int prec;
+};
+static std::vector<Type3> g_types3d;
+struct PGridRec {
+  int pdims[3];
+  MPI_Comm comm;
+  bool live;
+};
+static std::vector<PGridRec> g_pgrids;
+struct DGridRec {
+  GridDesc g;
+  int pgrid;
+  int dmap[3];
+};
+static std::vector<DGridRec> g_dgrids;
+
+static cudaStream_t g_stream = 0;
+static int g_sync = 1;
+static int g_arith = -1;
+static DeviceTables *g_tabs = nullptr;
+static std::atomic<long long> g_kcount(0);
+static bool g_timers_on = false;
+static double g_timer[6] = {0, 0, 0, 0, 0, 0};
+static int g_device_ok = -1;
+
+static bool ensure_device() {
+  if (g_device_ok == 1) return true;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    set_err(E_NO_DEVICE, "no CUDA device is available (%s); this library has no CPU path",
+            e != cudaSuccess ? cudaGetErrorString(e) : "device count 0");
+    return false;
+  }
+  g_device_ok = 1;
+  if (!g_tabs) g_tabs = tables_create();
+  return true;
+}
+
+static int arith_mode() {
+  if (g_arith < 0) {
+    const char *s = getenv("P3DFFT_GB300_FP64_ARITH");
+    g_arith = (s && (s[0] == '1' || s[0] == 'd' || s[0] == 'D')) ? AR_DF : AR_NATIVE;
+  }
+  return g_arith;
+}
+
+static long long elems(const GridDesc &g) { return (long long)g.gdims[0] * g.gdims[1] * g.gdims[2]; }
+
+static void strides(const GridDesc &g, long long s[3]) {
+  for (int i = 0; i < 3; i++) {
+    s[i] = 1;
+    for (int j = 0; j < 3; j++)
+      if (g.mo[j] < g.mo[i]) s[i] *= g.gdims[j];
+  }
+}
+
+static bool valid_mo(const int mo[3]) {
+  int seen = 0;
+  for (int i = 0; i < 3; i++) {
+    if (mo[i] < 0 || mo[i] > 2) return false;
+    seen |= 1 << mo[i];
+  }
+  return seen == 7;
+}
+
+static bool valid_grid(const GridDesc &g) {
+  for (int i = 0; i < 3; i++)
+    if (g.gdims[i] <= 0) return false;
+  return valid_mo(g.mo) && g.dcs >= -1 && g.dcs <= 2;
+}
+
+// ------------------------------------------------------------------------------------------
+// planner (templ.C), specialised to one task on a 1x1x1 processor grid: Pdims == 1 in every
+// dim, ProcGrid::nd == 1 (init.C:1634-1641) and DataGrid::L == {0,1,2} (init.C:1813-1818)
+
+// swap0, templ.C:816-858
+static void swap0(int newmo[3], const int mo[3], int L) {
+  int t[3] = {mo[0], mo[1], mo[2]};
+  if (t[L] == 1) {
+    int j = 0;
+    while (j < 3 && t[j] != 0) j++;
+    t[j] = 1;
+    t[L] = 0;
+  } else if (t[L] == 2) {
+    for (int i = 0; i < 3; i++) t[i] = (t[i] + 1) % 3;
+  }
+  for (int i = 0; i < 3; i++) newmo[i] = t[i];
+}
+
+// excl, templ.C:872-882
+static int excl(int a, int b) {
+  if (a * b == 0) return std::max(a, b) == 1 ? 2 : 1;
+  return 0;
+}
+
+// find_order, templ.C:627-802 (numtasks == 1 branch)
+static bool find_order(const int types[3], const GridDesc &g1, const GridDesc &g2, int L[3]) {
+  L[0] = L[1] = L[2] = -1;
+  bool ok = true;
+  for (int i = 0; i < 3; i++) {
+    const TypeInfo &t = g_types[types[i]];
+    if (t.dt1 < t.dt2) {
+      if (L[0] >= 0) ok = false;
+      else L[0] = i;
+    } else if (t.dt1 > t.dt2) {
+      if (L[2] >= 0) ok = false;
+      else L[2] = i;
+    }
+  }
+  if (L[0] >= 0 && L[2] >= 0) ok = false;
+  if (L[0] < 0) {
+    L[0] = 0;
+    if (L[2] < 0) {
+      if (g1.mo[0] > g1.mo[1]) L[0] = 1;
+    } else if (L[0] == L[2]) {
+      L[0] = 1;
+    }
+  }
+  if (L[2] < 0) {
+    for (int i = 0; i < 3; i++)
+      if (g2.mo[i] == 0) L[2] = i;
+    if (L[2] == L[0]) L[2] = (L[0] + 1) % 3;
+  }
+  L[1] = excl(L[0], L[2]);
+  return ok;
+}
+
+static int empty_type(int dt, int prec) { return dt == 2 ? (prec == 4 ? 2 : 3) : (prec == 4 ? 0 : 1); }
+
+// transform3D ctor stage loop, templ.C:224-420
+static Plan *make_plan3(const int types[3], const GridDesc &g1, const GridDesc &g2) {
+  for (int i = 0; i < 3; i++)
+    if (types[i] < 0 || types[i] >= 44) {
+      set_err(E_BAD_ARG, "transform type %d is undefined", types[i]);
+      return nullptr;
+    }
+  if (!valid_grid(g1) || !valid_grid(g2)) {
+    set_err(E_BAD_ARG, "invalid grid description (dims must be > 0, memory order a permutation of 0,1,2)");
+    return nullptr;
+  }
+  Plan *P = new Plan();
+  P->g1 = g1;
+  P->g2 = g2;
+  if (!find_order(types, g1, g2, P->L)) {
+    set_err(E_PLAN, "transform3D: more than one R2C or C2R 1D transform, or both (templ.C:640-658)");
+    delete P;
+    return nullptr;
+  }
+  const TypeInfo &t0 = g_types[types[P->L[0]]];
+  P->dt1 = t0.dt1;
+  P->prec = t0.prec;
+  int monext[3] = {g1.mo[0], g1.mo[1], g1.mo[2]}, mocurr[3];
+  int gd[3] = {g1.gdims[0], g1.gdims[1], g1.gdims[2]};
+  int dcs = g1.dcs, dt_prev = t0.dt1;
+  for (int s = 0; s < 3; s++) {
+    const int Ls = P->L[s];
+    const TypeInfo &t = g_types[types[Ls]];
+    if (t.prec != P->prec) {
+      set_err(E_PLAN, "transform3D: 1D transform types of different precision");
+      delete P;
+      return nullptr;
+    }
+    if (t.dt1 != dt_prev) {
+      set_err(E_PLAN, "transform3D: datatypes don't match between stages (%d %d)", t.dt1, dt_prev);
+      delete P;
+      return nullptr;
+    }
+    for (int i = 0; i < 3; i++) mocurr[i] = monext[i];
+    Stage st;
+    st.type = types[Ls];
+    st.dim = Ls;
+    st.g1 = GridDesc{{gd[0], gd[1], gd[2]}, {mocurr[0], mocurr[1], mocurr[2]}, dcs};
+    if (t.dt1 < t.dt2) {  // R2C
+      dcs = Ls;
+      gd[dcs] = gd[dcs] / 2 + 1;
+    } else if (t.dt2 < t.dt1) {  // C2R
+      if (dcs < 0) {
+        set_err(E_PLAN, "transform3D: complex-to-real stage but the input grid has no conjugate-symmetric dim");
+        delete P;
+        return nullptr;
+      }
+      gd[dcs] = (gd[dcs] - 1) * 2;
+      dcs = -1;
+    }
+    if (s < 2) {
+      if (t.kind != K_EMPTY) swap0(monext, mocurr, Ls);
+    } else {
+      for (int i = 0; i < 3; i++) monext[i] = g2.mo[i];
+      if (monext[Ls] != 0) swap0(monext, mocurr, Ls);
+    }
+    st.g2 = GridDesc{{gd[0], gd[1], gd[2]}, {monext[0], monext[1], monext[2]}, dcs};
+    P->st.push_back(st);
+    dt_prev = t.dt2;
+  }
+  P->dt2 = dt_prev;
+  for (int i = 0; i < 3; i++)
+    if (gd[i] != g2.gdims[i]) {
+      set_err(E_PLAN, "transform3D: output grid dims (%d %d %d) do not match the transform (%d %d %d)", g2.gdims[0],
+              g2.gdims[1], g2.gdims[2], gd[0], gd[1], gd[2]);
+      delete P;
+      return nullptr;
+    }
+  if (monext[0] != g2.mo[0] || monext[1] != g2.mo[1] || monext[2] != g2.mo[2]) {  // final_seq
+    Stage st;
+    const GridDesc &prev = P->st.back().g2;
+    int td = 0;
+    if (prev.mo[td] != 0 && g2.mo[td] != 0) td = 1;
+    st.type = empty_type(P->dt2, P->prec);
+    st.dim = td;
+    st.g1 = prev;
+    st.g2 = g2;
+    P->st.push_back(st);
+  }
+  return P;
+}
+
+static Plan *make_plan1(int type, const GridDesc &g1, const GridDesc &g2, int d) {
+  if (type < 0 || type >= 44 || d < 0 || d > 2) {
+    set_err(E_BAD_ARG, "transplan: undefined type %d or dimension %d", type, d);
+    return nullptr;
+  }
+  if (!valid_grid(g1) || !valid_grid(g2)) {
+    set_err(E_BAD_ARG, "transplan: invalid grid description");
+    return nullptr;
+  }
+  const TypeInfo &t = g_types[type];
+  int a = (d + 1) % 3, b = (d + 2) % 3;
+  if (g1.gdims[a] != g2.gdims[a] || g1.gdims[b] != g2.gdims[b]) {
+    set_err(E_PLAN, "transplan: grids differ outside the transform dimension");
+    return nullptr;
+  }
+  int n1 = g1.gdims[d], n2 = g2.gdims[d];
+  bool ok = (t.kind == K_R2C) ? (n2 == n1 / 2 + 1) : (t.kind == K_C2R) ? (n1 == n2 / 2 + 1) : (n1 == n2);
+  if (!ok) {
+    set_err(E_PLAN, "transplan: dimension %d sizes %d -> %d do not fit the transform type", d, n1, n2);
+    return nullptr;
+  }
+  Plan *P = new Plan();
+  P->g1 = g1;
+  P->g2 = g2;
+  P->dt1 = t.dt1;
+  P->dt2 = t.dt2;
+  P->prec = t.prec;
+  Stage st;
+  st.type = type;
+  st.dim = d;
+  st.g1 = g1;
+  st.g2 = g2;
+  P->st.push_back(st);
+  return P;
+}
+
+// ------------------------------------------------------------------------------------------
+// executor
+static bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static bool ensure_buf(void **p, size_t *have, size_t need) {
+  if (*have >= need && *p) return true;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  if (cudaMalloc(p, need) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    set_err(E_CUDA, "cudaMalloc of %zu bytes failed", need);
+    return false;
+  }
+  *have = need;
+  return true;
+}
+
+static size_t stage_out_bytes(const Plan *P, const Stage &s) {
+  const TypeInfo &t = g_types[s.type];
+  return (size_t)elems(s.g2) * t.dt2 * P->prec;
+}
+
+struct TimerScope {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int phase;
+  explicit TimerScope(int ph) : phase(ph) {
+    if (!g_timers_on) return;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, g_stream);
+  }
+  ~TimerScope() {
+    if (!g_timers_on || !a) return;
+    cudaEventRecord(b, g_stream);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    g_timer[phase] += ms * 1e-3;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv) {
+  const TypeInfo &t = g_types[s.type];
+  int launched = 0;
+  int rc = E_OK;
+  if (t.kind == K_EMPTY) {
+    bool same = s.g1.mo[0] == s.g2.mo[0] && s.g1.mo[1] == s.g2.mo[1] && s.g1.mo[2] == s.g2.mo[2];
+    size_t bytes = (size_t)elems(s.g1) * t.dt1 * P->prec;
+    TimerScope ts(2);
+    if (same) {
+      if (src != dst && cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, g_stream) != cudaSuccess)
+        rc = E_CUDA;
+    } else {
+      long long s1[3], s2[3];
+      strides(s.g1, s1);
+      strides(s.g2, s2);
+      rc = launch_permute(s.g1.gdims, s1, s2, t.dt1 * P->prec, src, dst, g_stream, &launched);
+    }
+  } else {
+    StageDesc d;
+    d.kind = t.kind;
+    d.r2r = t.r2r;
+    d.prec = P->prec;
+    d.dt1 = t.dt1;
+    d.dt2 = t.dt2;
+    d.L = s.dim;
+    for (int i = 0; i < 3; i++) {
+      d.d1[i] = s.g1.gdims[i];
+      d.d2[i] = s.g2.gdims[i];
+    }
+    strides(s.g1, d.s1);
+    strides(s.g2, d.s2);
+    d.deriv = deriv ? 1 : 0;
+    bool reorder = !(s.g1.mo[0] == s.g2.mo[0] && s.g1.mo[1] == s.g2.mo[1] && s.g1.mo[2] == s.g2.mo[2]);
+    TimerScope ts(deriv ? 3 : (reorder ? 1 : 0));
+    rc = launch_stage(d, src, dst, P->prec == 8 ? arith_mode() : AR_NATIVE, g_stream, g_tabs, &launched);
+  }
+  g_kcount += launched;
+  if (rc != E_OK) {
+    if (rc == E_CUDA) set_err(E_CUDA, "kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    else if (rc == E_TOO_LARGE) set_err(E_TOO_LARGE, "transform length or grid too large for this release");
+    else if (rc == E_UNSUPPORTED) set_err(E_UNSUPPORTED, "unsupported transform size/type combination");
+    else set_err(rc, "invalid stage description");
+  }
+  return rc;
+}
+
+static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW) {
+  if (!ensure_device()) return t_err;
+  if (!in || !out) {
+    set_err(E_BAD_ARG, "null data pointer");
+    return E_BAD_ARG;
+  }
+  (void)OW;  // the GPU path never modifies `in` unless in == out
+  const size_t in_bytes = (size_t)elems(P->g1) * P->dt1 * P->prec;
+  const size_t out_bytes = (size_t)elems(P->g2) * P->dt2 * P->prec;
+  const bool din_dev = is_device_ptr(in), dout_dev = is_device_ptr(out);
+  const void *din = in;
+  void *dout = out;
+  Buffers &B = P->buf;
+  if (!din_dev) {
+    if (!ensure_buf(&B.stage_in, &B.stage_in_bytes, in_bytes)) return E_CUDA;
+    TimerScope ts(4);
+    if (cudaMemcpyAsync(B.stage_in, in, in_bytes, cudaMemcpyHostToDevice, g_stream) != cudaSuccess) {
+      set_err(E_CUDA, "host-to-device copy failed");
+      return E_CUDA;
+    }
+    din = B.stage_in;
+  }
+  if (!dout_dev) {
+    if (!ensure_buf(&B.stage_out, &B.stage_out_bytes, out_bytes)) return E_CUDA;
+    dout = B.stage_out;
+  }
+  const int n = (int)P->st.size();
+  // buffer assignment: consecutive stages never share a buffer and stage 0 never writes `in`
+  size_t need = 0;
+  for (int s = 0; s < n - 1; s++) need = std::max(need, stage_out_bytes(P, P->st[s]));
+  std::vector<void *> dst(n, nullptr);
+  dst[n - 1] = dout;
+  int nscratch_used = 0;
+  for (int s = n - 2; s >= 0; s--) {
+    size_t bytes = stage_out_bytes(P, P->st[s]);
+    void *cand = nullptr;
+    if (dout != dst[s + 1] && bytes <= out_bytes && !(s == 0 && dout == din) && dout != din) cand = dout;
+    if (!cand) {
+      int k = (dst[s + 1] == B.scratch[0] && B.scratch[0]) ? 1 : 0;
+      if (need > B.scratch_bytes || !B.scratch[k]) {
+        // (re)allocate both scratch slots at the common size on first use
+        for (int i = 0; i < 2; i++)
+          if (B.scratch[i] && B.scratch_bytes < need) {
+            cudaFree(B.scratch[i]);
+            B.scratch[i] = nullptr;
+          }
+        size_t have = B.scratch_bytes < need ? 0 : B.scratch_bytes;
+        if (!B.scratch[k]) {
+          if (cudaMalloc(&B.scratch[k], need) != cudaSuccess) {
+            cudaGetLastError();
+            B.scratch[k] = nullptr;
+            set_err(E_CUDA, "cudaMalloc of %zu bytes (stage scratch) failed", need);
+            return E_CUDA;
+          }
+        }
+        B.scratch_bytes = std::max(have, need);
+      }
+      cand = B.scratch[k];
+      nscratch_used++;
+    }
+    dst[s] = cand;
+  }
+  const void *src = din;
+  int rc = E_OK;
+  for (int s = 0; s < n && rc == E_OK; s++) {
+    const Stage &st = P->st[s];
+    bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
+    void *d = dst[s];
+    if (d == src) {  // single-stage in-place call: go through scratch, then copy back
+      size_t bytes = stage_out_bytes(P, st);
+      if (!ensure_buf(&B.scratch[0], &B.scratch_bytes, std::max(bytes, B.scratch_bytes))) return E_CUDA;
+      rc = run_stage(P, st, src, B.scratch[0], deriv);
+      if (rc == E_OK && cudaMemcpyAsync(d, B.scratch[0], bytes, cudaMemcpyDeviceToDevice, g_stream) != cudaSuccess)
+        rc = E_CUDA;
+    } else {
+      rc = run_stage(P, st, src, d, deriv);
+    }
+    src = d;
+  }
+  if (rc != E_OK) return rc;
+  if (!dout_dev) {
+    TimerScope ts(5);
+    if (cudaMemcpyAsync(out, dout, out_bytes, cudaMemcpyDeviceToHost, g_stream) != cudaSuccess) {
+      set_err(E_CUDA, "device-to-host copy failed");
+      return E_CUDA;
+    }
+  }
+  if (g_sync || !din_dev || !dout_dev) {
+    cudaError_t e = cudaStreamSynchronize(g_stream);
+    if (e != cudaSuccess) {
+      set_err(E_CUDA, "stream synchronize failed: %s", cudaGetErrorString(e));
+      return E_CUDA;
+    }
+  }
+  return E_OK;
+}
+
+static Plan *get_plan(std::vector<Plan *> &v, int h) {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (h < 0 || h >= (int)v.size() || !v[h]) return nullptr;
+  return v[h];
+}
+
+static int store_plan(std::vector<Plan *> &v, Plan *P) {
+  std::lock_guard<std::mutex> g(g_mu);
+  v.push_back(P);
+  return (int)v.size() - 1;
+}
+
+static void ensure_setup() {
+  if (!g_setup_done) {
+    build_registry();
+    assign_globals();
+    g_setup_done = true;
+  }
+}
+
+}  // namespace p3d
+
+using namespace p3d;
+
+// ==========================================================================================
+// GB300 extension C ABI (p3dfft_gb300.h)
+extern "C" {
+
+int p3dfft_last_error(void) { return t_err; }
+const char *p3dfft_last_error_string(void) { return t_msg; }
+void p3dfft_clear_error(void) {
+  t_err = E_OK;
+  snprintf(t_msg, sizeof(t_msg), "no error");
+}
+void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
+void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
+void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }
+int p3dfft_gb300_get_fp64_arith(void) { return arith_mode(); }
+const char *p3dfft_gb300_version(void) { return "p3dfft-gb300 0.1 (sm_103a)"; }
+
+int p3dfft_gb300_plan3d(const int types[3], const int gdims1[3], const int mo1[3], int dcs1, const int gdims2[3],
+                        const int mo2[3], int dcs2) {
+  ensure_setup();
+  GridDesc g1{{gdims1[0], gdims1[1], gdims1[2]}, {mo1[0], mo1[1], mo1[2]}, dcs1};
+  GridDesc g2{{gdims2[0], gdims2[1], gdims2[2]}, {mo2[0], mo2[1], mo2[2]}, dcs2};
+  Plan *P = make_plan3(types, g1, g2);
+  if (!P) return -1;
+  return store_plan(g_plans3, P);
+}
+
+int p3dfft_gb300_exec3d(int plan, const void *in, void *out, int idir, int OW) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) {
+    set_err(E_BAD_ARG, "invalid 3D plan handle %d", plan);
+    return E_BAD_ARG;
+  }
+  if (idir > 2) {
+    set_err(E_BAD_ARG, "derivative direction %d out of range", idir);
+    return E_BAD_ARG;
+  }
+  return exec_plan(P, in, out, idir, OW);
+}
+
+int p3dfft_gb300_destroy3d(int plan) {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (plan < 0 || plan >= (int)g_plans3.size() || !g_plans3[plan]) return E_BAD_ARG;
+  g_plans3[plan]->buf.release();
+  delete g_plans3[plan];
+  g_plans3[plan] = nullptr;
+  return E_OK;
+}
+
+int p3dfft_gb300_plan3d_types(int plan, int *dt1, int *dt2, int *prec) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) return E_BAD_ARG;
+  *dt1 = P->dt1;
+  *dt2 = P->dt2;
+  *prec = P->prec;
+  return E_OK;
+}
+
+static int stages_info(Plan *P, int *info, int max_stages) {
+  int n = (int)P->st.size();
+  for (int s = 0; s < n && s < max_stages; s++) {
+    const Stage &st = P->st[s];
+    int *q = info + 16 * s;
+    q[0] = st.type;
+    q[1] = st.dim;
+    for (int i = 0; i < 3; i++) {
+      q[2 + i] = st.g1.gdims[i];
+      q[5 + i] = st.g1.mo[i];
+      q[9 + i] = st.g2.gdims[i];
+      q[12 + i] = st.g2.mo[i];
+    }
+    q[8] = st.g1.dcs;
+    q[15] = st.g2.dcs;
+  }
+  return n;
+}
+
+int p3dfft_gb300_plan3d_stages(int plan, int *info, int max_stages) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) return -1;
+  return stages_info(P, info, max_stages);
+}
+
+int p3dfft_gb300_plan1d(int type, const int gdims1[3], const int mo1[3], int dcs1, const int gdims2[3],
+                        const int mo2[3], int dcs2, int dim) {
+  ensure_setup();
+  GridDesc g1{{gdims1[0], gdims1[1], gdims1[2]}, {mo1[0], mo1[1], mo1[2]}, dcs1};
+  GridDesc g2{{gdims2[0], gdims2[1], gdims2[2]}, {mo2[0], mo2[1], mo2[2]}, dcs2};
+  Plan *P = make_plan1(type, g1, g2, dim);
+  if (!P) return -1;
+  return store_plan(g_plans1, P);
+}
+
+int p3dfft_gb300_exec1d(int plan, const void *in, void *out, int OW) {
+  Plan *P = get_plan(g_plans1, plan);
+  if (!P) {
+    set_err(E_BAD_ARG, "invalid 1D plan handle %d", plan);
+    return E_BAD_ARG;
+  }
+  return exec_plan(P, in, out, -1, OW);
+}
+
+int p3dfft_gb300_destroy1d(int plan) {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (plan < 0 || plan >= (int)g_plans1.size() || !g_plans1[plan]) return E_BAD_ARG;
+  g_plans1[plan]->buf.release();
+  delete g_plans1[plan];
+  g_plans1[plan] = nullptr;
+  return E_OK;
+}
+
+int p3dfft_gb300_compute_deriv(int prec, const void *in, void *out, const int gdims[3], const int mo[3], int dcs,
+                               int idir) {
+  ensure_setup();
+  if (!ensure_device()) return t_err;
+  GridDesc g{{gdims[0], gdims[1], gdims[2]}, {mo[0], mo[1], mo[2]}, dcs};
+  if (!valid_grid(g) || idir < 0 || idir > 2 || (prec != 4 && prec != 8) || !in || !out) {
+    set_err(E_BAD_ARG, "compute_deriv: invalid arguments");
+    return E_BAD_ARG;
+  }
+  size_t bytes = (size_t)elems(g) * 2 * prec;
+  long long s[3];
+  strides(g, s);
+  // g = (N-1)*2 along the conjugate-symmetric dim, else N (deriv.C:95-99)
+  int gg = (dcs == idir) ? (gdims[idir] - 1) * 2 : gdims[idir];
+  bool hin = !is_device_ptr(in), hout = !is_device_ptr(out);
+  static thread_local Buffers B;
+  const void *din = in;
+  void *dout = out;
+  if (hin) {
+    if (!ensure_buf(&B.stage_in, &B.stage_in_bytes, bytes)) return E_CUDA;
+    cudaMemcpyAsync(B.stage_in, in, bytes, cudaMemcpyHostToDevice, g_stream);
+    din = B.stage_in;
+  }
+  if (hout) {
+    if (!ensure_buf(&B.stage_out, &B.stage_out_bytes, bytes)) return E_CUDA;
+    dout = B.stage_out;
+  }
+  int launched = 0;
+  int rc = launch_deriv(prec, g.gdims, s, idir, gg, din, dout, g_stream, &launched);
+  g_kcount += launched;
+  if (rc != E_OK) {
+    set_err(rc, "compute_deriv launch failed");
+    return rc;
+  }
+  if (hout) cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, g_stream);
+  if (g_sync || hin || hout) {
+    if (cudaStreamSynchronize(g_stream) != cudaSuccess) {
+      set_err(E_CUDA, "compute_deriv: synchronize failed");
+      return E_CUDA;
+    }
+  }
+  return E_OK;
+}
+
+long long p3dfft_gb300_kernel_count(void) { return g_kcount.load(); }
+void p3dfft_gb300_reset_kernel_count(void) { g_kcount = 0; }
+void p3dfft_gb300_enable_timers(int on) { g_timers_on = on != 0; }
+double p3dfft_gb300_timer(int phase) { return (phase >= 0 && phase < 6) ? g_timer[phase] : 0.0; }
+void p3dfft_gb300_reset_timers(void) {
+  for (double &t : g_timer) t = 0;
+}
+void *p3dfft_gb300_device_alloc(long long bytes) {
+  if (!ensure_device()) return nullptr;
+  void *p = nullptr;
+  if (cudaMalloc(&p, (size_t)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    set_err(E_CUDA, "device allocation of %lld bytes failed", bytes);
+    return nullptr;
+  }
+  return p;
+}
+void p3dfft_gb300_device_free(void *p) {
+  if (p) cudaFree(p);
+}
+int p3dfft_gb300_memcpy_h2d(void *dst, const void *src, long long bytes) {
+  return cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyHostToDevice) == cudaSuccess ? E_OK : E_CUDA;
+}
+int p3dfft_gb300_memcpy_d2h(void *dst, const void *src, long long bytes) {
+  return cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? E_OK : E_CUDA;
+}
+int p3dfft_gb300_synchronize(void) { return cudaStreamSynchronize(g_stream) == cudaSuccess ? E_OK : E_CUDA; }
+
+// ==========================================================================================
+// Reference C ABI (Cwrap.h, build/wrap.C:85-571)
+
+void p3dfft_setup() { ensure_setup(); }
+
+void p3dfft_cleanup() {
+  std::lock_guard<std::mutex> g(g_mu);
+  for (auto *P : g_plans3)
+    if (P) {
+      P->buf.release();
+      delete P;
+    }
+  for (auto *P : g_plans1)
+    if (P) {
+      P->buf.release();
+      delete P;
+    }
+  g_plans3.clear();
+  g_plans1.clear();
+  g_types3d.clear();
+  g_dgrids.clear();
+  g_pgrids.clear();
+  if (g_tabs) {
+    tables_destroy(g_tabs);
+    g_tabs = nullptr;
+    g_device_ok = -1;
+  }
+}
+
+Type3D p3dfft_init_3Dtype(int types[3]) {
+  ensure_setup();
+  Type3 t;
+  for (int i = 0; i < 3; i++) t.types[i] = types[i];
+  t.prec = (types[0] >= 0 && types[0] < 44) ? g_types[types[0]].prec : 0;
+  std::lock_guard<std::mutex> g(g_mu);
+  g_types3d.push_back(t);
+  return (int)g_types3d.size() - 1;
+}
+
+int p3dfft_init_proc_grid(int pdims[3], MPI_Comm comm) {
+  ensure_setup();
+  if (pdims[0] * pdims[1] * pdims[2] != 1)
+    set_err(E_UNSUPPORTED, "processor grid %d x %d x %d: only the 1x1x1 grid of one GPU is supported", pdims[0],
+            pdims[1], pdims[2]);
+  std::lock_guard<std::mutex> g(g_mu);
+  g_pgrids.push_back(PGridRec{{pdims[0], pdims[1], pdims[2]}, comm, true});
+  return (int)g_pgrids.size() - 1;
+}
+
+static int pgrid_nd(const int pd[3]) {
+  int nd = 0;
+  for (int i = 0; i < 3; i++)
+    if (pd[i] > 1) nd++;
+  return nd == 0 ? 1 : nd;
+}
+
+Grid *p3dfft_init_data_grid(int gdims[3], int dim_conj_sym, int pgrid_id, int dmap[3], int mem_order[3]) {
+  ensure_setup();
+  PGridRec pg;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (pgrid_id < 0 || pgrid_id >= (int)g_pgrids.size()) {
+      set_err(E_BAD_ARG, "p3dfft_init_data_grid: invalid processor grid %d", pgrid_id);
+      return nullptr;
+    }
+    pg = g_pgrids[pgrid_id];
+  }
+  Grid *G = new Grid;
+  memset(G, 0, sizeof(*G));
+  G->numtasks = 1;
+  G->taskid = 0;
+  G->nd = pgrid_nd(pg.pdims);
+  G->pgrid = pgrid_id;
+  G->dim_conj_sym = dim_conj_sym;
+  for (int i = 0; i < 3; i++) {
+    G->Gdims[i] = gdims[i];
+    G->Ldims[i] = gdims[i];
+    G->MemOrder[i] = mem_order[i];
+    G->Dmap[i] = dmap[i];
+    G->ProcDims[i] = pg.pdims[i];
+    G->grid_id[i] = 0;
+    G->GlobStart[i] = 0;
+  }
+  G->mpi_comm_glob = pg.comm;
+  return G;
+}
+
+void p3dfft_free_data_grid(Grid *gr) { delete gr; }
+
+void p3dfft_free_proc_grid(int pgrid_id) {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (pgrid_id >= 0 && pgrid_id < (int)g_pgrids.size()) g_pgrids[pgrid_id].live = false;
+}
+
+void p3dfft_inv_mo(int mo[3], int imo[3]) {
+  for (int i = 0; i < 3; i++) imo[mo[i]] = i;
+}
+
+int find_grid(int gdims[3], int pgrid, int *dmap, int mem_order[3]) {
+  std::lock_guard<std::mutex> g(g_mu);
+  for (size_t i = 0; i < g_dgrids.size(); i++) {
+    const DGridRec &r = g_dgrids[i];
+    if (r.pgrid == pgrid && !memcmp(r.g.gdims, gdims, 3 * sizeof(int)) && !memcmp(r.dmap, dmap, 3 * sizeof(int)) &&
+        !memcmp(r.g.mo, mem_order, 3 * sizeof(int)))
+      return (int)i;
+  }
+  return -1;
+}
+
+Plan3D p3dfft_plan_3Dtrans(Grid *g1, Grid *g2, Type3D tp) {
+  ensure_setup();
+  Type3 t;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (tp < 0 || tp >= (int)g_types3d.size()) {
+      set_err(E_BAD_ARG, "p3dfft_plan_3Dtrans: invalid 3D type %d", tp);
+      return -1;
+    }
+    t = g_types3d[tp];
+  }
+  if (!g1 || !g2) {
+    set_err(E_BAD_ARG, "p3dfft_plan_3Dtrans: null grid");
+    return -1;
+  }
+  return p3dfft_gb300_plan3d(t.types, g1->Gdims, g1->MemOrder, g1->dim_conj_sym, g2->Gdims, g2->MemOrder,
+                             g2->dim_conj_sym);
+}
+
+int p3dfft_plan_1Dtrans(Grid *g1, Grid *g2, int type, int d) {
+  if (!g1 || !g2) {
+    set_err(E_BAD_ARG, "p3dfft_plan_1Dtrans: null grid");
+    return -1;
+  }
+  return p3dfft_gb300_plan1d(type, g1->Gdims, g1->MemOrder, g1->dim_conj_sym, g2->Gdims, g2->MemOrder,
+                             g2->dim_conj_sym, d);
+}
+
+static void exec3_checked(Plan3D plan, const void *in, void *out, int idir, int OW, int prec, const char *fn) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) {
+    set_err(E_BAD_ARG, "%s: invalid plan %d", fn, plan);
+    return;
+  }
+  if (P->prec != prec) {  // the reference calls MPI_Abort here (wrap.C:377-380)
+    set_err(E_BAD_ARG, "%s: expecting %s precision data", fn, prec == 8 ? "double" : "single");
+    return;
+  }
+  exec_plan(P, in, out, idir, OW);
+}
+
+void p3dfft_exec_3Dtrans_double(Plan3D plan, double *in, double *out, int OW) {
+  exec3_checked(plan, in, out, -1, OW, 8, "p3dfft_exec_3Dtrans_double");
+}
+void p3dfft_exec_3Dtrans_single(Plan3D plan, float *in, float *out, int OW) {
+  exec3_checked(plan, in, out, -1, OW, 4, "p3dfft_exec_3Dtrans_single");
+}
+void p3dfft_exec_3Dderiv_double(Plan3D plan, double *in, double *out, int idir, int OW) {
+  exec3_checked(plan, in, out, idir, OW, 8, "p3dfft_exec_3Dderiv_double");
+}
+void p3dfft_exec_3Dderiv_single(Plan3D plan, float *in, float *out, int idir, int OW) {
+  exec3_checked(plan, in, out, idir, OW, 4, "p3dfft_exec_3Dderiv_single");
+}
+void p3dfft_exec_1Dtrans_double(int plan, double *in, double *out, int OW) { p3dfft_gb300_exec1d(plan, in, out, OW); }
+void p3dfft_exec_1Dtrans_single(int plan, float *in, float *out, int OW) { p3dfft_gb300_exec1d(plan, in, out, OW); }
+
+void p3dfft_compute_deriv_single(float *in, float *out, Grid *g, int idir) {
+  p3dfft_gb300_compute_deriv(4, in, out, g->Gdims, g->MemOrder, g->dim_conj_sym, idir);
+}
+void p3dfft_compute_deriv_double(double *in, double *out, Grid *g, int idir) {
+  p3dfft_gb300_compute_deriv(8, in, out, g->Gdims, g->MemOrder, g->dim_conj_sym, idir);
+}
+
+// ---- Fortran glue (build/wrap.C:575-792): everything by reference, idir 1-based ----
+void p3dfft_init_3Dtype_f(int *type, int types[3]) { *type = p3dfft_init_3Dtype(types); }
+
+int p3dfft_init_proc_grid_f(int *pdims, int *mpicomm) { return p3dfft_init_proc_grid(pdims, (MPI_Comm)(*mpicomm)); }
+
+void p3dfft_init_data_grid_f(int *mygrid, int *ldims, int *glob_start, int *gdims, int *dim_conj_sym, int *pgrid_id,
+                             int *dmap, int *mem_order) {
+  ensure_setup();
+  int num = find_grid(gdims, *pgrid_id, dmap, mem_order);
+  if (num < 0) {
+    DGridRec r;
+    for (int i = 0; i < 3; i++) {
+      r.g.gdims[i] = gdims[i];
+      r.g.mo[i] = mem_order[i];
+      r.dmap[i] = dmap[i];
+    }
+    r.g.dcs = *dim_conj_sym;
+    r.pgrid = *pgrid_id;
+    std::lock_guard<std::mutex> g(g_mu);
+    g_dgrids.push_back(r);
+    num = (int)g_dgrids.size() - 1;
+  }
+  for (int i = 0; i < 3; i++) {
+    ldims[i] = gdims[i];
+    glob_start[i] = 0;
+  }
+  *mygrid = num;
+}
+
+static bool dgrid(int h, GridDesc *g) {
+  std::lock_guard<std::mutex> l(g_mu);
+  if (h < 0 || h >= (int)g_dgrids.size()) return false;
+  *g = g_dgrids[h].g;
+  return true;
+}
+
+void p3dfft_plan_3Dtrans_f(int *plan, int *Fgr1, int *Fgr2, Type3D *tp) {
+  GridDesc a, b;
+  Type3 t;
+  *plan = -1;
+  if (!dgrid(*Fgr1, &a) || !dgrid(*Fgr2, &b)) {
+    set_err(E_BAD_ARG, "p3dfft_plan_3Dtrans_f: invalid grid handle");
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (*tp < 0 || *tp >= (int)g_types3d.size()) {
+      set_err(E_BAD_ARG, "p3dfft_plan_3Dtrans_f: invalid type");
+      return;
+    }
+    t = g_types3d[*tp];
+  }
+  *plan = p3dfft_gb300_plan3d(t.types, a.gdims, a.mo, a.dcs, b.gdims, b.mo, b.dcs);
+}
+
+void p3dfft_plan_1Dtrans_f(int *plan, int *Fgr1, int *Fgr2, int *type, int *d) {
+  GridDesc a, b;
+  *plan = -1;
+  if (!dgrid(*Fgr1, &a) || !dgrid(*Fgr2, &b)) {
+    set_err(E_BAD_ARG, "p3dfft_plan_1Dtrans_f: invalid grid handle");
+    return;
+  }
+  *plan = p3dfft_gb300_plan1d(*type, a.gdims, a.mo, a.dcs, b.gdims, b.mo, b.dcs, *d);
+}
+
+void p3dfft_exec_3Dtrans_double_f(Plan3D *plan, double *in, double *out, int *OW) {
+  p3dfft_exec_3Dtrans_double(*plan, in, out, *OW);
+}
+void p3dfft_exec_3Dtrans_single_f(Plan3D *plan, float *in, float *out, int *OW) {
+  p3dfft_exec_3Dtrans_single(*plan, in, out, *OW);
+}
+void p3dfft_exec_3Dderiv_double_f(Plan3D *plan, double *in, double *out, int *idir, int *OW) {
+  p3dfft_exec_3Dderiv_double(*plan, in, out, *idir - 1, *OW);
+}
+void p3dfft_exec_3Dderiv_single_f(Plan3D *plan, float *in, float *out, int *idir, int *OW) {
+  p3dfft_exec_3Dderiv_single(*plan, in, out, *idir - 1, *OW);
+}
+void p3dfft_exec_1Dtrans_double_f(int *plan, double *in, double *out, int *OW) {
+  p3dfft_exec_1Dtrans_double(*plan, in, out, *OW);
+}
+void p3dfft_exec_1Dtrans_single_f(int *plan, float *in, float *out, int *OW) {
+  p3dfft_exec_1Dtrans_single(*plan, in, out, *OW);
+}
+void p3dfft_compute_deriv_single_f(float *in, float *out, int *igrid, int *idir) {
+  GridDesc g;
+  if (!dgrid(*igrid, &g)) {
+    set_err(E_BAD_ARG, "p3dfft_compute_deriv_single_f: invalid grid handle");
+    return;
+  }
+  p3dfft_gb300_compute_deriv(4, in, out, g.gdims, g.mo, g.dcs, *idir - 1);
+}
+void p3dfft_compute_deriv_double_f(double *in, double *out, int *igrid, int *idir) {
+  GridDesc g;
+  if (!dgrid(*igrid, &g)) {
+    set_err(E_BAD_ARG, "p3dfft_compute_deriv_double_f: invalid grid handle");
+    return;
+  }
+  p3dfft_gb300_compute_deriv(8, in, out, g.gdims, g.mo, g.dcs, *idir - 1);
+}
+
+}  // extern "C"
+
+// ==========================================================================================
+// C++ API objects (reference include/p3dfft.h)
+namespace p3dfft {
+
+void setup() { p3dfft_setup(); }
+void cleanup() { p3dfft_cleanup(); }
+void inv_mo(int mo[3], int imo[3]) { p3dfft_inv_mo(mo, imo); }
+
+// rel_change, build/exec.C:2270-2296: relative permutation between two inverse memory orders
+void rel_change(int *imo1, int *imo2, int *m) {
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++)
+      if (imo1[j] == imo2[i]) m[j] = i;
+}
+
+ProcGrid::ProcGrid(int procdims[3], MPI_Comm mpi_comm_init) {
+  p3d::ensure_setup();
+  nd = 0;
+  for (int i = 0; i < 3; i++) {
+    ProcDims[i] = procdims[i];
+    if (procdims[i] > 1) nd++;
+    grid_id_cart[i] = 0;
+    mpicomm[i] = mpi_comm_init;
+  }
+  if (nd == 0) nd = 1;
+  taskid = 0;
+  numtasks = 1;
+  mpi_comm_glob = mpi_comm_init;
+  mpi_comm_cart = mpi_comm_init;
+  if (procdims[0] * procdims[1] * procdims[2] != 1)
+    p3d::set_err(p3d::E_UNSUPPORTED, "ProcGrid %d x %d x %d: only the 1x1x1 grid of one GPU is supported",
+                 procdims[0], procdims[1], procdims[2]);
+}
+ProcGrid::ProcGrid(const ProcGrid &r) {
+  taskid = r.taskid;
+  numtasks = r.numtasks;
+  nd = r.nd;
+  mpi_comm_glob = r.mpi_comm_glob;
+  mpi_comm_cart = r.mpi_comm_cart;
+  for (int i = 0; i < 3; i++) {
+    ProcDims[i] = r.ProcDims[i];
+    grid_id_cart[i] = r.grid_id_cart[i];
+    mpicomm[i] = r.mpicomm[i];
+  }
+}
+ProcGrid::~ProcGrid() {}
+bool ProcGrid::operator==(const ProcGrid &P) const {
+  if (nd != P.nd || taskid != P.taskid || numtasks != P.numtasks) return false;
+  for (int i = 0; i < 3; i++)
+    if (ProcDims[i] != P.ProcDims[i] || grid_id_cart[i] != P.grid_id_cart[i]) return false;
+  return true;
+}
+
+// DataGrid ctor + InitPencil (init.C:1699-1729, 1806-1863) on one task: every dim is local
+DataGrid::DataGrid(int *gdims_, int dim_conj_sym_, ProcGrid *pgrid, int *dmap, int *mem_order) {
+  dim_conj_sym = dim_conj_sym_;
+  Pgrid = pgrid;
+  nd = pgrid ? pgrid->nd : 1;
+  int ploc = 0, n = 0;
+  for (int i = 0; i < 3; i++) {
+    Gdims[i] = gdims_[i];
+    Dmap[i] = dmap[i];
+    Pdims[i] = pgrid ? pgrid->ProcDims[dmap[i]] : 1;
+    MemOrder[i] = mem_order[i];
+    grid_id[i] = 0;
+    Ldims[i] = Gdims[i];
+    GlobStart[i] = 0;
+    D[i] = -1;
+    L[i] = -1;
+  }
+  for (int k = 0; k < 3; k++) {
+    if (Pdims[k] == 1) L[ploc++] = k;
+    else D[n++] = k;
+  }
+  is_set = true;
+}
+DataGrid::DataGrid(const DataGrid &r) { memcpy((void *)this, (const void *)&r, sizeof(DataGrid)); }
+DataGrid::~DataGrid() {}
+void DataGrid::set_gdims(int gdims[3]) {
+  for (int i = 0; i < 3; i++) {
+    Gdims[i] = gdims[i];
+    Ldims[i] = gdims[i];
+  }
+}
+
+trans_type3D::trans_type3D(int types_IDs[3]) {
+  p3d::ensure_setup();
+  name = nullptr;
+  is_set = true;
+  for (int i = 0; i < 3; i++) {
+    if (types_IDs[i] < 0 || types_IDs[i] >= 44) {
+      cout << "Error in init trans_plan: type is undefined " << types_IDs[i] << endl;
+      is_set = false;
+    }
+    types[i] = types_IDs[i];
+  }
+  prec = is_set ? p3d::g_types[types[0]].prec : 0;
+}
+trans_type3D::trans_type3D(const trans_type3D &r) {
+  name = nullptr;
+  is_set = r.is_set;
+  prec = r.prec;
+  for (int i = 0; i < 3; i++) types[i] = r.types[i];
+}
+trans_type3D::~trans_type3D() {}
+
+void timer::init() {
+  p3dfft_gb300_reset_timers();
+  p3dfft_gb300_enable_timers(1);
+  reorder_deriv = reorder_trans = reorder_out = reorder_in = trans_exec = trans_deriv = 0;
+  packsend = packsend_trans = packsend_deriv = unpackrecv = alltoall = 0;
+}
+void timer::print(MPI_Comm) {
+  trans_exec = p3dfft_gb300_timer(0);
+  reorder_trans = p3dfft_gb300_timer(1);
+  reorder_out = p3dfft_gb300_timer(2);
+  trans_deriv = p3dfft_gb300_timer(3);
+  printf("P3DFFT++ (GB300) timers (device seconds): trans_exec=%lg reorder_trans=%lg reorder_out=%lg "
+         "trans_deriv=%lg h2d=%lg d2h=%lg\n",
+         trans_exec, reorder_trans, reorder_out, trans_deriv, p3dfft_gb300_timer(4), p3dfft_gb300_timer(5));
+}
+
+}  // namespace p3dfft

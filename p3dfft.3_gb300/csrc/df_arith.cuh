@@ -1,0 +1,145 @@
+// Float-float ("double-float") arithmetic on the FP32 pipe, used for FP64 data on GB300 where
+// native DFMA issues at under 2 instructions per SM per clock versus ~128 for FFMA.
+//
+// A value is hi + lo with |lo| <= ulp(hi)/2 after normalisation, giving a ~48-bit significand.
+// The error-free transformations are the classical ones (Knuth TwoSum, Dekker/FMA TwoProd,
+// FastTwoSum); no CUDA math-library routine is involved.
+//
+// Conversions to and from IEEE double use integer bit manipulation only, so that no
+// instruction is issued to the FP64 pipe.  Supported magnitude range: 2^-100 <= |x| < 2^126
+// (values below are flushed to zero, values above saturate to infinity).
+#pragma once
+#include <cstdint>
+
+namespace p3d {
+
+struct __align__(8) ff {
+  float hi, lo;
+};
+struct __align__(16) cff {
+  ff x, y;
+};
+
+// 1/sqrt(2) = FF_RSQRT2_HI + FF_RSQRT2_LO
+#define FF_RSQRT2_HI __int_as_float(0x3f3504f3)
+#define FF_RSQRT2_LO __int_as_float(0x324fe77a)
+
+__device__ __forceinline__ ff ff_fast2sum(float s, float e) {
+  float h = s + e;
+  return ff{h, e - (h - s)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  return ff_fast2sum(s, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ ff ff_half(ff a) { return ff{a.hi * 0.5f, a.lo * 0.5f}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  float p = a.hi * b.hi;
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return ff_fast2sum(p, e);
+}
+__device__ __forceinline__ ff ff_mul_const(ff a, float chi, float clo) { return ff_mul(a, ff{chi, clo}); }
+__device__ __forceinline__ ff ff_mul_int(ff a, int k) {
+  float kf = (float)k;  // exact for |k| < 2^24
+  float p = a.hi * kf;
+  float e = __fmaf_rn(a.hi, kf, -p);
+  e = __fmaf_rn(a.lo, kf, e);
+  return ff_fast2sum(p, e);
+}
+// a.x*b.x - a.y*b.y (+i ...) with one TwoSum per component
+__device__ __forceinline__ cff cff_mul(cff a, cff b) {
+  cff r;
+  {
+    float p1 = a.x.hi * b.x.hi, e1 = __fmaf_rn(a.x.hi, b.x.hi, -p1);
+    float p2 = -a.y.hi * b.y.hi, e2 = __fmaf_rn(-a.y.hi, b.y.hi, -p2);
+    float s = p1 + p2, bb = s - p1, e3 = (p1 - (s - bb)) + (p2 - bb);
+    float lo = (e1 + e2) + e3;
+    lo = __fmaf_rn(a.x.hi, b.x.lo, lo);
+    lo = __fmaf_rn(a.x.lo, b.x.hi, lo);
+    lo = __fmaf_rn(-a.y.hi, b.y.lo, lo);
+    lo = __fmaf_rn(-a.y.lo, b.y.hi, lo);
+    r.x = ff_fast2sum(s, lo);
+  }
+  {
+    float p1 = a.x.hi * b.y.hi, e1 = __fmaf_rn(a.x.hi, b.y.hi, -p1);
+    float p2 = a.y.hi * b.x.hi, e2 = __fmaf_rn(a.y.hi, b.x.hi, -p2);
+    float s = p1 + p2, bb = s - p1, e3 = (p1 - (s - bb)) + (p2 - bb);
+    float lo = (e1 + e2) + e3;
+    lo = __fmaf_rn(a.x.hi, b.y.lo, lo);
+    lo = __fmaf_rn(a.x.lo, b.y.hi, lo);
+    lo = __fmaf_rn(a.y.hi, b.x.lo, lo);
+    lo = __fmaf_rn(a.y.lo, b.x.hi, lo);
+    r.y = ff_fast2sum(s, lo);
+  }
+  return r;
+}
+
+// IEEE double bits -> float-float (truncating split of the 53-bit significand into 24 + 24 bits)
+__device__ __forceinline__ ff ff_from_double_bits(long long bits) {
+  const unsigned long long b = (unsigned long long)bits;
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const int E = (int)((b >> 52) & 0x7ff);
+  const int e = E - 1023;
+  if (e < -100) return ff{__int_as_float(sign), 0.f};
+  if (e > 127) return ff{__int_as_float(sign | 0x7f800000u), 0.f};
+  const unsigned long long m = b & 0xfffffffffffffull;
+  const unsigned int hib = sign | ((unsigned int)(e + 127) << 23) | (unsigned int)(m >> 29);
+  const unsigned int r = (unsigned int)(m & 0x1fffffffu);  // 29 bits below hi, weight 2^(e-52)
+  float lo = 0.f;
+  if (r) {
+    const int lz = __clz(r) - 3;  // leading zeros inside the 29-bit field
+    const unsigned int nrm = r << lz;  // leading one at bit 28
+    const int el = e - 24 - lz;        // exponent of that leading one
+    if (el >= -126) lo = __int_as_float(sign | ((unsigned int)(el + 127) << 23) | ((nrm >> 5) & 0x7fffffu));
+  }
+  return ff{__int_as_float(hib), lo};
+}
+
+// float (normal or zero) bits -> double bits
+__device__ __forceinline__ long long f_to_double_bits(float f) {
+  unsigned int u = __float_as_uint(f);
+  unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  unsigned int E = (u >> 23) & 0xff;
+  if (E == 0) return (long long)s;
+  if (E == 0xff) return (long long)(s | 0x7ff0000000000000ull | ((unsigned long long)(u & 0x7fffff) << 29));
+  return (long long)(s | ((unsigned long long)(E - 127 + 1023) << 52) | ((unsigned long long)(u & 0x7fffff) << 29));
+}
+
+// float-float -> IEEE double bits (hi + lo, truncated to 53 bits).  Requires a normalised pair.
+__device__ __forceinline__ long long ff_to_double_bits(ff v) {
+  const unsigned int uh = __float_as_uint(v.hi);
+  const unsigned int Eh = (uh >> 23) & 0xff;
+  if (Eh == 0 || Eh == 0xff) return f_to_double_bits(v.hi);
+  const unsigned int ul = __float_as_uint(v.lo);
+  const unsigned int El = (ul >> 23) & 0xff;
+  // significand of hi in units of 2^(eh-52): (2^23 | mant) << 29
+  long long S = (long long)((0x800000u | (uh & 0x7fffffu))) << 29;
+  if (El != 0) {
+    long long ml = (long long)(0x800000u | (ul & 0x7fffffu));
+    int sh = (int)El - (int)Eh + 29;  // lo = ml * 2^(el-23); in units 2^(eh-52): shift el-eh+29
+    long long add = sh >= 0 ? (sh < 40 ? (ml << sh) : 0) : (sh > -32 ? (ml >> (-sh)) : 0);
+    if ((uh ^ ul) & 0x80000000u) S -= add;
+    else S += add;
+  }
+  int eh = (int)Eh - 127;
+  // renormalise to [2^52, 2^53)
+  if (S >= (1ll << 53)) {
+    S >>= 1;
+    eh += 1;
+  }
+  while (S < (1ll << 52) && S > 0) {
+    S <<= 1;
+    eh -= 1;
+  }
+  const unsigned long long sign = (unsigned long long)(uh & 0x80000000u) << 32;
+  return (long long)(sign | ((unsigned long long)(eh + 1023) << 52) | ((unsigned long long)S & 0xfffffffffffffull));
+}
+
+}  // namespace p3d

@@ -1,0 +1,62 @@
+// Internal interface between the host runtime (core.cpp) and the sm_103a kernels
+// (stage_kernels.cu).  Not part of the public C ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace p3d {
+
+// 1D transform kinds (the reference's trans_type1D flavours, build/init.C:121-731)
+enum Kind { K_EMPTY = 0, K_R2C = 1, K_C2R = 2, K_C2C_FWD = 3, K_C2C_BWD = 4, K_R2R = 5 };
+// FFTW r2r kinds
+enum R2R { REDFT00 = 0, REDFT10, REDFT01, REDFT11, RODFT00, RODFT10, RODFT01, RODFT11 };
+
+// Arithmetic used inside a stage for FP64 data: native DFMA, or float-float (two FP32 limbs,
+// ~48-bit significand) on the FP32 pipe.  FP32 data always uses native FP32.
+enum Arith { AR_NATIVE = 0, AR_DF = 1 };
+
+// Error codes recorded by p3dfft_last_error()
+enum Err {
+  E_OK = 0,
+  E_BAD_ARG = 1,
+  E_UNSUPPORTED = 2,
+  E_CUDA = 3,
+  E_NO_DEVICE = 4,
+  E_TOO_LARGE = 5,
+  E_PLAN = 6,
+};
+
+// One stage of a 3D (or 1D) plan, in logical-dimension terms: a 1D transform of `type kind`
+// along logical dim L, reading a field of logical dims d1 stored with strides s1 (elements) and
+// writing dims d2 with strides s2.  The two batch dims are the same size in and out.
+struct StageDesc {
+  int kind;       // Kind
+  int r2r;        // R2R when kind == K_R2R
+  int prec;       // 4 or 8
+  int dt1, dt2;   // 1 real, 2 complex
+  int L;          // transform dim
+  int d1[3], d2[3];
+  long long s1[3], s2[3];
+  int deriv;      // fuse the i*k multiply (compute_deriv_loc)
+};
+
+struct DeviceTables;  // twiddle-table cache, one per device
+
+// Launch one stage on `stream`.  in != out is required (the host runtime guarantees it).
+int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
+                 DeviceTables *tabs, int *kernels_launched);
+// Pure permutation copy of an element size `esize` bytes field (EMPTY stages).
+int launch_permute(const int d[3], const long long s1[3], const long long s2[3], int esize,
+                   const void *in, void *out, cudaStream_t stream, int *kernels_launched);
+// Standalone spectral derivative on a complex field (build/deriv.C:85-184), in may equal out.
+int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, const void *in,
+                 void *out, cudaStream_t stream, int *kernels_launched);
+
+DeviceTables *tables_create();
+void tables_destroy(DeviceTables *);
+
+// Smallest / largest supported transform length inside one CTA (per precision)
+int max_line_len(int prec);
+
+}  // namespace p3d

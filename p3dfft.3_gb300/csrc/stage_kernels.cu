@@ -1,0 +1,823 @@
+// sm_103a kernels for the P3DFFT++ stage pipeline.
+//
+// One kernel family, `k_stage`, executes a whole reference "transplan" stage
+// (build/exec.C:522-702): it gathers a tile of TB lines along the transform dimension L from
+// the input memory order, runs the 1D transform in shared memory (Stockham autosort, mixed
+// radix 2/3/4/5/7/8 + generic odd radix), applies the kind's pre/post-processing (R2C/C2R
+// half-length packing, DCT/DST extensions, the fused i*k derivative of compute_deriv_loc,
+// build/exec.C:228-287) and scatters the tile into the output memory order.  Each stage
+// therefore reads and writes HBM exactly once; the reference's reorder_trans/reorder_out
+// transposes (build/exec.C:737-2032) are folded into the tile gather/scatter.
+//
+// The arithmetic is a policy template:
+//   Native<double>  FP64 data, DFMA arithmetic
+//   Native<float>   FP32 data, FFMA arithmetic, twiddles rounded from FP64/long-double tables
+//   DF              FP64 data, float-float arithmetic on the FP32 pipe (df_arith.cuh)
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "df_arith.cuh"
+#include "kernels.h"
+
+namespace p3d {
+
+// ------------------------------------------------------------------------------------------
+// Arithmetic policies
+template <class R>
+struct __align__(2 * sizeof(R)) cx {
+  R x, y;
+};
+
+__device__ __forceinline__ cx<double> ldg_c(const cx<double> *p) {
+  double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+  cx<double> r;
+  r.x = v.x;
+  r.y = v.y;
+  return r;
+}
+__device__ __forceinline__ cx<float> ldg_c(const cx<float> *p) {
+  float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  cx<float> r;
+  r.x = v.x;
+  r.y = v.y;
+  return r;
+}
+
+template <class R>
+struct Native {
+  using G = R;       // global real type
+  using S = R;       // shared-memory real type
+  using C = cx<R>;   // working complex
+  using T = cx<R>;   // twiddle-table entry
+  static __device__ __forceinline__ C mk(S a, S b) { C c; c.x = a; c.y = b; return c; }
+  static __device__ __forceinline__ C add(C a, C b) { return mk(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ C sub(C a, C b) { return mk(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ C mul(C a, C b) {
+    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  }
+  static __device__ __forceinline__ C muli(C a) { return mk(-a.y, a.x); }
+  static __device__ __forceinline__ C mulmi(C a) { return mk(a.y, -a.x); }
+  static __device__ __forceinline__ C conj(C a) { return mk(a.x, -a.y); }
+  static __device__ __forceinline__ C half(C a) { return mk(a.x * R(0.5), a.y * R(0.5)); }
+  static __device__ __forceinline__ C neg(C a) { return mk(-a.x, -a.y); }
+  static __device__ __forceinline__ C rsqrt2(C a) {
+    const R c = R(0.70710678118654752440084436210485);
+    return mk(a.x * c, a.y * c);
+  }
+  static __device__ __forceinline__ C iscale(C a, int k) {  // a * (i*k)
+    R kk = R(k);
+    return mk(-kk * a.y, kk * a.x);
+  }
+  static __device__ __forceinline__ S rzero() { return R(0); }
+  static __device__ __forceinline__ C zero() { return mk(R(0), R(0)); }
+  static __device__ __forceinline__ S negs(S a) { return -a; }
+  static __device__ __forceinline__ S halfs(S a) { return a * R(0.5); }
+  static __device__ __forceinline__ S ld(const G *p) { return __ldg(p); }
+  static __device__ __forceinline__ C ldc(const G *p) {
+    cx<R> v = ldg_c(reinterpret_cast<const cx<R> *>(p));
+    return mk(v.x, v.y);
+  }
+  static __device__ __forceinline__ void st(G *p, S v) { *p = v; }
+  static __device__ __forceinline__ void stc(G *p, C v) {
+    cx<R> w; w.x = v.x; w.y = v.y;
+    *reinterpret_cast<cx<R> *>(p) = w;
+  }
+  static __device__ __forceinline__ C tw(const T *t, int k) {
+    T v = ldg_c(t + k);
+    return mk(v.x, v.y);
+  }
+};
+
+// float-float arithmetic for FP64 data (see df_arith.cuh)
+struct DF {
+  using G = double;
+  using S = ff;
+  using C = cff;
+  using T = cff;
+  static __device__ __forceinline__ C mk(S a, S b) { C c; c.x = a; c.y = b; return c; }
+  static __device__ __forceinline__ C add(C a, C b) { return mk(ff_add(a.x, b.x), ff_add(a.y, b.y)); }
+  static __device__ __forceinline__ C sub(C a, C b) { return mk(ff_sub(a.x, b.x), ff_sub(a.y, b.y)); }
+  static __device__ __forceinline__ C mul(C a, C b) { return cff_mul(a, b); }
+  static __device__ __forceinline__ C muli(C a) { return mk(ff_neg(a.y), a.x); }
+  static __device__ __forceinline__ C mulmi(C a) { return mk(a.y, ff_neg(a.x)); }
+  static __device__ __forceinline__ C conj(C a) { return mk(a.x, ff_neg(a.y)); }
+  static __device__ __forceinline__ C half(C a) { return mk(ff_half(a.x), ff_half(a.y)); }
+  static __device__ __forceinline__ C neg(C a) { return mk(ff_neg(a.x), ff_neg(a.y)); }
+  static __device__ __forceinline__ C rsqrt2(C a) {
+    return mk(ff_mul_const(a.x, FF_RSQRT2_HI, FF_RSQRT2_LO), ff_mul_const(a.y, FF_RSQRT2_HI, FF_RSQRT2_LO));
+  }
+  static __device__ __forceinline__ C iscale(C a, int k) {
+    return mk(ff_neg(ff_mul_int(a.y, k)), ff_mul_int(a.x, k));
+  }
+  static __device__ __forceinline__ S rzero() { return ff{0.f, 0.f}; }
+  static __device__ __forceinline__ C zero() { return mk(rzero(), rzero()); }
+  static __device__ __forceinline__ S negs(S a) { return ff_neg(a); }
+  static __device__ __forceinline__ S halfs(S a) { return ff_half(a); }
+  static __device__ __forceinline__ S ld(const G *p) { return ff_from_double_bits(__ldg(reinterpret_cast<const long long *>(p))); }
+  static __device__ __forceinline__ C ldc(const G *p) {
+    longlong2 v = __ldg(reinterpret_cast<const longlong2 *>(p));
+    return mk(ff_from_double_bits(v.x), ff_from_double_bits(v.y));
+  }
+  static __device__ __forceinline__ void st(G *p, S v) { *reinterpret_cast<long long *>(p) = ff_to_double_bits(v); }
+  static __device__ __forceinline__ void stc(G *p, C v) {
+    longlong2 w;
+    w.x = ff_to_double_bits(v.x);
+    w.y = ff_to_double_bits(v.y);
+    *reinterpret_cast<longlong2 *>(p) = w;
+  }
+  static __device__ __forceinline__ C tw(const T *t, int k) {
+    float4 v = __ldg(reinterpret_cast<const float4 *>(t + k));
+    C c;
+    c.x = ff{v.x, v.y};
+    c.y = ff{v.z, v.w};
+    return c;
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+struct KParams {
+  const void *in;
+  void *out;
+  const void *tw;   // W_tabN^m, m < tabN (forward sign)
+  const void *aux;  // generic r2r: W_{8n'}^m
+  int kind, r2r, sign;
+  int nfft, twstep;  // W_nfft^m = tw[m * twstep]
+  int nrad;
+  int rad[24];
+  int nin, nout, nlog;  // line lengths (elements) in / out, logical length
+  int ls;               // shared-memory line stride (complex slots)
+  int TB, nfl;          // data lines per CTA, FFT lines per data line (1 or 2)
+  int ntile, dt, dother;
+  long long iL, it, io, oL, ot, oo;
+  int load_Lmajor, store_Lmajor;
+  int deriv, dg, dmid;
+  int r2r_np, r2r_a2, r2r_b2, r2r_sin, r2r_halffirst, r2r_halflast;
+  int in_complex, out_complex;
+};
+
+template <class O>
+__device__ __forceinline__ typename O::C twid(const KParams &p, int m, int sign) {
+  typename O::C w = O::tw(reinterpret_cast<const typename O::T *>(p.tw), m * p.twstep);
+  return sign < 0 ? w : O::conj(w);
+}
+
+// DFT of radix R in registers, sign -1 forward.  Odd R uses the twiddle table for W_R^q.
+template <class O, int R>
+__device__ __forceinline__ void dft_reg(typename O::C *v, int sign, const KParams &p) {
+  using C = typename O::C;
+  if (R == 2) {
+    C a = v[0], b = v[1];
+    v[0] = O::add(a, b);
+    v[1] = O::sub(a, b);
+  } else if (R == 4) {
+    C t0 = O::add(v[0], v[2]), t1 = O::sub(v[0], v[2]);
+    C t2 = O::add(v[1], v[3]), t3 = O::sub(v[1], v[3]);
+    t3 = sign < 0 ? O::mulmi(t3) : O::muli(t3);
+    v[0] = O::add(t0, t2);
+    v[2] = O::sub(t0, t2);
+    v[1] = O::add(t1, t3);
+    v[3] = O::sub(t1, t3);
+  } else if (R == 8) {
+    C e[4], o[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      e[k] = v[2 * k];
+      o[k] = v[2 * k + 1];
+    }
+    dft_reg<O, 4>(e, sign, p);
+    dft_reg<O, 4>(o, sign, p);
+    // o[k] *= W8^k (forward), conj for backward
+    C o1 = O::rsqrt2(sign < 0 ? O::add(o[1], O::mulmi(o[1])) : O::add(o[1], O::muli(o[1])));
+    C o2 = sign < 0 ? O::mulmi(o[2]) : O::muli(o[2]);
+    C o3 = O::rsqrt2(sign < 0 ? O::sub(O::mulmi(o[3]), o[3]) : O::sub(O::muli(o[3]), o[3]));
+    v[0] = O::add(e[0], o[0]);
+    v[4] = O::sub(e[0], o[0]);
+    v[1] = O::add(e[1], o1);
+    v[5] = O::sub(e[1], o1);
+    v[2] = O::add(e[2], o2);
+    v[6] = O::sub(e[2], o2);
+    v[3] = O::add(e[3], o3);
+    v[7] = O::sub(e[3], o3);
+  } else {
+    // odd radix: direct sum with W_R^q from the table (index q * nfft/R)
+    C out[R];
+    const int unit = p.nfft / R;
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      C acc = v[0];
+#pragma unroll
+      for (int r = 1; r < R; r++) acc = O::add(acc, O::mul(v[r], twid<O>(p, ((r * q) % R) * unit, sign)));
+      out[q] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < R; q++) v[q] = out[q];
+  }
+}
+
+template <class O, int R>
+__device__ __forceinline__ void bfly(const typename O::C *src, typename O::C *dst, int j, int T, int Ns,
+                                     int sign, const KParams &p) {
+  using C = typename O::C;
+  C v[R];
+  int k = j % Ns;
+#pragma unroll
+  for (int r = 0; r < R; r++) v[r] = src[j + r * T];
+  if (Ns > 1) {
+    int unit = k * (p.nfft / (Ns * R));
+#pragma unroll
+    for (int r = 1; r < R; r++) v[r] = O::mul(v[r], twid<O>(p, r * unit, sign));
+  }
+  dft_reg<O, R>(v, sign, p);
+  int base = (j - k) * R + k;
+#pragma unroll
+  for (int r = 0; r < R; r++) dst[base + r * Ns] = v[r];
+}
+
+template <class O>
+__device__ void bfly_generic(const typename O::C *src, typename O::C *dst, int j, int T, int Ns, int R,
+                             int sign, const KParams &p) {
+  using C = typename O::C;
+  int k = j % Ns;
+  int unit = k * (p.nfft / (Ns * R));
+  int runit = p.nfft / R;
+  int base = (j - k) * R + k;
+  for (int q = 0; q < R; q++) {
+    C acc = O::zero();
+    for (int r = 0; r < R; r++) {
+      C x = src[j + r * T];
+      int m = r * unit + ((r * q) % R) * runit;  // twiddle * W_R^{rq}
+      m %= p.nfft;
+      acc = O::add(acc, O::mul(x, twid<O>(p, m, sign)));
+    }
+    dst[base + q * Ns] = acc;
+  }
+}
+
+// Runs the radix passes over `nlines` lines; returns the buffer index holding the result.
+template <class O>
+__device__ int fft_passes(const KParams &p, typename O::C *b0, typename O::C *b1, int nlines, int sign) {
+  using C = typename O::C;
+  int Ns = 1, cur = 0;
+  for (int s = 0; s < p.nrad; s++) {
+    const int R = p.rad[s];
+    const int T = p.nfft / R;
+    const C *src = cur ? b1 : b0;
+    C *dst = cur ? b0 : b1;
+    const int total = nlines * T;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      int lt = idx / T, j = idx - lt * T;
+      const C *sl = src + (size_t)lt * p.ls;
+      C *dl = dst + (size_t)lt * p.ls;
+      switch (R) {
+        case 2: bfly<O, 2>(sl, dl, j, T, Ns, sign, p); break;
+        case 3: bfly<O, 3>(sl, dl, j, T, Ns, sign, p); break;
+        case 4: bfly<O, 4>(sl, dl, j, T, Ns, sign, p); break;
+        case 5: bfly<O, 5>(sl, dl, j, T, Ns, sign, p); break;
+        case 7: bfly<O, 7>(sl, dl, j, T, Ns, sign, p); break;
+        case 8: bfly<O, 8>(sl, dl, j, T, Ns, sign, p); break;
+        default: bfly_generic<O>(sl, dl, j, T, Ns, R, sign, p); break;
+      }
+    }
+    __syncthreads();
+    cur ^= 1;
+    Ns *= R;
+  }
+  return cur;
+}
+
+// Element offsets of a line position in global memory (elements, not reals)
+__device__ __forceinline__ long long in_off(const KParams &p, int lt, int j, int t0, int ioth) {
+  return (long long)j * p.iL + (long long)(t0 + lt) * p.it + (long long)ioth * p.io;
+}
+__device__ __forceinline__ long long out_off(const KParams &p, int lt, int k, int t0, int ioth) {
+  return (long long)k * p.oL + (long long)(t0 + lt) * p.ot + (long long)ioth * p.oo;
+}
+
+__device__ __forceinline__ void map_idx(int idx, int n, int nlines, int Lmajor, int &lt, int &j) {
+  if (Lmajor) {
+    lt = idx / n;
+    j = idx - lt * n;
+  } else {
+    j = idx / nlines;
+    lt = idx - j * nlines;
+  }
+}
+
+template <class O>
+__device__ __forceinline__ typename O::C apply_deriv(const KParams &p, typename O::C v, int k) {
+  if (!p.deriv) return v;
+  if (k == p.dmid) return O::zero();
+  int kk = (k < p.dmid) ? k : k - p.dg;
+  return O::iscale(v, kk);
+}
+
+// ------------------------------------------------------------------------------------------
+template <class O>
+__global__ void __launch_bounds__(256) k_stage(KParams p) {
+  using C = typename O::C;
+  using S = typename O::S;
+  using G = typename O::G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *b0 = reinterpret_cast<C *>(smem_raw);
+  C *b1 = b0 + (size_t)p.TB * p.nfl * p.ls;
+  const int tile = blockIdx.x % p.ntile;
+  const int ioth = blockIdx.x / p.ntile;
+  const int t0 = tile * p.TB;
+  const int nlines = min(p.TB, p.dt - t0);
+  const G *gin = reinterpret_cast<const G *>(p.in);
+  G *gout = reinterpret_cast<G *>(p.out);
+  const int kind = p.kind;
+
+  // ---------------- gather + pre-processing into b0 ----------------
+  const bool direct = (kind == K_C2C_FWD || kind == K_C2C_BWD || kind == K_R2C ||
+                       (kind == K_C2R && (p.nlog & 1)));
+  {
+    C *dstbuf = direct ? b0 : b1;
+    const int total = nlines * p.nin;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      int lt, j;
+      map_idx(idx, p.nin, nlines, p.load_Lmajor, lt, j);
+      long long off = in_off(p, lt, j, t0, ioth);
+      C *line = dstbuf + (size_t)lt * p.nfl * p.ls;
+      if (p.in_complex) {
+        line[j] = O::ldc(gin + 2 * off);
+      } else if (kind == K_R2C && !(p.nlog & 1)) {
+        reinterpret_cast<S *>(line)[j] = O::ld(gin + off);  // packed z[n] = x[2n] + i x[2n+1]
+      } else {
+        line[j] = O::mk(O::ld(gin + off), O::rzero());
+      }
+    }
+  }
+  __syncthreads();
+  if (!direct) {
+    if (kind == K_C2R) {  // even N: Z'[k] = (X[k]+conj X[M-k]) + i conj(W_N^k) (X[k]-conj X[M-k])
+      const int M = p.nfft;
+      const int total = nlines * M;
+      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        int lt = idx / M, k = idx - lt * M;
+        const C *X = b1 + (size_t)lt * p.ls;
+        C a = X[k], b = X[M - k];
+        if (k == 0) {
+          a.y = O::rzero();
+          b.y = O::rzero();
+        }
+        C bc = O::conj(b);
+        C s = O::add(a, bc), d = O::sub(a, bc);
+        C w = O::conj(O::tw(reinterpret_cast<const typename O::T *>(p.tw), k));  // W_N^-k
+        b0[(size_t)lt * p.ls + k] = O::add(s, O::muli(O::mul(w, d)));
+      }
+    } else if (kind == K_C2R) {
+      // unreachable: odd C2R is direct
+    } else if (kind == K_R2R && p.r2r == REDFT00) {
+      // even extension of length M = 2(n-1)
+      const int n = p.nin, M = p.nfft;
+      const int total = nlines * M;
+      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        int lt = idx / M, j = idx - lt * M;
+        const C *x = b1 + (size_t)lt * p.ls;
+        b0[(size_t)lt * p.ls + j] = (j < n) ? x[j] : x[M - j];
+      }
+    } else if (kind == K_R2R && p.r2r == RODFT00) {
+      // odd extension of length M = 2(n+1): [0, x0..x_{n-1}, 0, -x_{n-1}..-x0]
+      const int n = p.nin, M = p.nfft;
+      const int total = nlines * M;
+      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        int lt = idx / M, j = idx - lt * M;
+        const C *x = b1 + (size_t)lt * p.ls;
+        C v;
+        if (j == 0 || j == n + 1) v = O::zero();
+        else if (j <= n) v = x[j - 1];
+        else v = O::neg(x[M - j - 1]);
+        b0[(size_t)lt * p.ls + j] = v;
+      }
+    } else if (kind == K_R2R) {
+      // generic kinds II/III/IV: u_j = x_j exp(-i pi beta j / n'), zero padded to 2n'.
+      // complex data: FFT line 2lt holds u(x), line 2lt+1 holds u(conj x).
+      const int n = p.nin, M = p.nfft;
+      const int total = nlines * M;
+      const typename O::T *aux = reinterpret_cast<const typename O::T *>(p.aux);
+      for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        int lt = idx / M, j = idx - lt * M;
+        const C *x = b1 + (size_t)lt * p.nfl * p.ls;
+        C u = O::zero(), uc = O::zero();
+        if (j < n) {
+          C xv = x[j];
+          if ((p.r2r_halffirst && j == 0) || (p.r2r_halflast && j == n - 1)) xv = O::half(xv);
+          C w = O::tw(aux, 2 * p.r2r_b2 * j);
+          u = O::mul(xv, w);
+          uc = O::mul(O::conj(xv), w);
+        }
+        C *fl = b0 + (size_t)lt * p.nfl * p.ls;
+        fl[j] = u;
+        if (p.nfl == 2) fl[p.ls + j] = uc;
+      }
+    }
+    __syncthreads();
+  } else if (kind == K_C2R) {
+    // odd N: Hermitian extension X[N-k] = conj X[k], imag of DC ignored
+    const int N = p.nlog, h = (N + 1) / 2;
+    const int total = nlines * N;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      int lt = idx / N, k = idx - lt * N;
+      C *X = b0 + (size_t)lt * p.ls;
+      if (k == 0) X[0].y = O::rzero();
+      else if (k >= h) X[k] = O::conj(X[N - k]);
+    }
+    __syncthreads();
+  }
+
+  // ---------------- FFT passes ----------------
+  const int cur = fft_passes<O>(p, b0, b1, nlines * p.nfl, p.sign);
+  const C *res = cur ? b1 : b0;
+
+  // ---------------- post-processing + scatter ----------------
+  const int total = nlines * p.nout;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int lt, k;
+    map_idx(idx, p.nout, nlines, p.store_Lmajor, lt, k);
+    const C *Y = res + (size_t)lt * p.nfl * p.ls;
+    long long off = out_off(p, lt, k, t0, ioth);
+    if (kind == K_C2C_FWD || kind == K_C2C_BWD) {
+      O::stc(gout + 2 * off, apply_deriv<O>(p, Y[k], k));
+    } else if (kind == K_R2C) {
+      C v;
+      if (p.nlog & 1) {
+        v = Y[k];
+      } else {
+        const int M = p.nfft;
+        C a = Y[k % M], b = O::conj(Y[(M - k) % M]);
+        C w = O::tw(reinterpret_cast<const typename O::T *>(p.tw), k);  // W_N^k
+        C s = O::add(a, b), d = O::sub(a, b);
+        v = O::half(O::sub(s, O::muli(O::mul(w, d))));
+      }
+      O::stc(gout + 2 * off, apply_deriv<O>(p, v, k));
+    } else if (kind == K_C2R) {
+      S v;
+      if (p.nlog & 1) v = Y[k].x;
+      else v = (k & 1) ? Y[k >> 1].y : Y[k >> 1].x;
+      O::st(gout + off, v);
+    } else {  // K_R2R
+      C v;
+      if (p.r2r == REDFT00) {
+        v = Y[k];
+      } else if (p.r2r == RODFT00) {
+        v = O::muli(Y[k + 1]);
+      } else {
+        const typename O::T *aux = reinterpret_cast<const typename O::T *>(p.aux);
+        C w = O::tw(aux, p.r2r_a2 * (2 * k + p.r2r_b2));
+        C sm = O::mul(w, Y[k]);  // S-_k
+        C sp;
+        if (p.nfl == 2) sp = O::conj(O::mul(w, Y[p.ls + k]));
+        else sp = O::conj(sm);
+        v = p.r2r_sin ? O::mulmi(O::sub(sp, sm)) : O::add(sp, sm);
+      }
+      if (p.out_complex) O::stc(gout + 2 * off, apply_deriv<O>(p, v, k));
+      else O::st(gout + off, v.x);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// EMPTY stages: pure permutation (reorder_out / reorder_in, build/exec.C:1858-2266)
+template <class E>
+__global__ void __launch_bounds__(256) k_permute(const E *__restrict__ in, E *__restrict__ out, int da, int db,
+                                                 long long ia, long long ib, long long ic, long long oa,
+                                                 long long ob, long long oc, int ta, int tb) {
+  // a = input-fastest dim, b = output-fastest dim, c = remaining dim (one CTA per 32x32 tile)
+  __shared__ E tile[32][33];
+  const int bx = blockIdx.x % ta, by = (blockIdx.x / ta) % tb;
+  const long long c = blockIdx.x / ((long long)ta * tb);
+  const int a0 = bx * 32, b0 = by * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    int a = a0 + threadIdx.x, b = b0 + y;
+    if (a < da && b < db) tile[y][threadIdx.x] = in[a * ia + b * ib + c * ic];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    int b = b0 + threadIdx.x, a = a0 + y;
+    if (a < da && b < db) out[a * oa + b * ob + c * oc] = tile[threadIdx.x][y];
+  }
+}
+
+// Standalone derivative on a complex field: storage-order traversal, multiply by i*k along
+// logical dim idir (build/deriv.C:85-184 with GlobStart = 0).
+template <class R>
+__global__ void k_deriv(const R *in, R *out, long long n, int sd0, int sd1, int pos, int g, int mid) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (; q < n; q += stride) {
+    long long c0 = q % sd0, r = q / sd0, c1 = r % sd1, c2 = r / sd1;
+    int k = (int)(pos == 0 ? c0 : (pos == 1 ? c1 : c2));
+    R x = in[2 * q], y = in[2 * q + 1];
+    R rx, ry;
+    if (k == mid) {
+      rx = 0;
+      ry = 0;
+    } else {
+      R kk = (R)((k < mid) ? k : k - g);
+      rx = -kk * y;
+      ry = kk * x;
+    }
+    out[2 * q] = rx;
+    out[2 * q + 1] = ry;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side: twiddle tables (generated in long double, kept resident per device)
+struct DeviceTables {
+  std::mutex mu;
+  // key: (N, format) format 0 = double, 1 = float, 2 = float-float
+  std::map<std::pair<int, int>, void *> tabs;
+  ~DeviceTables() {
+    for (auto &kv : tabs) cudaFree(kv.second);
+  }
+  const void *get(int N, int fmt, int *err) {
+    std::lock_guard<std::mutex> g(mu);
+    auto key = std::make_pair(N, fmt);
+    auto it = tabs.find(key);
+    if (it != tabs.end()) return it->second;
+    const long double TWO_PI = 6.283185307179586476925286766559005768L;
+    size_t bytes = (size_t)N * (fmt == 1 ? 8 : 16);
+    std::vector<unsigned char> host(bytes);
+    for (int k = 0; k < N; k++) {
+      long double a = TWO_PI * (long double)k / (long double)N;
+      long double c = cosl(a), s = -sinl(a);
+      if (fmt == 0) {
+        double v[2] = {(double)c, (double)s};
+        memcpy(&host[(size_t)k * 16], v, 16);
+      } else if (fmt == 1) {
+        float v[2] = {(float)c, (float)s};
+        memcpy(&host[(size_t)k * 8], v, 8);
+      } else {
+        float ch = (float)c, sh = (float)s;
+        float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
+        memcpy(&host[(size_t)k * 16], v, 16);
+      }
+    }
+    void *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+      *err = E_CUDA;
+      return nullptr;
+    }
+    if (cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(d);
+      *err = E_CUDA;
+      return nullptr;
+    }
+    tabs[key] = d;
+    return d;
+  }
+};
+
+DeviceTables *tables_create() { return new DeviceTables(); }
+void tables_destroy(DeviceTables *t) { delete t; }
+
+static void factorize(int n, std::vector<int> &rad) {
+  rad.clear();
+  while (n % 8 == 0 && n > 8) { rad.push_back(8); n /= 8; }
+  if (n % 8 == 0) { rad.push_back(8); n /= 8; }
+  while (n % 4 == 0) { rad.push_back(4); n /= 4; }
+  while (n % 2 == 0) { rad.push_back(2); n /= 2; }
+  const int small[3] = {3, 5, 7};
+  for (int f : small)
+    while (n % f == 0) { rad.push_back(f); n /= f; }
+  for (int f = 11; (long long)f * f <= n; f += 2)
+    while (n % f == 0) { rad.push_back(f); n /= f; }
+  if (n > 1) rad.push_back(n);
+}
+
+int max_line_len(int prec) { return prec == 8 ? 6144 : 12288; }
+
+template <class O>
+static int launch_k(const KParams &p, size_t smem, int grid, cudaStream_t st) {
+  static int configured_smem = 0;  // per instantiation
+  if ((int)smem > configured_smem) {
+    if (cudaFuncSetAttribute(k_stage<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return E_CUDA;
+    configured_smem = (int)smem;
+  }
+  k_stage<O><<<grid, 256, smem, st>>>(p);
+  return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+}
+
+int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
+                 DeviceTables *tabs, int *kernels_launched) {
+  const int L = d.L;
+  const int a = (L + 1) % 3, b = (L + 2) % 3;
+  if (d.d1[a] != d.d2[a] || d.d1[b] != d.d2[b]) return E_BAD_ARG;
+  KParams p;
+  memset(&p, 0, sizeof(p));
+  p.in = in;
+  p.out = out;
+  p.kind = d.kind;
+  p.r2r = d.r2r;
+  p.nin = d.d1[L];
+  p.nout = d.d2[L];
+  p.in_complex = d.dt1 == 2;
+  p.out_complex = d.dt2 == 2;
+  p.nfl = 1;
+  p.sign = -1;
+  int tabN = 0;
+  switch (d.kind) {
+    case K_C2C_FWD:
+    case K_C2C_BWD:
+      if (p.nin != p.nout) return E_BAD_ARG;
+      p.nlog = p.nin;
+      p.nfft = p.nin;
+      tabN = p.nfft;
+      p.twstep = 1;
+      p.sign = d.kind == K_C2C_FWD ? -1 : 1;
+      break;
+    case K_R2C:
+      p.nlog = p.nin;
+      if (p.nout != p.nlog / 2 + 1) return E_BAD_ARG;
+      if (p.nlog % 2 == 0 && p.nlog >= 2) {
+        p.nfft = p.nlog / 2;
+        tabN = p.nlog;
+        p.twstep = 2;
+      } else {
+        p.nfft = p.nlog;
+        tabN = p.nlog;
+        p.twstep = 1;
+      }
+      break;
+    case K_C2R:
+      p.nlog = p.nout;
+      if (p.nin != p.nlog / 2 + 1) return E_BAD_ARG;
+      p.sign = 1;
+      if (p.nlog % 2 == 0 && p.nlog >= 2) {
+        p.nfft = p.nlog / 2;
+        tabN = p.nlog;
+        p.twstep = 2;
+      } else {
+        p.nfft = p.nlog;
+        tabN = p.nlog;
+        p.twstep = 1;
+      }
+      break;
+    case K_R2R: {
+      if (p.nin != p.nout) return E_BAD_ARG;
+      int n = p.nin;
+      p.nlog = n;
+      if (d.r2r == REDFT00) {
+        if (n < 2) return E_UNSUPPORTED;
+        p.nfft = 2 * (n - 1);
+      } else if (d.r2r == RODFT00) {
+        p.nfft = 2 * (n + 1);
+      } else {
+        p.nfft = 2 * n;
+        p.r2r_np = n;
+        p.nfl = p.in_complex ? 2 : 1;
+        switch (d.r2r) {
+          case REDFT10: p.r2r_a2 = 1; p.r2r_b2 = 0; break;
+          case REDFT01: p.r2r_a2 = 0; p.r2r_b2 = 1; p.r2r_halffirst = 1; break;
+          case REDFT11: p.r2r_a2 = 1; p.r2r_b2 = 1; break;
+          case RODFT10: p.r2r_a2 = 1; p.r2r_b2 = 2; p.r2r_sin = 1; break;
+          case RODFT01: p.r2r_a2 = 2; p.r2r_b2 = 1; p.r2r_sin = 1; p.r2r_halflast = 1; break;
+          case RODFT11: p.r2r_a2 = 1; p.r2r_b2 = 1; p.r2r_sin = 1; break;
+          default: return E_BAD_ARG;
+        }
+      }
+      tabN = p.nfft;
+      p.twstep = 1;
+      break;
+    }
+    default:
+      return E_BAD_ARG;
+  }
+  if (p.nfft > max_line_len(d.prec)) return E_TOO_LARGE;
+  std::vector<int> rad;
+  factorize(p.nfft, rad);
+  if ((int)rad.size() > 24) return E_UNSUPPORTED;
+  p.nrad = (int)rad.size();
+  for (int i = 0; i < p.nrad; i++) p.rad[i] = rad[i];
+
+  const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? 2 : 0);
+  int err = E_OK;
+  p.tw = tabs->get(tabN, fmt, &err);
+  if (!p.tw) return err;
+  if (d.kind == K_R2R && p.r2r_np > 0) {
+    p.aux = tabs->get(8 * p.r2r_np, fmt, &err);
+    if (!p.aux) return err;
+  }
+  if (d.deriv && d.dt2 == 2) {
+    p.deriv = 1;
+    p.dg = (d.kind == K_R2C) ? (p.nout - 1) * 2 : p.nout;  // exec.C:240-243
+    p.dmid = p.dg / 2;
+  }
+  // tile selection: t = batch dim along which consecutive lines are taken
+  p.iL = d.s1[L];
+  p.oL = d.s2[L];
+  int t, o;
+  if (d.s1[L] == 1) {
+    t = d.s1[a] <= d.s1[b] ? a : b;
+    p.load_Lmajor = 1;
+  } else {
+    t = d.s1[a] <= d.s1[b] ? a : b;
+    p.load_Lmajor = 0;
+  }
+  o = (t == a) ? b : a;
+  p.store_Lmajor = (d.s2[L] == 1) ? 1 : ((d.s2[t] == 1) ? 0 : 1);
+  p.it = d.s1[t];
+  p.io = d.s1[o];
+  p.ot = d.s2[t];
+  p.oo = d.s2[o];
+  p.dt = d.d1[t];
+  p.dother = d.d1[o];
+
+  const size_t csz = (d.prec == 4) ? 8 : 16;
+  int slots = p.nfft;
+  if (p.nin > slots) slots = p.nin;
+  if (p.nout > slots) slots = p.nout;
+  if (d.kind == K_C2R) slots = std::max(slots, p.nfft + 1);
+  p.ls = slots;
+  const size_t per_line = 2 * (size_t)p.nfl * p.ls * csz;
+  const size_t smem_cap = 110 * 1024;
+  int TB;
+  if (!p.load_Lmajor || !p.store_Lmajor) {
+    int esz = (int)((p.in_complex ? 2 : 1) * d.prec);
+    TB = std::max(2, 64 / esz);
+  } else {
+    TB = std::max(1, 2048 / std::max(1, p.nfft));
+  }
+  while (TB > 1 && per_line * TB > smem_cap) TB--;
+  if (per_line * TB > 227 * 1024) return E_TOO_LARGE;
+  if (TB > p.dt) TB = p.dt;
+  if (TB < 1) TB = 1;
+  p.TB = TB;
+  p.ntile = (p.dt + TB - 1) / TB;
+  long long grid = (long long)p.ntile * p.dother;
+  if (grid <= 0) return E_OK;
+  if (grid > 0x7fffffffLL) return E_TOO_LARGE;
+  size_t smem = per_line * TB;
+  int rc;
+  if (d.prec == 4) rc = launch_k<Native<float>>(p, smem, (int)grid, stream);
+  else if (arith == AR_DF) rc = launch_k<DF>(p, smem, (int)grid, stream);
+  else rc = launch_k<Native<double>>(p, smem, (int)grid, stream);
+  if (rc == E_OK && kernels_launched) (*kernels_launched)++;
+  return rc;
+}
+
+template <class E>
+static int permute_t(const int d[3], const long long s1[3], const long long s2[3], const void *in, void *out,
+                     cudaStream_t st) {
+  int a = 0, b = 0;
+  for (int i = 0; i < 3; i++) {
+    if (s1[i] < s1[a]) a = i;
+    if (s2[i] < s2[b]) b = i;
+  }
+  if (a == b) b = (a + 1) % 3;
+  int c = 3 - a - b;
+  int ta = (d[a] + 31) / 32, tb = (d[b] + 31) / 32;
+  long long grid = (long long)ta * tb * d[c];
+  if (grid <= 0) return E_OK;
+  if (grid > 0x7fffffffLL) return E_TOO_LARGE;
+  dim3 blk(32, 8);
+  k_permute<E><<<(unsigned)grid, blk, 0, st>>>((const E *)in, (E *)out, d[a], d[b], s1[a], s1[b], s1[c], s2[a],
+                                               s2[b], s2[c], ta, tb);
+  return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+}
+
+int launch_permute(const int d[3], const long long s1[3], const long long s2[3], int esize, const void *in,
+                   void *out, cudaStream_t stream, int *kernels_launched) {
+  int rc;
+  switch (esize) {
+    case 4: rc = permute_t<float>(d, s1, s2, in, out, stream); break;
+    case 8: rc = permute_t<double>(d, s1, s2, in, out, stream); break;
+    case 16: rc = permute_t<double2>(d, s1, s2, in, out, stream); break;
+    default: return E_BAD_ARG;
+  }
+  if (rc == E_OK && kernels_launched) (*kernels_launched)++;
+  return rc;
+}
+
+int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, const void *in, void *out,
+                 cudaStream_t stream, int *kernels_launched) {
+  // storage dims (fastest first) and the storage position of idir
+  int order[3] = {0, 1, 2};
+  for (int i = 0; i < 3; i++)
+    for (int j = i + 1; j < 3; j++)
+      if (s[order[j]] < s[order[i]]) std::swap(order[i], order[j]);
+  int pos = 0;
+  for (int i = 0; i < 3; i++)
+    if (order[i] == idir) pos = i;
+  long long n = (long long)d[0] * d[1] * d[2];
+  if (n == 0) return E_OK;
+  int mid = g / 2;
+  int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  if (prec == 8)
+    k_deriv<double><<<blocks, 256, 0, stream>>>((const double *)in, (double *)out, n, d[order[0]], d[order[1]], pos, g, mid);
+  else
+    k_deriv<float><<<blocks, 256, 0, stream>>>((const float *)in, (float *)out, n, d[order[0]], d[order[1]], pos, g, mid);
+  if (kernels_launched) (*kernels_launched)++;
+  return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+}
+
+}  // namespace p3d

@@ -1,0 +1,243 @@
+"""Python mirror of the P3DFFT++ interface over libp3dfft_gb300.so (ctypes, C ABI only).
+
+Mirrors the reference's C++ objects (include/p3dfft.h): `setup`/`cleanup`, the type-ID
+constants, `Transform3D` (transform3D<T1,T2>: plan in the constructor, `exec` / `exec_deriv`),
+`TransPlan` (transplan<T1,T2>) and `compute_deriv`.  Arrays are numpy arrays (host memory,
+staged through HBM by the library) or objects exposing a CUDA pointer (torch CUDA tensors, or an
+int device address), used in place.
+
+There is no CPU path: if the shared library is missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libp3dfft_gb300.so")
+
+# Type IDs: registration order of p3dfft::setup() (reference build/init.C:121-731)
+EMPTY_TYPE_SINGLE, EMPTY_TYPE_DOUBLE, EMPTY_TYPE_SINGLE_COMPLEX, EMPTY_TYPE_DOUBLE_COMPLEX = 0, 1, 2, 3
+R2CFFT_S, R2CFFT_D, C2RFFT_S, C2RFFT_D = 4, 5, 6, 7
+CFFT_FORWARD_S, CFFT_FORWARD_D, CFFT_BACKWARD_S, CFFT_BACKWARD_D = 8, 9, 10, 11
+_FAMILIES = ["DCT1", "DST1", "DCT2", "DST2", "DCT3", "DST3", "DCT4", "DST4"]
+TYPE_IDS = {
+    "EMPTY_TYPE_SINGLE": 0, "EMPTY_TYPE_DOUBLE": 1, "EMPTY_TYPE_SINGLE_COMPLEX": 2,
+    "EMPTY_TYPE_DOUBLE_COMPLEX": 3, "R2CFFT_S": 4, "R2CFFT_D": 5, "C2RFFT_S": 6, "C2RFFT_D": 7,
+    "CFFT_FORWARD_S": 8, "CFFT_FORWARD_D": 9, "CFFT_BACKWARD_S": 10, "CFFT_BACKWARD_D": 11,
+}
+for _f, _fam in enumerate(_FAMILIES):
+    for _v, _suf in enumerate(["REAL_S", "REAL_D", "COMPLEX_S", "COMPLEX_D"]):
+        TYPE_IDS[f"{_fam}_{_suf}"] = 12 + 4 * _f + _v
+globals().update(TYPE_IDS)
+
+ERR_NAMES = {0: "OK", 1: "BAD_ARG", 2: "UNSUPPORTED", 3: "CUDA", 4: "NO_DEVICE", 5: "TOO_LARGE", 6: "PLAN"}
+
+
+class P3DFFTError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Loads the C-ABI library (built by build_lib.py); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise P3DFFTError(f"{LIB_PATH} is missing: run `python p3dfft.3_gb300/build_lib.py` "
+                          "(or __graft_entry__.build()) first")
+    L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+    ip = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    sig = {
+        "p3dfft_setup": ([], None), "p3dfft_cleanup": ([], None),
+        "p3dfft_last_error": ([], ctypes.c_int), "p3dfft_last_error_string": ([], ctypes.c_char_p),
+        "p3dfft_clear_error": ([], None),
+        "p3dfft_gb300_set_stream": ([vp], None), "p3dfft_gb300_set_sync": ([ctypes.c_int], None),
+        "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
+        "p3dfft_gb300_plan3d": ([ip, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_exec3d": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_destroy3d": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_plan3d_types": ([ctypes.c_int, ip, ip, ip], ctypes.c_int),
+        "p3dfft_gb300_plan3d_stages": ([ctypes.c_int, ip, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_plan1d": ([ctypes.c_int, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_exec1d": ([ctypes.c_int, vp, vp, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_destroy1d": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_compute_deriv": ([ctypes.c_int, vp, vp, ip, ip, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_kernel_count": ([], ctypes.c_longlong), "p3dfft_gb300_reset_kernel_count": ([], None),
+        "p3dfft_gb300_enable_timers": ([ctypes.c_int], None), "p3dfft_gb300_timer": ([ctypes.c_int], ctypes.c_double),
+        "p3dfft_gb300_reset_timers": ([], None),
+        "p3dfft_gb300_device_alloc": ([ctypes.c_longlong], vp), "p3dfft_gb300_device_free": ([vp], None),
+        "p3dfft_gb300_memcpy_h2d": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
+        "p3dfft_gb300_memcpy_d2h": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
+        "p3dfft_gb300_synchronize": ([], ctypes.c_int), "p3dfft_gb300_version": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _i3(v):
+    return (ctypes.c_int * 3)(*[int(x) for x in v])
+
+
+def check(rc=None):
+    code = lib().p3dfft_last_error()
+    if (rc is not None and rc != 0) or code != 0:
+        msg = lib().p3dfft_last_error_string().decode()
+        lib().p3dfft_clear_error()
+        raise P3DFFTError(f"{ERR_NAMES.get(code, code)}: {msg}")
+
+
+def setup():
+    lib().p3dfft_setup()
+
+
+def cleanup():
+    lib().p3dfft_cleanup()
+
+
+def set_fp64_arith(mode: int):
+    """0: native FP64 (DFMA); 1: float-float on the FP32 pipe."""
+    lib().p3dfft_gb300_set_fp64_arith(int(mode))
+
+
+def set_sync(sync: bool):
+    lib().p3dfft_gb300_set_sync(1 if sync else 0)
+
+
+def set_stream(stream_ptr: int):
+    lib().p3dfft_gb300_set_stream(ctypes.c_void_p(int(stream_ptr)))
+
+
+def kernel_count() -> int:
+    return int(lib().p3dfft_gb300_kernel_count())
+
+
+def storage_shape(gdims, mo):
+    """numpy shape (slowest dimension first) of a field of logical dims gdims stored with memory
+    order mo (mo[d] = storage rank of logical dim d, 0 = stride-1)."""
+    sd = [0, 0, 0]
+    for i in range(3):
+        sd[mo[i]] = gdims[i]
+    return (sd[2], sd[1], sd[0])
+
+
+def _ptr(a):
+    """Returns (void pointer, keep-alive) for numpy arrays, torch tensors or int addresses."""
+    if isinstance(a, np.ndarray):
+        if not a.flags.c_contiguous:
+            raise P3DFFTError("arrays must be C-contiguous")
+        return ctypes.c_void_p(a.ctypes.data), a
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr()), a
+    return ctypes.c_void_p(int(a)), None
+
+
+class Transform3D:
+    """transform3D<T1,T2>: the constructor plans (reference build/templ.C:91-420)."""
+
+    def __init__(self, types, gdims1, mo1, gdims2, mo2, dcs1=-1, dcs2=-1):
+        setup()
+        self.types = tuple(int(t) for t in types)
+        self.gdims1, self.mo1, self.dcs1 = tuple(gdims1), tuple(mo1), int(dcs1)
+        self.gdims2, self.mo2, self.dcs2 = tuple(gdims2), tuple(mo2), int(dcs2)
+        t = _i3(self.types)
+        h = lib().p3dfft_gb300_plan3d(t, _i3(gdims1), _i3(mo1), self.dcs1, _i3(gdims2), _i3(mo2), self.dcs2)
+        if h < 0:
+            check(-1)
+        self.handle = h
+        a, b, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        lib().p3dfft_gb300_plan3d_types(h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(p))
+        self.dt1, self.dt2, self.prec = a.value, b.value, p.value
+
+    def stages(self):
+        buf = (ctypes.c_int * (16 * 8))()
+        n = lib().p3dfft_gb300_plan3d_stages(self.handle, buf, 8)
+        out = []
+        for s in range(n):
+            q = buf[16 * s:16 * s + 16]
+            out.append(dict(type=q[0], dim=q[1], gdims1=tuple(q[2:5]), mo1=tuple(q[5:8]), dcs1=q[8],
+                            gdims2=tuple(q[9:12]), mo2=tuple(q[12:15]), dcs2=q[15]))
+        return out
+
+    def in_dtype(self):
+        return _np_dtype(self.dt1, self.prec)
+
+    def out_dtype(self):
+        return _np_dtype(self.dt2, self.prec)
+
+    def in_shape(self):
+        return storage_shape(self.gdims1, self.mo1)
+
+    def out_shape(self):
+        return storage_shape(self.gdims2, self.mo2)
+
+    def exec(self, inp, out=None, OW=False, idir=-1):
+        if out is None:
+            out = np.empty(self.out_shape(), self.out_dtype())
+        pi, _k1 = _ptr(inp)
+        po, _k2 = _ptr(out)
+        rc = lib().p3dfft_gb300_exec3d(self.handle, pi, po, int(idir), 1 if OW else 0)
+        check(rc)
+        return out
+
+    def exec_deriv(self, inp, out=None, idir=0, OW=False):
+        return self.exec(inp, out, OW=OW, idir=idir)
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", -1) >= 0 and _lib is not None:
+                _lib.p3dfft_gb300_destroy3d(self.handle)
+        except Exception:
+            pass
+
+
+class TransPlan:
+    """transplan<T1,T2>: one 1D transform with a local reorder (reference templ.C:900-1075)."""
+
+    def __init__(self, type_id, gdims1, mo1, gdims2, mo2, dim, dcs1=-1, dcs2=-1):
+        setup()
+        self.type_id = int(type_id)
+        self.gdims1, self.mo1 = tuple(gdims1), tuple(mo1)
+        self.gdims2, self.mo2 = tuple(gdims2), tuple(mo2)
+        self.dim = int(dim)
+        h = lib().p3dfft_gb300_plan1d(self.type_id, _i3(gdims1), _i3(mo1), int(dcs1), _i3(gdims2), _i3(mo2),
+                                      int(dcs2), self.dim)
+        if h < 0:
+            check(-1)
+        self.handle = h
+
+    def exec(self, inp, out, OW=False):
+        pi, _k1 = _ptr(inp)
+        po, _k2 = _ptr(out)
+        check(lib().p3dfft_gb300_exec1d(self.handle, pi, po, 1 if OW else 0))
+        return out
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", -1) >= 0 and _lib is not None:
+                _lib.p3dfft_gb300_destroy1d(self.handle)
+        except Exception:
+            pass
+
+
+def compute_deriv(inp, out, gdims, mo, dcs, idir, prec=8):
+    pi, _k1 = _ptr(inp)
+    po, _k2 = _ptr(out)
+    check(lib().p3dfft_gb300_compute_deriv(int(prec), pi, po, _i3(gdims), _i3(mo), int(dcs), int(idir)))
+    return out
+
+
+def _np_dtype(dt, prec):
+    if dt == 2:
+        return np.complex128 if prec == 8 else np.complex64
+    return np.float64 if prec == 8 else np.float32
