@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark: 512^3 FP64 R2C -> (fused d/dz) -> C2R round trip of the P3DFFT++ pipeline.
+
+One step = transform3D<double,complex_double>::exec_deriv (x R2C, y C2C, z C2C with the i*k_z
+multiply fused into the z stage) followed by transform3D<complex_double,double>::exec (y C2C,
+z C2C, x C2R), memory orders as in the reference sample test3D_r2c.C ((0,1,2) <-> (1,2,0)).
+
+metric  GB/s of algorithmic traffic: the 3-pass pencil model, one HBM read + write per stage:
+        round trip = 2*S_r + 10*S_c = 12,926,844,928 B at 512^3 FP64 (derivative adds 0).
+value   device-resident buffers (inputs > L2, no flush needed), CUDA events on the library's
+        stream, max over ranks.
+e2e     same metric through the public C ABI with pinned HOST input and output buffers:
+        H2D of the real field + forward + backward + D2H of the result inside the timed region.
+
+--impl reference times the reference's CPU path for this workload on the host cores: the CPU
+oracle (a plain-C restatement of the reference pipeline; FFTW and MPI, which the reference
+needs, are absent on both machines) over a bounded sample of the same stages.
+Multi-GPU: independent replicas (the path has no inter-GPU exchange on one rank's grid).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "p3dfft.3_gb300")
+sys.path.insert(0, PKG)
+
+N = int(os.environ.get("P3D_BENCH_N", "512"))
+GD = tuple(int(v) for v in os.environ.get("P3D_BENCH_DIMS", f"{N},{N},{N}").split(","))
+GD2 = (GD[0] // 2 + 1, GD[1], GD[2])
+MO1, MO2 = (0, 1, 2), (1, 2, 0)
+FWD = (5, 9, 9)    # R2CFFT_D, CFFT_FORWARD_D, CFFT_FORWARD_D
+BWD = (7, 11, 11)  # C2RFFT_D, CFFT_BACKWARD_D, CFFT_BACKWARD_D
+IDIR = 2           # d/dz, fused into the last forward stage
+S_R = 8 * GD[0] * GD[1] * GD[2]
+S_C = 16 * GD2[0] * GD2[1] * GD2[2]
+ALG_BYTES = 2 * S_R + 10 * S_C
+METRIC = "3D R2C+C2R GB/s (512^3 FP64 round trip with fused d/dz, 3-pass algorithmic bytes)"
+WORKLOAD = f"{GD[0]}x{GD[1]}x{GD[2]} FP64 R2C/C2C/C2C + fused d/dz -> C2C/C2C/C2R round trip, memory orders (0,1,2)<->(1,2,0)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    """CPU reference arm: the oracle port of the reference path on all host cores."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    cores = os.cpu_count() or 1
+    runners = []
+    for types, g1, m1, d1, g2, m2, d2, idir in ((FWD, GD, MO1, -1, GD2, MO2, 0, IDIR),
+                                                (BWD, GD2, MO2, 0, GD, MO1, -1, -1)):
+        for st in pyoracle.OraclePlan(types, g1, m1, g2, m2, d1, d2).stages():
+            run, b_in, b_out, nlines = pyoracle.stage_lines_runner(st, nthreads=cores)
+            runners.append((run, b_in, b_out, nlines, st["dim"] == idir))
+    frac = float(os.environ.get("P3D_REF_SAMPLE", "0.0625"))
+
+    def step():
+        nb = 0
+        for run, b_in, b_out, nlines, deriv in runners:
+            m = max(1, int(nlines * frac))
+            run(0, m, deriv)
+            nb += (b_in + b_out) * m / nlines
+        return nb
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    nbytes = 0.0
+    for _ in range(args.steps):
+        nbytes += step()
+    dt = time.perf_counter() - t0
+    value = nbytes / dt / 1e9
+    sample = (f"{frac:.4f} of the lines of each of the 6 stages of the {N}^3 round trip per step "
+              f"(oracle C port, OpenMP {cores} threads)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample():
+    """Oracle port timed on a bounded sample (1/8 of the lines of every stage), all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    cores = os.cpu_count() or 1
+    frac = 0.125
+    t_tot, b_tot = 0.0, 0.0
+    for types, g1, m1, d1, g2, m2, d2, idir in ((FWD, GD, MO1, -1, GD2, MO2, 0, IDIR),
+                                                (BWD, GD2, MO2, 0, GD, MO1, -1, -1)):
+        for st in pyoracle.OraclePlan(types, g1, m1, g2, m2, d1, d2).stages():
+            run, b_in, b_out, nlines = pyoracle.stage_lines_runner(st, nthreads=cores)
+            m = max(1, int(nlines * frac))
+            run(0, m, st["dim"] == idir)  # warm
+            t0 = time.perf_counter()
+            run(0, m, st["dim"] == idir)
+            t_tot += time.perf_counter() - t0
+            b_tot += (b_in + b_out) * m / nlines
+    return {"value": b_tot / t_tot / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"1/8 of the lines of each of the 6 stages of the {N}^3 FP64 round trip "
+                      f"(CPU oracle port, OpenMP {cores} threads, {t_tot:.2f} s)"}
+
+
+def load_traffic(kernel_key):
+    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel_key)
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--arith", default="auto", choices=["auto", "df", "native"],
+                    help="FP64 arithmetic: float-float (df) or native DFMA; auto = df")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import ctypes
+
+    import p3dfft_gb300 as p3d
+    import build_lib
+    build_lib.build()
+    L = p3d.lib()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = (torch, tdist)
+    else:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", "0"))
+
+    arith = 0 if args.arith == "native" else 1
+    p3d.set_fp64_arith(arith)
+    f = p3d.Transform3D(FWD, GD, MO1, GD2, MO2, -1, 0)
+    b = p3d.Transform3D(BWD, GD2, MO2, GD, MO1, 0, -1)
+    x = np.random.default_rng(512 + rank).uniform(-1.0, 1.0, p3d.storage_shape(GD, MO1))
+    d_in = p3d.DeviceArray(S_R)
+    d_spec = p3d.DeviceArray(S_C)
+    d_out = p3d.DeviceArray(S_R)
+    d_in.upload(x)
+
+    def step(fin, fout):
+        p3d.check(L.p3dfft_gb300_exec3d(f.handle, ctypes.c_void_p(fin), ctypes.c_void_p(d_spec.ptr), IDIR, 0))
+        p3d.check(L.p3dfft_gb300_exec3d(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(fout), -1, 0))
+
+    def barrier():
+        if dist:
+            dist[0].cuda.synchronize()
+            dist[1].barrier()
+
+    def max_over_ranks(v):
+        if not dist:
+            return v
+        t = dist[0].tensor([v], dtype=dist[0].float64, device="cuda")
+        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident timed region ----
+    p3d.set_sync(False)
+    for _ in range(args.warmup):
+        step(d_in.ptr, d_out.ptr)
+    L.p3dfft_gb300_synchronize()
+    barrier()
+    k0 = p3d.kernel_count()
+    with ClockSampler(local) as clk:
+        L.p3dfft_gb300_synchronize()
+        L.p3dfft_gb300_event_record(0)
+        for _ in range(args.steps):
+            step(d_in.ptr, d_out.ptr)
+        L.p3dfft_gb300_event_record(1)
+        ms = L.p3dfft_gb300_event_elapsed_ms(0, 1)
+        L.p3dfft_gb300_synchronize()
+    launches = p3d.kernel_count() - k0
+    barrier()
+    ms_step = max_over_ranks(ms / args.steps)
+    value = ALG_BYTES * world / (ms_step * 1e-3) / 1e9
+    clocks = clk.summary()
+
+    # ---- full-size properties: normalised round trip recovers the derivative field ----
+    y = np.empty(p3d.storage_shape(GD, MO1), np.float64)
+    d_out.download(y)
+
+    # ---- per-stage profile (dominant kernel for the roofline) ----
+    nst_f = len(f.stages())
+    ms_f = (ctypes.c_double * 8)()
+    ms_b = (ctypes.c_double * 8)()
+    L.p3dfft_gb300_profile_stages(f.handle, ctypes.c_void_p(d_in.ptr), ctypes.c_void_p(d_spec.ptr), IDIR, 5, ms_f, 8)
+    L.p3dfft_gb300_profile_stages(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(d_out.ptr), -1, 5, ms_b, 8)
+    stages = []
+    for plan, msv in ((f, ms_f), (b, ms_b)):
+        for i, st in enumerate(plan.stages()):
+            dt1 = 1 if st["type"] in (5,) else 2
+            dt2 = 1 if st["type"] in (7,) else 2
+            bytes_ = 8 * (dt1 * int(np.prod(st["gdims1"])) + dt2 * int(np.prod(st["gdims2"])))
+            stages.append({"dim": st["dim"], "type": st["type"], "ms": msv[i], "bytes": bytes_,
+                           "gbs": bytes_ / (msv[i] * 1e-3) / 1e9 if msv[i] > 0 else None})
+    dom = max(range(len(stages)), key=lambda i: stages[i]["ms"])
+    peak, peak_kind = measured_peak()
+    ds = stages[dom]
+    kernel_key = f"k_stage<{'DF' if arith else 'Native<double>'}> stage{dom} dim{ds['dim']} type{ds['type']}"
+    traffic = load_traffic(kernel_key)
+    roofline = {"bound": "hbm", "achieved": ds["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": ds["gbs"] / peak if ds["gbs"] else None, "traffic": traffic,
+                "kernel": kernel_key, "peak_source": peak_kind,
+                "bytes_per_launch": ds["bytes"], "ms_per_launch": ds["ms"],
+                "whole_step_frac": value / world / peak,
+                "stages_ms": [round(s["ms"], 4) for s in stages]}
+
+    # ---- e2e: pinned host buffers through the public API ----
+    hin = p3d.PinnedArray(p3d.storage_shape(GD, MO1), np.float64)
+    hout = p3d.PinnedArray(p3d.storage_shape(GD, MO1), np.float64)
+    hin.array[...] = x
+    n_e2e = max(3, min(args.steps, 20))
+    for _ in range(2):
+        step(hin.ptr, hout.ptr)
+    L.p3dfft_gb300_synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        step(hin.ptr, hout.ptr)  # host pointers: H2D inside exec_deriv, D2H inside exec (synchronous)
+    L.p3dfft_gb300_synchronize()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / n_e2e * 1e3)
+    e2e = {"value": ALG_BYTES * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": S_R,
+           "d2h_bytes_per_step": S_R, "ms_per_step": e2e_ms}
+    rt_err = float(np.linalg.norm(hout.array - y) / max(np.linalg.norm(y), 1e-300))
+
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": list(GD), "types_forward": "R2C_D,CFFT_FORWARD_D,CFFT_FORWARD_D",
+                       "types_backward": "C2R_D,CFFT_BACKWARD_D,CFFT_BACKWARD_D", "deriv": "d/dz fused",
+                       "fp64_arith": "float-float (FP32 pipe, ~48-bit)" if arith else "native FP64 (DFMA)",
+                       "l2": "inputs larger than L2 (1.07 GB real field, 1.08 GB spectrum); no flush",
+                       "input": "numpy PCG64 U[-1,1) seed 512+rank", "parallelism": f"replicas x{world}",
+                       "algorithmic_bytes_per_step": ALG_BYTES},
+            "roofline": roofline, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+            "host_vs_device_rel_diff": rt_err}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist[1].destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

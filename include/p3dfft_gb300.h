@@ -70,9 +70,20 @@ void p3dfft_gb300_reset_kernel_count(void);
 void p3dfft_gb300_enable_timers(int on);
 double p3dfft_gb300_timer(int phase);
 void p3dfft_gb300_reset_timers(void);
+/* CUDA events on the library's stream (slots 0..63), for timing from a caller without its
+ * own CUDA runtime; elapsed_ms synchronises on event b and returns -1 on error */
+int p3dfft_gb300_event_record(int slot);
+double p3dfft_gb300_event_elapsed_ms(int a, int b);
+/* Runs a 3D plan `reps` times on device-resident buffers with an event between stages and
+ * returns the stage count; ms[s] = average duration of stage s in milliseconds. */
+int p3dfft_gb300_profile_stages(int plan, const void *in, void *out, int idir, int reps, double *ms,
+                                int max_stages);
 /* device-memory helpers for callers without a CUDA runtime of their own */
 void *p3dfft_gb300_device_alloc(long long bytes);
 void p3dfft_gb300_device_free(void *p);
+/* page-locked host memory (fast staging for host-pointer execs) */
+void *p3dfft_gb300_host_alloc_pinned(long long bytes);
+void p3dfft_gb300_host_free_pinned(void *p);
 int p3dfft_gb300_memcpy_h2d(void *dst, const void *src, long long bytes);
 int p3dfft_gb300_memcpy_d2h(void *dst, const void *src, long long bytes);
 int p3dfft_gb300_synchronize(void);

@@ -510,6 +510,12 @@ static void strides_of(const orc_grid *g, long long s[3])
 
 int orc_exec_stage(const orc_stage *S, const double *in, double *out, int deriv, int nthreads)
 {
+  return orc_exec_stage_lines(S, in, out, deriv, nthreads, 0, -1);
+}
+
+int orc_exec_stage_lines(const orc_stage *S, const double *in, double *out, int deriv, int nthreads,
+                         long long line0, long long line1)
+{
   orc_type_info ti;
   int L = S->dim, a, b, nin, nout, nlog, kind;
   long long s1[3], s2[3], na, nb, line;
@@ -544,8 +550,9 @@ int orc_exec_stage(const orc_stage *S, const double *in, double *out, int deriv,
     double *lout = (double *)malloc(sizeof(double) * 2 * maxn);
     double *work = (double *)malloc(sizeof(double) * (4 * (size_t)maxn + 2 * maxp + 8));
     long long ln;
+    long long lend = (line1 < 0 || line1 > na * nb) ? na * nb : line1;
 #pragma omp for schedule(static)
-    for (ln = 0; ln < na * nb; ln++) {
+    for (ln = line0; ln < lend; ln++) {
       long long ia = ln % na, ib = ln / na, j;
       long long o1 = ia * s1[a] + ib * s1[b], o2 = ia * s2[a] + ib * s2[b];
       if (ti.dt1 == 2)

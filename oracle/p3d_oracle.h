@@ -91,6 +91,10 @@ int orc_plan3d_make(const int types[3], const orc_grid *g1, const orc_grid *g2, 
 int orc_exec3d(const orc_plan3d *p, const double *in, double *out, int idir, int nthreads);
 /* One 1D stage (transplan::exec, build/exec.C:522-622) on explicit grids. */
 int orc_exec_stage(const orc_stage *s, const double *in, double *out, int deriv, int nthreads);
+/* Same, restricted to lines [line0, line1) of the stage (line = index over the two batch dims,
+ * first batch dim fastest); line1 < 0 means all lines.  Used to time bounded samples. */
+int orc_exec_stage_lines(const orc_stage *s, const double *in, double *out, int deriv, int nthreads,
+                         long long line0, long long line1);
 /* Standalone spectral derivative (build/deriv.C:85-184) on a complex field. */
 int orc_compute_deriv(const orc_grid *g, const double *in, double *out, int idir);
 

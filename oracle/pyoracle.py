@@ -84,6 +84,8 @@ def lib():
                                          ctypes.POINTER(Grid), ctypes.POINTER(Plan3D)]
         _lib.orc_exec3d.argtypes = [ctypes.POINTER(Plan3D), dp, dp, ctypes.c_int, ctypes.c_int]
         _lib.orc_exec_stage.argtypes = [ctypes.POINTER(Stage), dp, dp, ctypes.c_int, ctypes.c_int]
+        _lib.orc_exec_stage_lines.argtypes = [ctypes.POINTER(Stage), dp, dp, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_longlong, ctypes.c_longlong]
         _lib.orc_compute_deriv.argtypes = [ctypes.POINTER(Grid), dp, dp, ctypes.c_int]
         _lib.orc_type_info_get.argtypes = [ctypes.c_int, ctypes.POINTER(TypeInfo)]
         _lib.orc_swap0.argtypes = [ctypes.POINTER(ctypes.c_int * 3), ctypes.POINTER(ctypes.c_int * 3), ctypes.c_int]
@@ -225,3 +227,40 @@ def compute_deriv(x, gdims, mo, dcs, idir):
     if rc != 0:
         raise RuntimeError("oracle compute_deriv failed")
     return out.reshape(storage_shape(gdims, mo))
+
+
+_SHARED = {}
+
+
+def _shared_buf(key, n):
+    b = _SHARED.get(key)
+    if b is None or b.size < n:
+        b = np.random.default_rng(7).uniform(-1, 1, n) if key == "in" else np.empty(n, np.float64)
+        _SHARED[key] = b
+    return b
+
+
+def stage_lines_runner(stage: dict, nthreads=0):
+    """Returns (run(line0, line1, deriv), bytes_in, bytes_out, nlines) for timing a bounded sample
+    of one stage of a plan (stage dicts as returned by OraclePlan.stages()).  All runners share
+    one input and one output buffer sized for the largest stage."""
+    st = Stage()
+    st.type = stage["type"]
+    st.dim = stage["dim"]
+    st.g1 = Grid.make(stage["gdims1"], stage["mo1"], stage["dcs1"])
+    st.g2 = Grid.make(stage["gdims2"], stage["mo2"], stage["dcs2"])
+    ti = type_info(stage["type"])
+    n1 = int(np.prod(stage["gdims1"])) * ti["dt1"]
+    n2 = int(np.prod(stage["gdims2"])) * ti["dt2"]
+    inb = _shared_buf("in", n1)
+    outb = _shared_buf("out", n2)
+    L = stage["dim"]
+    nlines = int(np.prod([stage["gdims1"][i] for i in range(3) if i != L]))
+
+    def run(line0, line1, deriv=False):
+        rc = lib().orc_exec_stage_lines(ctypes.byref(st), _dp(inb), _dp(outb), int(deriv), int(nthreads),
+                                        int(line0), int(line1))
+        if rc != 0:
+            raise RuntimeError("oracle stage failed")
+
+    return run, n1 * 8, n2 * 8, nlines

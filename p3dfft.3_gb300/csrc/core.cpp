@@ -522,7 +522,7 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
   return rc;
 }
 
-static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW) {
+static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaEvent_t *stage_ev = nullptr) {
   if (!ensure_device()) return t_err;
   if (!in || !out) {
     set_err(E_BAD_ARG, "null data pointer");
@@ -590,6 +590,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW) {
     const Stage &st = P->st[s];
     bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
     void *d = dst[s];
+    if (stage_ev) cudaEventRecord(stage_ev[s], g_stream);
     if (d == src) {  // single-stage in-place call: go through scratch, then copy back
       size_t bytes = stage_out_bytes(P, st);
       if (!ensure_buf(&B.scratch[0], &B.scratch_bytes, std::max(bytes, B.scratch_bytes))) return E_CUDA;
@@ -601,6 +602,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW) {
     }
     src = d;
   }
+  if (stage_ev) cudaEventRecord(stage_ev[n], g_stream);
   if (rc != E_OK) return rc;
   if (!dout_dev) {
     TimerScope ts(5);
@@ -797,6 +799,52 @@ int p3dfft_gb300_compute_deriv(int prec, const void *in, void *out, const int gd
   return E_OK;
 }
 
+static cudaEvent_t g_events[64];
+static bool g_events_made = false;
+
+int p3dfft_gb300_event_record(int slot) {
+  if (slot < 0 || slot >= 64 || !ensure_device()) return E_BAD_ARG;
+  if (!g_events_made) {
+    for (auto &e : g_events) cudaEventCreate(&e);
+    g_events_made = true;
+  }
+  return cudaEventRecord(g_events[slot], g_stream) == cudaSuccess ? E_OK : E_CUDA;
+}
+
+double p3dfft_gb300_event_elapsed_ms(int a, int b) {
+  if (!g_events_made || a < 0 || a >= 64 || b < 0 || b >= 64) return -1.0;
+  if (cudaEventSynchronize(g_events[b]) != cudaSuccess) return -1.0;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, g_events[a], g_events[b]) != cudaSuccess) return -1.0;
+  return (double)ms;
+}
+
+int p3dfft_gb300_profile_stages(int plan, const void *in, void *out, int idir, int reps, double *ms, int max_stages) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) {
+    set_err(E_BAD_ARG, "invalid 3D plan handle %d", plan);
+    return -1;
+  }
+  if (!ensure_device()) return -1;
+  const int n = (int)P->st.size();
+  std::vector<cudaEvent_t> ev(n + 1);
+  for (auto &e : ev) cudaEventCreate(&e);
+  std::vector<double> acc(n, 0.0);
+  int rc = E_OK;
+  for (int r = 0; r < reps && rc == E_OK; r++) {
+    rc = exec_plan(P, in, out, idir, 0, ev.data());
+    cudaEventSynchronize(ev[n]);
+    for (int s = 0; s < n; s++) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[s], ev[s + 1]);
+      acc[s] += t;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (int s = 0; s < n && s < max_stages; s++) ms[s] = reps > 0 ? acc[s] / reps : 0.0;
+  return rc == E_OK ? n : -1;
+}
+
 long long p3dfft_gb300_kernel_count(void) { return g_kcount.load(); }
 void p3dfft_gb300_reset_kernel_count(void) { g_kcount = 0; }
 void p3dfft_gb300_enable_timers(int on) { g_timers_on = on != 0; }
@@ -813,6 +861,19 @@ void *p3dfft_gb300_device_alloc(long long bytes) {
     return nullptr;
   }
   return p;
+}
+void *p3dfft_gb300_host_alloc_pinned(long long bytes) {
+  if (!ensure_device()) return nullptr;
+  void *p = nullptr;
+  if (cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    set_err(E_CUDA, "pinned host allocation of %lld bytes failed", bytes);
+    return nullptr;
+  }
+  return p;
+}
+void p3dfft_gb300_host_free_pinned(void *p) {
+  if (p) cudaFreeHost(p);
 }
 void p3dfft_gb300_device_free(void *p) {
   if (p) cudaFree(p);

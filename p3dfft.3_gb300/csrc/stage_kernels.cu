@@ -17,6 +17,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -317,12 +318,84 @@ __device__ __forceinline__ typename O::C apply_deriv(const KParams &p, typename 
   return O::iscale(v, kk);
 }
 
+// Shared-memory slot of line element i: one padding slot every 2^SH elements (SH = 0: none),
+// which keeps the Stockham scatter of the register engines free of bank conflicts.
+template <int SH>
+__device__ __forceinline__ int pad(int i) {
+  return SH ? i + (i >> SH) : i;
+}
+
 // ------------------------------------------------------------------------------------------
-template <class O>
+// FFT engines.  An engine runs the complex FFT of length nfft on every line of the tile held in
+// shared memory and returns which of the two buffers holds the result.
+//
+// GenericFFT: runtime mixed-radix plan (any length), ping-pong buffers, 256 threads.
+struct GenericFFT {
+  static constexpr int PADSH = 0;
+  static constexpr bool FIXED = false;
+  template <class O>
+  __device__ static int run(const KParams &p, typename O::C *b0, typename O::C *b1, int nflines, int sign) {
+    return fft_passes<O>(p, b0, b1, nflines, sign);
+  }
+};
+
+// Register engine for power-of-two lengths known at compile time: each line is processed by
+// N/V threads holding V points in registers; pass s applies V/R radix-R butterflies per thread
+// (twiddle multiply + DFT-R in registers) and one scatter through shared memory.
+template <class O, int N, int V, int Ns, int R, int... Rest>
+__device__ __forceinline__ void fixed_pass(const KParams &p, typename O::C *line, int j, bool active, int sign) {
+  using C = typename O::C;
+  constexpr int T = N / V, NB = V / R, M = N / R;
+  C v[V];
+  if (active) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      const int jj = j + b * T;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[b * R + r] = line[pad<3>(jj + r * M)];
+      if (Ns > 1) {
+        const int k = jj & (Ns - 1);
+#pragma unroll
+        for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], twid<O>(p, r * k * (N / (Ns * R)), sign));
+      }
+      dft_reg<O, R>(&v[b * R], sign, p);
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      const int jj = j + b * T;
+      const int k = jj & (Ns - 1);
+      const int base = (jj - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) line[pad<3>(base + r * Ns)] = v[b * R + r];
+    }
+  }
+  __syncthreads();
+  if constexpr (sizeof...(Rest) > 0) fixed_pass<O, N, V, Ns * R, Rest...>(p, line, j, active, sign);
+}
+
+template <int N_, int V_, int... Rs>
+struct FixedFFT {
+  static constexpr int PADSH = 3;
+  static constexpr bool FIXED = true;
+  static constexpr int N = N_, V = V_, T = N_ / V_;
+  template <class O>
+  __device__ static int run(const KParams &p, typename O::C *b0, typename O::C *, int nflines, int sign) {
+    const int l = threadIdx.x / T, j = threadIdx.x - l * T;
+    fixed_pass<O, N, V, 1, Rs...>(p, b0 + (size_t)l * p.ls, j, l < nflines, sign);
+    return 0;
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+template <class O, class E>
 __global__ void __launch_bounds__(256) k_stage(KParams p) {
   using C = typename O::C;
   using S = typename O::S;
   using G = typename O::G;
+  constexpr int SH = E::PADSH;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *b0 = reinterpret_cast<C *>(smem_raw);
   C *b1 = b0 + (size_t)p.TB * p.nfl * p.ls;
@@ -346,11 +419,13 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
       long long off = in_off(p, lt, j, t0, ioth);
       C *line = dstbuf + (size_t)lt * p.nfl * p.ls;
       if (p.in_complex) {
-        line[j] = O::ldc(gin + 2 * off);
+        line[pad<SH>(j)] = O::ldc(gin + 2 * off);
       } else if (kind == K_R2C && !(p.nlog & 1)) {
-        reinterpret_cast<S *>(line)[j] = O::ld(gin + off);  // packed z[n] = x[2n] + i x[2n+1]
+        S v = O::ld(gin + off);  // packed z[n] = x[2n] + i x[2n+1]
+        if (j & 1) line[pad<SH>(j >> 1)].y = v;
+        else line[pad<SH>(j >> 1)].x = v;
       } else {
-        line[j] = O::mk(O::ld(gin + off), O::rzero());
+        line[pad<SH>(j)] = O::mk(O::ld(gin + off), O::rzero());
       }
     }
   }
@@ -362,7 +437,7 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
       for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
         int lt = idx / M, k = idx - lt * M;
         const C *X = b1 + (size_t)lt * p.ls;
-        C a = X[k], b = X[M - k];
+        C a = X[pad<SH>(k)], b = X[pad<SH>(M - k)];
         if (k == 0) {
           a.y = O::rzero();
           b.y = O::rzero();
@@ -370,10 +445,8 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
         C bc = O::conj(b);
         C s = O::add(a, bc), d = O::sub(a, bc);
         C w = O::conj(O::tw(reinterpret_cast<const typename O::T *>(p.tw), k));  // W_N^-k
-        b0[(size_t)lt * p.ls + k] = O::add(s, O::muli(O::mul(w, d)));
+        b0[(size_t)lt * p.ls + pad<SH>(k)] = O::add(s, O::muli(O::mul(w, d)));
       }
-    } else if (kind == K_C2R) {
-      // unreachable: odd C2R is direct
     } else if (kind == K_R2R && p.r2r == REDFT00) {
       // even extension of length M = 2(n-1)
       const int n = p.nin, M = p.nfft;
@@ -381,7 +454,7 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
       for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
         int lt = idx / M, j = idx - lt * M;
         const C *x = b1 + (size_t)lt * p.ls;
-        b0[(size_t)lt * p.ls + j] = (j < n) ? x[j] : x[M - j];
+        b0[(size_t)lt * p.ls + pad<SH>(j)] = (j < n) ? x[pad<SH>(j)] : x[pad<SH>(M - j)];
       }
     } else if (kind == K_R2R && p.r2r == RODFT00) {
       // odd extension of length M = 2(n+1): [0, x0..x_{n-1}, 0, -x_{n-1}..-x0]
@@ -392,9 +465,9 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
         const C *x = b1 + (size_t)lt * p.ls;
         C v;
         if (j == 0 || j == n + 1) v = O::zero();
-        else if (j <= n) v = x[j - 1];
-        else v = O::neg(x[M - j - 1]);
-        b0[(size_t)lt * p.ls + j] = v;
+        else if (j <= n) v = x[pad<SH>(j - 1)];
+        else v = O::neg(x[pad<SH>(M - j - 1)]);
+        b0[(size_t)lt * p.ls + pad<SH>(j)] = v;
       }
     } else if (kind == K_R2R) {
       // generic kinds II/III/IV: u_j = x_j exp(-i pi beta j / n'), zero padded to 2n'.
@@ -407,15 +480,15 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
         const C *x = b1 + (size_t)lt * p.nfl * p.ls;
         C u = O::zero(), uc = O::zero();
         if (j < n) {
-          C xv = x[j];
+          C xv = x[pad<SH>(j)];
           if ((p.r2r_halffirst && j == 0) || (p.r2r_halflast && j == n - 1)) xv = O::half(xv);
           C w = O::tw(aux, 2 * p.r2r_b2 * j);
           u = O::mul(xv, w);
           uc = O::mul(O::conj(xv), w);
         }
         C *fl = b0 + (size_t)lt * p.nfl * p.ls;
-        fl[j] = u;
-        if (p.nfl == 2) fl[p.ls + j] = uc;
+        fl[pad<SH>(j)] = u;
+        if (p.nfl == 2) fl[p.ls + pad<SH>(j)] = uc;
       }
     }
     __syncthreads();
@@ -427,13 +500,13 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
       int lt = idx / N, k = idx - lt * N;
       C *X = b0 + (size_t)lt * p.ls;
       if (k == 0) X[0].y = O::rzero();
-      else if (k >= h) X[k] = O::conj(X[N - k]);
+      else if (k >= h) X[pad<SH>(k)] = O::conj(X[pad<SH>(N - k)]);
     }
     __syncthreads();
   }
 
-  // ---------------- FFT passes ----------------
-  const int cur = fft_passes<O>(p, b0, b1, nlines * p.nfl, p.sign);
+  // ---------------- FFT ----------------
+  const int cur = E::template run<O>(p, b0, b1, nlines * p.nfl, p.sign);
   const C *res = cur ? b1 : b0;
 
   // ---------------- post-processing + scatter ----------------
@@ -444,14 +517,15 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
     const C *Y = res + (size_t)lt * p.nfl * p.ls;
     long long off = out_off(p, lt, k, t0, ioth);
     if (kind == K_C2C_FWD || kind == K_C2C_BWD) {
-      O::stc(gout + 2 * off, apply_deriv<O>(p, Y[k], k));
+      O::stc(gout + 2 * off, apply_deriv<O>(p, Y[pad<SH>(k)], k));
     } else if (kind == K_R2C) {
       C v;
       if (p.nlog & 1) {
-        v = Y[k];
+        v = Y[pad<SH>(k)];
       } else {
         const int M = p.nfft;
-        C a = Y[k % M], b = O::conj(Y[(M - k) % M]);
+        const int k1 = (k == M) ? 0 : k, k2 = (k == 0) ? 0 : M - k;
+        C a = Y[pad<SH>(k1)], b = O::conj(Y[pad<SH>(k2)]);
         C w = O::tw(reinterpret_cast<const typename O::T *>(p.tw), k);  // W_N^k
         C s = O::add(a, b), d = O::sub(a, b);
         v = O::half(O::sub(s, O::muli(O::mul(w, d))));
@@ -459,21 +533,21 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
       O::stc(gout + 2 * off, apply_deriv<O>(p, v, k));
     } else if (kind == K_C2R) {
       S v;
-      if (p.nlog & 1) v = Y[k].x;
-      else v = (k & 1) ? Y[k >> 1].y : Y[k >> 1].x;
+      if (p.nlog & 1) v = Y[pad<SH>(k)].x;
+      else v = (k & 1) ? Y[pad<SH>(k >> 1)].y : Y[pad<SH>(k >> 1)].x;
       O::st(gout + off, v);
     } else {  // K_R2R
       C v;
       if (p.r2r == REDFT00) {
-        v = Y[k];
+        v = Y[pad<SH>(k)];
       } else if (p.r2r == RODFT00) {
-        v = O::muli(Y[k + 1]);
+        v = O::muli(Y[pad<SH>(k + 1)]);
       } else {
         const typename O::T *aux = reinterpret_cast<const typename O::T *>(p.aux);
         C w = O::tw(aux, p.r2r_a2 * (2 * k + p.r2r_b2));
-        C sm = O::mul(w, Y[k]);  // S-_k
+        C sm = O::mul(w, Y[pad<SH>(k)]);  // S-_k
         C sp;
-        if (p.nfl == 2) sp = O::conj(O::mul(w, Y[p.ls + k]));
+        if (p.nfl == 2) sp = O::conj(O::mul(w, Y[p.ls + pad<SH>(k)]));
         else sp = O::conj(sm);
         v = p.r2r_sin ? O::mulmi(O::sub(sp, sm)) : O::add(sp, sm);
       }
@@ -595,16 +669,46 @@ static void factorize(int n, std::vector<int> &rad) {
 
 int max_line_len(int prec) { return prec == 8 ? 6144 : 12288; }
 
-template <class O>
-static int launch_k(const KParams &p, size_t smem, int grid, cudaStream_t st) {
+template <class O, class E>
+static int launch_k(const KParams &p, size_t smem, int grid, int threads, cudaStream_t st) {
   static int configured_smem = 0;  // per instantiation
   if ((int)smem > configured_smem) {
-    if (cudaFuncSetAttribute(k_stage<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_stage<O, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return E_CUDA;
     configured_smem = (int)smem;
   }
-  k_stage<O><<<grid, 256, smem, st>>>(p);
+  k_stage<O, E><<<grid, threads, smem, st>>>(p);
   return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+}
+
+// Register engines available for a complex FFT length (power-of-two lengths 16..4096)
+static bool fixed_engine_len(int n) {
+  switch (n) {
+    case 16: case 32: case 64: case 128: case 256: case 512: case 1024: case 2048: case 4096: return true;
+    default: return false;
+  }
+}
+
+template <class O>
+static int launch_fixed(const KParams &p, size_t smem, int grid, int threads, cudaStream_t st) {
+  switch (p.nfft) {
+    case 16: return launch_k<O, FixedFFT<16, 4, 4, 4>>(p, smem, grid, threads, st);
+    case 32: return launch_k<O, FixedFFT<32, 8, 8, 4>>(p, smem, grid, threads, st);
+    case 64: return launch_k<O, FixedFFT<64, 8, 8, 8>>(p, smem, grid, threads, st);
+    case 128: return launch_k<O, FixedFFT<128, 8, 8, 8, 2>>(p, smem, grid, threads, st);
+    case 256: return launch_k<O, FixedFFT<256, 8, 8, 8, 4>>(p, smem, grid, threads, st);
+    case 512: return launch_k<O, FixedFFT<512, 8, 8, 8, 8>>(p, smem, grid, threads, st);
+    case 1024: return launch_k<O, FixedFFT<1024, 8, 8, 8, 8, 2>>(p, smem, grid, threads, st);
+    case 2048: return launch_k<O, FixedFFT<2048, 8, 8, 8, 8, 4>>(p, smem, grid, threads, st);
+    case 4096: return launch_k<O, FixedFFT<4096, 8, 8, 8, 8, 8>>(p, smem, grid, threads, st);
+    default: return E_UNSUPPORTED;
+  }
+}
+
+template <class O>
+static int launch_any(const KParams &p, bool fixed, size_t smem, int grid, int threads, cudaStream_t st) {
+  if (fixed) return launch_fixed<O>(p, smem, grid, threads, st);
+  return launch_k<O, GenericFFT>(p, smem, grid, threads, st);
 }
 
 int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
@@ -733,23 +837,36 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   p.dother = d.d1[o];
 
   const size_t csz = (d.prec == 4) ? 8 : 16;
+  const bool fixed = fixed_engine_len(p.nfft) && !getenv("P3DFFT_GB300_GENERIC_ONLY");
   int slots = p.nfft;
   if (p.nin > slots) slots = p.nin;
   if (p.nout > slots) slots = p.nout;
   if (d.kind == K_C2R) slots = std::max(slots, p.nfft + 1);
+  if (fixed) slots += slots / 8 + 1;  // padding slots of the register engine
   p.ls = slots;
-  const size_t per_line = 2 * (size_t)p.nfl * p.ls * csz;
+  // the register engine needs the second buffer only for kinds with a pre-processing step
+  const bool need_b1 = !fixed || d.kind == K_R2R || (d.kind == K_C2R && !(p.nlog & 1));
+  const size_t per_line = (need_b1 ? 2 : 1) * (size_t)p.nfl * p.ls * csz;
   const size_t smem_cap = 110 * 1024;
-  int TB;
-  if (!p.load_Lmajor || !p.store_Lmajor) {
+  int TB, threads = 256;
+  if (fixed) {
+    const int T = p.nfft / (p.nfft == 16 ? 4 : 8);  // threads per FFT line
+    TB = std::max(1, 256 / (T * p.nfl));
+    while (TB > 1 && per_line * TB > smem_cap) TB /= 2;
+    threads = TB * p.nfl * T;
+    if (threads > 1024 || threads < 32) {
+      // fall back to the generic engine for shapes the register engine cannot tile
+      return E_UNSUPPORTED;
+    }
+  } else if (!p.load_Lmajor || !p.store_Lmajor) {
     int esz = (int)((p.in_complex ? 2 : 1) * d.prec);
     TB = std::max(2, 64 / esz);
   } else {
     TB = std::max(1, 2048 / std::max(1, p.nfft));
   }
-  while (TB > 1 && per_line * TB > smem_cap) TB--;
+  while (!fixed && TB > 1 && per_line * TB > smem_cap) TB--;
   if (per_line * TB > 227 * 1024) return E_TOO_LARGE;
-  if (TB > p.dt) TB = p.dt;
+  if (!fixed && TB > p.dt) TB = p.dt;
   if (TB < 1) TB = 1;
   p.TB = TB;
   p.ntile = (p.dt + TB - 1) / TB;
@@ -758,9 +875,9 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   if (grid > 0x7fffffffLL) return E_TOO_LARGE;
   size_t smem = per_line * TB;
   int rc;
-  if (d.prec == 4) rc = launch_k<Native<float>>(p, smem, (int)grid, stream);
-  else if (arith == AR_DF) rc = launch_k<DF>(p, smem, (int)grid, stream);
-  else rc = launch_k<Native<double>>(p, smem, (int)grid, stream);
+  if (d.prec == 4) rc = launch_any<Native<float>>(p, fixed, smem, (int)grid, threads, stream);
+  else if (arith == AR_DF) rc = launch_any<DF>(p, fixed, smem, (int)grid, threads, stream);
+  else rc = launch_any<Native<double>>(p, fixed, smem, (int)grid, threads, stream);
   if (rc == E_OK && kernels_launched) (*kernels_launched)++;
   return rc;
 }

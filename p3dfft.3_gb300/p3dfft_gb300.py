@@ -76,6 +76,11 @@ def lib():
         "p3dfft_gb300_memcpy_h2d": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
         "p3dfft_gb300_memcpy_d2h": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
         "p3dfft_gb300_synchronize": ([], ctypes.c_int), "p3dfft_gb300_version": ([], ctypes.c_char_p),
+        "p3dfft_gb300_host_alloc_pinned": ([ctypes.c_longlong], vp), "p3dfft_gb300_host_free_pinned": ([vp], None),
+        "p3dfft_gb300_event_record": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_event_elapsed_ms": ([ctypes.c_int, ctypes.c_int], ctypes.c_double),
+        "p3dfft_gb300_profile_stages": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_double), ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -241,3 +246,56 @@ def _np_dtype(dt, prec):
     if dt == 2:
         return np.complex128 if prec == 8 else np.complex64
     return np.float64 if prec == 8 else np.float32
+
+
+class DeviceArray:
+    """A device allocation made by the library (no torch needed); frees on deletion."""
+
+    def __init__(self, nbytes: int):
+        self.nbytes = int(nbytes)
+        p = lib().p3dfft_gb300_device_alloc(self.nbytes)
+        if not p:
+            check(-1)
+        self.ptr = int(p)
+
+    def data_ptr(self):
+        return self.ptr
+
+    def upload(self, a: np.ndarray):
+        a = np.ascontiguousarray(a)
+        assert a.nbytes <= self.nbytes
+        check(lib().p3dfft_gb300_memcpy_h2d(ctypes.c_void_p(self.ptr), ctypes.c_void_p(a.ctypes.data), a.nbytes))
+
+    def download(self, a: np.ndarray):
+        assert a.flags.c_contiguous and a.nbytes <= self.nbytes
+        check(lib().p3dfft_gb300_memcpy_d2h(ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(self.ptr), a.nbytes))
+        return a
+
+    def __del__(self):
+        try:
+            if _lib is not None and self.ptr:
+                _lib.p3dfft_gb300_device_free(ctypes.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+class PinnedArray:
+    """numpy view over page-locked host memory allocated by the library."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        p = lib().p3dfft_gb300_host_alloc_pinned(n)
+        if not p:
+            check(-1)
+        self.ptr = int(p)
+        buf = (ctypes.c_char * n).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def __del__(self):
+        try:
+            if _lib is not None and self.ptr:
+                self.array = None
+                _lib.p3dfft_gb300_host_free_pinned(ctypes.c_void_p(self.ptr))
+        except Exception:
+            pass
