@@ -59,6 +59,22 @@ int p3dfft_gb300_destroy1d(int plan);
 int p3dfft_gb300_compute_deriv(int prec, const void *in, void *out, const int gdims[3],
                                const int mo[3], int dcs, int idir);
 
+/* ---- allocation-free execution (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc (an application that gives all device memory to its own
+ * allocator at start-up, a real-time loop that may not take cudaMalloc's implicit device
+ * synchronisation, a plugin host that forbids device allocations): runs a 3D plan like
+ * p3dfft_gb300_exec3d, with
+ * the intermediate fields and twiddle tables in a static device array of
+ * P3DFFT_GB300_NOALLOC_BYTES that every GPU loading the library holds until exit.  `in` and
+ * `out` must be device memory; each intermediate field must fit in
+ * p3dfft_gb300_noalloc_max_field_bytes() (about 95 MiB, e.g. a 128^3 or 256x256x128 FP64
+ * R2C round trip), larger transforms are rejected with P3DFFT_ERR_TOO_LARGE.  The first call on
+ * a device resolves the array's device address (cudaGetSymbolAddress) and should come before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+#define P3DFFT_GB300_NOALLOC_BYTES (192ull << 20)
+int p3dfft_gb300_exec3d_noalloc(int plan, const void *in, void *out, int idir);
+long long p3dfft_gb300_noalloc_max_field_bytes(void);
+
 /* ---- introspection and timers ---- */
 /* number of kernels this library launched since the last reset */
 long long p3dfft_gb300_kernel_count(void);

@@ -26,7 +26,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
 
-SOURCES = ["stage_kernels.cu", "core.cpp"]
+SOURCES = ["stage_kernels.cu", "core.cpp", "noalloc.cu"]
 HEADERS = ["kernels.h", "df_arith.cuh"]
 
 

@@ -476,7 +476,25 @@ struct TimerScope {
   }
 };
 
-static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv) {
+static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc &d) {
+  const TypeInfo &t = g_types[s.type];
+  d.kind = t.kind;
+  d.r2r = t.r2r;
+  d.prec = P->prec;
+  d.dt1 = t.dt1;
+  d.dt2 = t.dt2;
+  d.L = s.dim;
+  for (int i = 0; i < 3; i++) {
+    d.d1[i] = s.g1.gdims[i];
+    d.d2[i] = s.g2.gdims[i];
+  }
+  strides(s.g1, d.s1);
+  strides(s.g2, d.s2);
+  d.deriv = deriv ? 1 : 0;
+}
+
+static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv,
+                     const void *tw_given = nullptr, const void *aux_given = nullptr) {
   const TypeInfo &t = g_types[s.type];
   int launched = 0;
   int rc = E_OK;
@@ -495,22 +513,11 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
     }
   } else {
     StageDesc d;
-    d.kind = t.kind;
-    d.r2r = t.r2r;
-    d.prec = P->prec;
-    d.dt1 = t.dt1;
-    d.dt2 = t.dt2;
-    d.L = s.dim;
-    for (int i = 0; i < 3; i++) {
-      d.d1[i] = s.g1.gdims[i];
-      d.d2[i] = s.g2.gdims[i];
-    }
-    strides(s.g1, d.s1);
-    strides(s.g2, d.s2);
-    d.deriv = deriv ? 1 : 0;
+    fill_stage_desc(P, s, deriv, d);
     bool reorder = !(s.g1.mo[0] == s.g2.mo[0] && s.g1.mo[1] == s.g2.mo[1] && s.g1.mo[2] == s.g2.mo[2]);
     TimerScope ts(deriv ? 3 : (reorder ? 1 : 0));
-    rc = launch_stage(d, src, dst, P->prec == 8 ? arith_mode() : AR_NATIVE, g_stream, g_tabs, &launched);
+    rc = launch_stage(d, src, dst, P->prec == 8 ? arith_mode() : AR_NATIVE, g_stream, g_tabs, &launched, tw_given,
+                      aux_given);
   }
   g_kcount += launched;
   if (rc != E_OK) {
@@ -632,6 +639,97 @@ static int store_plan(std::vector<Plan *> &v, Plan *P) {
   v.push_back(P);
   return (int)v.size() - 1;
 }
+
+// Runs a 3D plan entirely in caller-provided device memory: `scratch0` / `scratch1` hold the
+// intermediate fields (each `scratch_bytes` long) and `tw_dev` (tw_bytes) the twiddle tables,
+// which are generated into `tw_host` and copied in stream order.  Makes no device allocation.
+int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *scratch0, void *scratch1,
+                           size_t scratch_bytes, void *tw_dev, size_t tw_bytes, void *tw_host) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) {
+    set_err(E_BAD_ARG, "invalid 3D plan handle %d", plan);
+    return E_BAD_ARG;
+  }
+  if (idir > 2) {
+    set_err(E_BAD_ARG, "derivative direction %d out of range", idir);
+    return E_BAD_ARG;
+  }
+  if (!in || !out || !is_device_ptr(in) || !is_device_ptr(out)) {
+    set_err(E_BAD_ARG, "this entry point takes device pointers only (host data would need staging buffers)");
+    return E_BAD_ARG;
+  }
+  const int n = (int)P->st.size();
+  const size_t out_bytes = (size_t)elems(P->g2) * P->dt2 * P->prec;
+  // buffer assignment as in exec_plan, with the two given scratch buffers
+  void *dst[8];
+  dst[n - 1] = out;
+  for (int s = n - 2; s >= 0; s--) {
+    size_t bytes = stage_out_bytes(P, P->st[s]);
+    if (out != dst[s + 1] && out != in && bytes <= out_bytes) dst[s] = out;
+    else dst[s] = (dst[s + 1] == scratch0) ? scratch1 : scratch0;
+    if ((dst[s] == scratch0 || dst[s] == scratch1) && bytes > scratch_bytes) {
+      set_err(E_TOO_LARGE, "intermediate field of %zu bytes exceeds the %zu-byte static scratch buffer", bytes,
+              scratch_bytes);
+      return E_TOO_LARGE;
+    }
+  }
+  if (n == 1 && in == out) {
+    set_err(E_BAD_ARG, "single-stage in-place transform needs an extra buffer; pass in != out");
+    return E_BAD_ARG;
+  }
+  // twiddle tables of every stage, packed into the given region
+  const void *tw[8] = {nullptr}, *aux[8] = {nullptr};
+  size_t off = 0;
+  unsigned char *host = static_cast<unsigned char *>(tw_host);
+  for (int s = 0; s < n; s++) {
+    const Stage &st = P->st[s];
+    if (g_types[st.type].kind == K_EMPTY) continue;
+    StageDesc d;
+    fill_stage_desc(P, st, false, d);
+    TableNeed need{0, 0, 0};
+    int rc = launch_stage(d, nullptr, nullptr, P->prec == 8 ? arith_mode() : AR_NATIVE, g_stream, nullptr, nullptr,
+                          nullptr, nullptr, &need);
+    if (rc != E_OK) {
+      set_err(rc, "stage %d cannot run (transform length unsupported)", s);
+      return rc;
+    }
+    size_t b1 = table_bytes(need.tabN, need.fmt), b2 = need.auxN ? table_bytes(need.auxN, need.fmt) : 0;
+    if (off + b1 + b2 > tw_bytes) {
+      set_err(E_TOO_LARGE, "twiddle tables exceed the %zu-byte static table region", tw_bytes);
+      return E_TOO_LARGE;
+    }
+    fill_table(need.tabN, need.fmt, host + off);
+    tw[s] = static_cast<unsigned char *>(tw_dev) + off;
+    off += (b1 + 255) & ~(size_t)255;
+    if (b2) {
+      fill_table(need.auxN, need.fmt, host + off);
+      aux[s] = static_cast<unsigned char *>(tw_dev) + off;
+      off += (b2 + 255) & ~(size_t)255;
+    }
+  }
+  if (off && cudaMemcpyAsync(tw_dev, tw_host, off, cudaMemcpyHostToDevice, g_stream) != cudaSuccess) {
+    set_err(E_CUDA, "twiddle upload failed");
+    return E_CUDA;
+  }
+  const void *src = in;
+  for (int s = 0; s < n; s++) {
+    const Stage &st = P->st[s];
+    bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
+    int rc = run_stage(P, st, src, dst[s], deriv, tw[s], aux[s]);
+    if (rc != E_OK) return rc;
+    src = dst[s];
+  }
+  if (g_sync) {
+    cudaError_t e = cudaStreamSynchronize(g_stream);
+    if (e != cudaSuccess) {
+      set_err(E_CUDA, "stream synchronize failed: %s", cudaGetErrorString(e));
+      return E_CUDA;
+    }
+  }
+  return E_OK;
+}
+
+void record_error(int code, const char *msg) { set_err(code, "%s", msg); }
 
 static void ensure_setup() {
   if (!g_setup_done) {

@@ -43,9 +43,21 @@ struct StageDesc {
 
 struct DeviceTables;  // twiddle-table cache, one per device
 
+// Twiddle tables a stage needs: W_tabN^k (and W_auxN^k for the generic DCT/DST kinds, auxN 0
+// if none), in format fmt (0 double pairs, 1 float pairs, 2 float-float pairs).
+struct TableNeed {
+  int fmt, tabN, auxN;
+};
+size_t table_bytes(int N, int fmt);
+void fill_table(int N, int fmt, void *host_dst);
+
 // Launch one stage on `stream`.  in != out is required (the host runtime guarantees it).
+// Tables come from `tabs` (allocated on first use) unless `tw_given` is non-null, in which case
+// tw_given / aux_given are used as they are.  With `tabs_out` non-null nothing is launched: the
+// call only reports the tables the stage needs.
 int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
-                 DeviceTables *tabs, int *kernels_launched);
+                 DeviceTables *tabs, int *kernels_launched, const void *tw_given = nullptr,
+                 const void *aux_given = nullptr, TableNeed *tabs_out = nullptr);
 // Pure permutation copy of an element size `esize` bytes field (EMPTY stages).
 int launch_permute(const int d[3], const long long s1[3], const long long s2[3], int esize,
                    const void *in, void *out, cudaStream_t stream, int *kernels_launched);

@@ -604,7 +604,31 @@ __global__ void k_deriv(const R *in, R *out, long long n, int sd0, int sd1, int 
 }
 
 // ------------------------------------------------------------------------------------------
-// Host side: twiddle tables (generated in long double, kept resident per device)
+// Host side: twiddle tables W_N^k = exp(-2 pi i k / N), generated in long double and stored as
+// double pairs (fmt 0), float pairs (fmt 1) or float-float pairs (fmt 2).
+size_t table_bytes(int N, int fmt) { return (size_t)N * (fmt == 1 ? 8 : 16); }
+
+void fill_table(int N, int fmt, void *dst) {
+  const long double TWO_PI = 6.283185307179586476925286766559005768L;
+  unsigned char *host = static_cast<unsigned char *>(dst);
+  for (int k = 0; k < N; k++) {
+    long double a = TWO_PI * (long double)k / (long double)N;
+    long double c = cosl(a), s = -sinl(a);
+    if (fmt == 0) {
+      double v[2] = {(double)c, (double)s};
+      memcpy(&host[(size_t)k * 16], v, 16);
+    } else if (fmt == 1) {
+      float v[2] = {(float)c, (float)s};
+      memcpy(&host[(size_t)k * 8], v, 8);
+    } else {
+      float ch = (float)c, sh = (float)s;
+      float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
+      memcpy(&host[(size_t)k * 16], v, 16);
+    }
+  }
+}
+
+// Kept resident per device; the map owns device allocations made on first use of each length.
 struct DeviceTables {
   std::mutex mu;
   // key: (N, format) format 0 = double, 1 = float, 2 = float-float
@@ -617,24 +641,9 @@ struct DeviceTables {
     auto key = std::make_pair(N, fmt);
     auto it = tabs.find(key);
     if (it != tabs.end()) return it->second;
-    const long double TWO_PI = 6.283185307179586476925286766559005768L;
-    size_t bytes = (size_t)N * (fmt == 1 ? 8 : 16);
+    size_t bytes = table_bytes(N, fmt);
     std::vector<unsigned char> host(bytes);
-    for (int k = 0; k < N; k++) {
-      long double a = TWO_PI * (long double)k / (long double)N;
-      long double c = cosl(a), s = -sinl(a);
-      if (fmt == 0) {
-        double v[2] = {(double)c, (double)s};
-        memcpy(&host[(size_t)k * 16], v, 16);
-      } else if (fmt == 1) {
-        float v[2] = {(float)c, (float)s};
-        memcpy(&host[(size_t)k * 8], v, 8);
-      } else {
-        float ch = (float)c, sh = (float)s;
-        float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
-        memcpy(&host[(size_t)k * 16], v, 16);
-      }
-    }
+    fill_table(N, fmt, host.data());
     void *d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) {
       *err = E_CUDA;
@@ -653,18 +662,24 @@ struct DeviceTables {
 DeviceTables *tables_create() { return new DeviceTables(); }
 void tables_destroy(DeviceTables *t) { delete t; }
 
-static void factorize(int n, std::vector<int> &rad) {
-  rad.clear();
-  while (n % 8 == 0 && n > 8) { rad.push_back(8); n /= 8; }
-  if (n % 8 == 0) { rad.push_back(8); n /= 8; }
-  while (n % 4 == 0) { rad.push_back(4); n /= 4; }
-  while (n % 2 == 0) { rad.push_back(2); n /= 2; }
+// Radix plan of a length (8s first, then 4, 2, 3, 5, 7, larger primes); returns the count or -1
+// when more than `cap` factors would be needed.
+static int factorize(int n, int *rad, int cap) {
+  int k = 0;
+  auto push = [&](int f) {
+    if (k < cap) rad[k] = f;
+    k++;
+  };
+  while (n % 8 == 0) { push(8); n /= 8; }
+  while (n % 4 == 0) { push(4); n /= 4; }
+  while (n % 2 == 0) { push(2); n /= 2; }
   const int small[3] = {3, 5, 7};
   for (int f : small)
-    while (n % f == 0) { rad.push_back(f); n /= f; }
+    while (n % f == 0) { push(f); n /= f; }
   for (int f = 11; (long long)f * f <= n; f += 2)
-    while (n % f == 0) { rad.push_back(f); n /= f; }
-  if (n > 1) rad.push_back(n);
+    while (n % f == 0) { push(f); n /= f; }
+  if (n > 1) push(n);
+  return k <= cap ? k : -1;
 }
 
 int max_line_len(int prec) { return prec == 8 ? 6144 : 12288; }
@@ -712,7 +727,8 @@ static int launch_any(const KParams &p, bool fixed, size_t smem, int grid, int t
 }
 
 int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
-                 DeviceTables *tabs, int *kernels_launched) {
+                 DeviceTables *tabs, int *kernels_launched, const void *tw_given, const void *aux_given,
+                 TableNeed *tabs_out) {
   const int L = d.L;
   const int a = (L + 1) % 3, b = (L + 2) % 3;
   if (d.d1[a] != d.d2[a] || d.d1[b] != d.d2[b]) return E_BAD_ARG;
@@ -797,19 +813,27 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
       return E_BAD_ARG;
   }
   if (p.nfft > max_line_len(d.prec)) return E_TOO_LARGE;
-  std::vector<int> rad;
-  factorize(p.nfft, rad);
-  if ((int)rad.size() > 24) return E_UNSUPPORTED;
-  p.nrad = (int)rad.size();
-  for (int i = 0; i < p.nrad; i++) p.rad[i] = rad[i];
+  p.nrad = factorize(p.nfft, p.rad, 24);
+  if (p.nrad < 0) return E_UNSUPPORTED;
 
   const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? 2 : 0);
+  if (tabs_out) {  // caller supplies the tables: report what is needed, launch nothing
+    tabs_out->fmt = fmt;
+    tabs_out->tabN = tabN;
+    tabs_out->auxN = (d.kind == K_R2R && p.r2r_np > 0) ? 8 * p.r2r_np : 0;
+    return E_OK;
+  }
   int err = E_OK;
-  p.tw = tabs->get(tabN, fmt, &err);
-  if (!p.tw) return err;
-  if (d.kind == K_R2R && p.r2r_np > 0) {
-    p.aux = tabs->get(8 * p.r2r_np, fmt, &err);
-    if (!p.aux) return err;
+  if (tw_given) {
+    p.tw = tw_given;
+    p.aux = aux_given;
+  } else {
+    p.tw = tabs->get(tabN, fmt, &err);
+    if (!p.tw) return err;
+    if (d.kind == K_R2R && p.r2r_np > 0) {
+      p.aux = tabs->get(8 * p.r2r_np, fmt, &err);
+      if (!p.aux) return err;
+    }
   }
   if (d.deriv && d.dt2 == 2) {
     p.deriv = 1;

@@ -77,6 +77,8 @@ def lib():
         "p3dfft_gb300_memcpy_d2h": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
         "p3dfft_gb300_synchronize": ([], ctypes.c_int), "p3dfft_gb300_version": ([], ctypes.c_char_p),
         "p3dfft_gb300_host_alloc_pinned": ([ctypes.c_longlong], vp), "p3dfft_gb300_host_free_pinned": ([vp], None),
+        "p3dfft_gb300_exec3d_noalloc": ([ctypes.c_int, vp, vp, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_noalloc_max_field_bytes": ([], ctypes.c_longlong),
         "p3dfft_gb300_event_record": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_event_elapsed_ms": ([ctypes.c_int, ctypes.c_int], ctypes.c_double),
         "p3dfft_gb300_profile_stages": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int,
