@@ -20,6 +20,7 @@ extern "C" {
 #define P3DFFT_ERR_NO_DEVICE 4
 #define P3DFFT_ERR_TOO_LARGE 5
 #define P3DFFT_ERR_PLAN 6
+#define P3DFFT_ERR_ALIGN 7
 /* last error code of this thread's calls into the library, cleared by p3dfft_clear_error */
 int p3dfft_last_error(void);
 const char *p3dfft_last_error_string(void);

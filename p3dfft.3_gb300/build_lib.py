@@ -25,9 +25,10 @@ MPI_SO = os.path.join(LIB, "libp3dfft_mpi1.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
+CFLAGS += os.environ.get("P3DFFT_GB300_NVCC_FLAGS", "").split()  # extra tuning defines
 
-SOURCES = ["stage_kernels.cu", "core.cpp", "noalloc.cu"]
-HEADERS = ["kernels.h", "df_arith.cuh"]
+SOURCES = ["stage_kernels.cu", "core.cpp", "noalloc.cu", "fast_df.cu", "fast_f64.cu", "fast_f32.cu"]
+HEADERS = ["kernels.h", "df_arith.cuh", "fx_arith.cuh", "stage_common.cuh", "fast_stage.cuh"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

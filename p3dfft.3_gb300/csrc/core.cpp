@@ -524,6 +524,8 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
     if (rc == E_CUDA) set_err(E_CUDA, "kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     else if (rc == E_TOO_LARGE) set_err(E_TOO_LARGE, "transform length or grid too large for this release");
     else if (rc == E_UNSUPPORTED) set_err(E_UNSUPPORTED, "unsupported transform size/type combination");
+    else if (rc == E_ALIGN)
+      set_err(E_ALIGN, "data pointers must be aligned to one complex element (16 bytes FP64, 8 bytes FP32)");
     else set_err(rc, "invalid stage description");
   }
   return rc;

@@ -35,6 +35,15 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
   e += a.lo + b.lo;
   return ff_fast2sum(s, e);
 }
+// Unnormalised sum: the hi parts are added exactly (TwoSum), the rounding error and both lo parts
+// collect in lo.  Used inside a butterfly; ff_norm restores |lo| <= ulp(hi)/2 afterwards.
+__device__ __forceinline__ ff ff_add_nn(ff a, ff b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  return ff{s, e + (a.lo + b.lo)};
+}
+__device__ __forceinline__ ff ff_norm(ff a) { return ff_fast2sum(a.hi, a.lo); }
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 __device__ __forceinline__ ff ff_half(ff a) { return ff{a.hi * 0.5f, a.lo * 0.5f}; }
@@ -81,6 +90,42 @@ __device__ __forceinline__ cff cff_mul(cff a, cff b) {
   return r;
 }
 
+// Unnormalised products for use inside a butterfly (the sums that follow do not need |lo| <=
+// ulp(hi)/2; values are normalised before they are stored).
+__device__ __forceinline__ cff cff_mul_nn(cff a, cff b) {
+  cff r;
+  {
+    float p1 = a.x.hi * b.x.hi, e1 = __fmaf_rn(a.x.hi, b.x.hi, -p1);
+    float p2 = -a.y.hi * b.y.hi, e2 = __fmaf_rn(-a.y.hi, b.y.hi, -p2);
+    float s = p1 + p2, bb = s - p1, e3 = (p1 - (s - bb)) + (p2 - bb);
+    float lo = (e1 + e2) + e3;
+    lo = __fmaf_rn(a.x.hi, b.x.lo, lo);
+    lo = __fmaf_rn(a.x.lo, b.x.hi, lo);
+    lo = __fmaf_rn(-a.y.hi, b.y.lo, lo);
+    lo = __fmaf_rn(-a.y.lo, b.y.hi, lo);
+    r.x = ff{s, lo};
+  }
+  {
+    float p1 = a.x.hi * b.y.hi, e1 = __fmaf_rn(a.x.hi, b.y.hi, -p1);
+    float p2 = a.y.hi * b.x.hi, e2 = __fmaf_rn(a.y.hi, b.x.hi, -p2);
+    float s = p1 + p2, bb = s - p1, e3 = (p1 - (s - bb)) + (p2 - bb);
+    float lo = (e1 + e2) + e3;
+    lo = __fmaf_rn(a.x.hi, b.y.lo, lo);
+    lo = __fmaf_rn(a.x.lo, b.y.hi, lo);
+    lo = __fmaf_rn(a.y.hi, b.x.lo, lo);
+    lo = __fmaf_rn(a.y.lo, b.x.hi, lo);
+    r.y = ff{s, lo};
+  }
+  return r;
+}
+__device__ __forceinline__ ff ff_mul_const_nn(ff a, float chi, float clo) {
+  float p = a.hi * chi;
+  float e = __fmaf_rn(a.hi, chi, -p);
+  e = __fmaf_rn(a.hi, clo, e);
+  e = __fmaf_rn(a.lo, chi, e);
+  return ff{p, e};
+}
+
 // IEEE double bits -> float-float (truncating split of the 53-bit significand into 24 + 24 bits)
 __device__ __forceinline__ ff ff_from_double_bits(long long bits) {
   const unsigned long long b = (unsigned long long)bits;
@@ -100,6 +145,44 @@ __device__ __forceinline__ ff ff_from_double_bits(long long bits) {
     if (el >= -126) lo = __int_as_float(sign | ((unsigned int)(el + 127) << 23) | ((nrm >> 5) & 0x7fffffu));
   }
   return ff{__int_as_float(hib), lo};
+}
+
+// Tile-scaled conversions of the specialised stage kernels.  A tile is multiplied by 2^sc
+// (an integer added to every exponent field) so that its largest value is near 2^20; values
+// more than 2^94 below the tile maximum are flushed to zero.  Only integer and FP32 pipe
+// instructions are used.
+__device__ __forceinline__ int dbl_biased_exp(long long bits) { return (int)(((unsigned long long)bits >> 52) & 0x7ff); }
+
+__device__ __forceinline__ ff ff_from_bits_scaled(long long bits, int sc) {
+  const unsigned H = (unsigned)((unsigned long long)bits >> 32), Lw = (unsigned)bits;
+  const unsigned sign = H & 0x80000000u;
+  const int E0 = (int)((H >> 20) & 0x7ff);
+  const int E = E0 + sc;  // scaled biased exponent
+  if (E0 == 0 || E < 949) return ff{0.f, 0.f};
+  const unsigned t = ((H & 0x000fffffu) | ((unsigned)E << 20)) - (896u << 20);
+  const float hi = __uint_as_float(__funnelshift_l(Lw, t, 3) | sign);
+  const float rf = __uint2float_rz(Lw & 0x1fffffffu);
+  const float lo = rf * __uint_as_float((unsigned)(E - 948) << 23);
+  return ff{hi, __uint_as_float(__float_as_uint(lo) ^ sign)};
+}
+
+// normalised float-float times 2^-sc -> IEEE double bits (round to nearest on the lo part)
+__device__ __forceinline__ long long ff_to_bits_scaled(ff v, int sc) {
+  const unsigned uh = __float_as_uint(v.hi);
+  const unsigned Ef = (uh >> 23) & 0xff;
+  const unsigned sign = uh & 0x80000000u;
+  if (Ef == 0) return 0;
+  const int E = (int)Ef + 896 - sc;
+  if (E <= 0) return (long long)((unsigned long long)sign << 32);
+  const unsigned H = sign | ((unsigned)E << 20) | ((uh & 0x7fffffu) >> 3);
+  const unsigned L = uh << 29;
+  const float kf = v.lo * __uint_as_float((306u - Ef) << 23);  // lo in units of ulp_double(hi)
+  int k = __float2int_rn(kf);
+  if (sign) k = -k;
+  if ((uh & 0x7fffffu) == 0 && k < 0) k *= 2;  // sum lies in the binade below hi
+  unsigned long long bits = ((unsigned long long)H << 32) | L;
+  bits += (unsigned long long)(long long)k;
+  return (long long)bits;
 }
 
 // float (normal or zero) bits -> double bits

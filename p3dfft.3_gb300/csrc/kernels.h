@@ -25,6 +25,7 @@ enum Err {
   E_NO_DEVICE = 4,
   E_TOO_LARGE = 5,
   E_PLAN = 6,
+  E_ALIGN = 7,
 };
 
 // One stage of a 3D (or 1D) plan, in logical-dimension terms: a 1D transform of `type kind`

@@ -1,0 +1,231 @@
+// Arithmetic policies shared by the stage kernels (generic engine in stage_kernels.cu, the
+// specialised fast kernels in fast_stage.cuh).
+//   Native<double>  FP64 data, DFMA arithmetic
+//   Native<float>   FP32 data, FFMA arithmetic, twiddles rounded from long-double tables
+//   DF              FP64 data, float-float arithmetic on the FP32 pipe (df_arith.cuh)
+#pragma once
+#include <cuda_runtime.h>
+
+#include "df_arith.cuh"
+#include "kernels.h"
+
+namespace p3d {
+
+// ------------------------------------------------------------------------------------------
+// Arithmetic policies
+template <class R>
+struct __align__(2 * sizeof(R)) cx {
+  R x, y;
+};
+
+__device__ __forceinline__ cx<double> ldg_c(const cx<double> *p) {
+  double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+  cx<double> r;
+  r.x = v.x;
+  r.y = v.y;
+  return r;
+}
+__device__ __forceinline__ cx<float> ldg_c(const cx<float> *p) {
+  float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  cx<float> r;
+  r.x = v.x;
+  r.y = v.y;
+  return r;
+}
+
+template <class R>
+struct Native {
+  using G = R;       // global real type
+  using S = R;       // shared-memory real type
+  using C = cx<R>;   // working complex
+  using T = cx<R>;   // twiddle-table entry
+  static __device__ __forceinline__ C mk(S a, S b) { C c; c.x = a; c.y = b; return c; }
+  static __device__ __forceinline__ C add(C a, C b) { return mk(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ C sub(C a, C b) { return mk(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ C mul(C a, C b) {
+    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  }
+  static __device__ __forceinline__ C muli(C a) { return mk(-a.y, a.x); }
+  static __device__ __forceinline__ C mulmi(C a) { return mk(a.y, -a.x); }
+  static __device__ __forceinline__ C conj(C a) { return mk(a.x, -a.y); }
+  static __device__ __forceinline__ C half(C a) { return mk(a.x * R(0.5), a.y * R(0.5)); }
+  static __device__ __forceinline__ C neg(C a) { return mk(-a.x, -a.y); }
+  static __device__ __forceinline__ C rsqrt2(C a) {
+    const R c = R(0.70710678118654752440084436210485);
+    return mk(a.x * c, a.y * c);
+  }
+  static __device__ __forceinline__ C iscale(C a, int k) {  // a * (i*k)
+    R kk = R(k);
+    return mk(-kk * a.y, kk * a.x);
+  }
+  static __device__ __forceinline__ S rzero() { return R(0); }
+  static __device__ __forceinline__ C zero() { return mk(R(0), R(0)); }
+  static __device__ __forceinline__ S negs(S a) { return -a; }
+  static __device__ __forceinline__ S halfs(S a) { return a * R(0.5); }
+  static __device__ __forceinline__ S ld(const G *p) { return __ldg(p); }
+  static __device__ __forceinline__ C ldc(const G *p) {
+    cx<R> v = ldg_c(reinterpret_cast<const cx<R> *>(p));
+    return mk(v.x, v.y);
+  }
+  static __device__ __forceinline__ void st(G *p, S v) { *p = v; }
+  static __device__ __forceinline__ void stc(G *p, C v) {
+    cx<R> w; w.x = v.x; w.y = v.y;
+    *reinterpret_cast<cx<R> *>(p) = w;
+  }
+  static __device__ __forceinline__ C tw(const T *t, int k) {
+    T v = ldg_c(t + k);
+    return mk(v.x, v.y);
+  }
+  static __device__ __forceinline__ C norm(C a) { return a; }
+  static __device__ __forceinline__ C tws(const T *t, int k) { return t[k]; }
+  // register-level I/O of the specialised kernels (no tile scaling for native arithmetic)
+  static constexpr bool SCALED = false;
+  using RAW = cx<R>;
+  static __device__ __forceinline__ RAW ldraw(const G *p) { return ldg_c(reinterpret_cast<const cx<R> *>(p)); }
+  static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
+    RAW r;
+    r.x = __ldg(p0);
+    r.y = __ldg(p1);
+    return r;
+  }
+  static __device__ __forceinline__ int rexp(RAW) { return 0; }
+  static __device__ __forceinline__ C from_raw(RAW r, int) { return mk(r.x, r.y); }
+  static __device__ __forceinline__ RAW to_raw(C v, int) {
+    RAW r;
+    r.x = v.x;
+    r.y = v.y;
+    return r;
+  }
+  static __device__ __forceinline__ void straw(G *p, RAW r) { *reinterpret_cast<cx<R> *>(p) = r; }
+  static __device__ __forceinline__ void straw2(G *p0, G *p1, RAW r) {
+    *p0 = r.x;
+    *p1 = r.y;
+  }
+};
+
+// float-float arithmetic for FP64 data (see df_arith.cuh)
+struct DF {
+  using G = double;
+  using S = ff;
+  using C = cff;
+  using T = cff;
+  static __device__ __forceinline__ C mk(S a, S b) { C c; c.x = a; c.y = b; return c; }
+  // sums are left unnormalised inside a butterfly; norm() is applied before values are stored
+  static __device__ __forceinline__ C add(C a, C b) { return mk(ff_add_nn(a.x, b.x), ff_add_nn(a.y, b.y)); }
+  static __device__ __forceinline__ C sub(C a, C b) {
+    return mk(ff_add_nn(a.x, ff_neg(b.x)), ff_add_nn(a.y, ff_neg(b.y)));
+  }
+  static __device__ __forceinline__ C norm(C a) { return mk(ff_norm(a.x), ff_norm(a.y)); }
+  static __device__ __forceinline__ C mul(C a, C b) { return cff_mul_nn(a, b); }
+  static __device__ __forceinline__ C muli(C a) { return mk(ff_neg(a.y), a.x); }
+  static __device__ __forceinline__ C mulmi(C a) { return mk(a.y, ff_neg(a.x)); }
+  static __device__ __forceinline__ C conj(C a) { return mk(a.x, ff_neg(a.y)); }
+  static __device__ __forceinline__ C half(C a) { return mk(ff_half(a.x), ff_half(a.y)); }
+  static __device__ __forceinline__ C neg(C a) { return mk(ff_neg(a.x), ff_neg(a.y)); }
+  static __device__ __forceinline__ C rsqrt2(C a) {
+    return mk(ff_mul_const_nn(a.x, FF_RSQRT2_HI, FF_RSQRT2_LO), ff_mul_const_nn(a.y, FF_RSQRT2_HI, FF_RSQRT2_LO));
+  }
+  static __device__ __forceinline__ C iscale(C a, int k) {
+    return mk(ff_neg(ff_mul_int(a.y, k)), ff_mul_int(a.x, k));
+  }
+  static __device__ __forceinline__ S rzero() { return ff{0.f, 0.f}; }
+  static __device__ __forceinline__ C zero() { return mk(rzero(), rzero()); }
+  static __device__ __forceinline__ S negs(S a) { return ff_neg(a); }
+  static __device__ __forceinline__ S halfs(S a) { return ff_half(a); }
+  static __device__ __forceinline__ S ld(const G *p) { return ff_from_double_bits(__ldg(reinterpret_cast<const long long *>(p))); }
+  static __device__ __forceinline__ C ldc(const G *p) {
+    longlong2 v = __ldg(reinterpret_cast<const longlong2 *>(p));
+    return mk(ff_from_double_bits(v.x), ff_from_double_bits(v.y));
+  }
+  static __device__ __forceinline__ void st(G *p, S v) {
+    *reinterpret_cast<long long *>(p) = ff_to_double_bits(ff_norm(v));
+  }
+  static __device__ __forceinline__ void stc(G *p, C v) {
+    longlong2 w;
+    w.x = ff_to_double_bits(ff_norm(v.x));
+    w.y = ff_to_double_bits(ff_norm(v.y));
+    *reinterpret_cast<longlong2 *>(p) = w;
+  }
+  // register-level I/O of the specialised kernels: raw IEEE bits, tile scaled by 2^sc
+  static constexpr bool SCALED = true;
+  using RAW = longlong2;
+  static __device__ __forceinline__ RAW ldraw(const G *p) { return __ldg(reinterpret_cast<const longlong2 *>(p)); }
+  static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
+    RAW r;
+    r.x = __ldg(reinterpret_cast<const long long *>(p0));
+    r.y = __ldg(reinterpret_cast<const long long *>(p1));
+    return r;
+  }
+  static __device__ __forceinline__ int rexp(RAW r) { return max(dbl_biased_exp(r.x), dbl_biased_exp(r.y)); }
+  static __device__ __forceinline__ C from_raw(RAW r, int sc) {
+    return mk(ff_from_bits_scaled(r.x, sc), ff_from_bits_scaled(r.y, sc));
+  }
+  static __device__ __forceinline__ RAW to_raw(C v, int sc) {
+    RAW r;
+    r.x = ff_to_bits_scaled(ff_norm(v.x), sc);
+    r.y = ff_to_bits_scaled(ff_norm(v.y), sc);
+    return r;
+  }
+  static __device__ __forceinline__ void straw(G *p, RAW r) { *reinterpret_cast<longlong2 *>(p) = r; }
+  static __device__ __forceinline__ void straw2(G *p0, G *p1, RAW r) {
+    *reinterpret_cast<long long *>(p0) = r.x;
+    *reinterpret_cast<long long *>(p1) = r.y;
+  }
+  static __device__ __forceinline__ C tws(const T *t, int k) { return t[k]; }
+  static __device__ __forceinline__ C tw(const T *t, int k) {
+    float4 v = __ldg(reinterpret_cast<const float4 *>(t + k));
+    C c;
+    c.x = ff{v.x, v.y};
+    c.y = ff{v.z, v.w};
+    return c;
+  }
+};
+
+
+// Shared-memory slot of line element i: one padding slot every 2^SH elements (SH = 0: none),
+// which keeps the Stockham scatter of the register engines free of bank conflicts.
+template <int SH>
+__device__ __forceinline__ int pad(int i) {
+  return SH ? i + (i >> SH) : i;
+}
+
+// In-register DFTs of radix 2, 4 and 8 (sign -1 forward, +1 backward); results normalised.
+template <class O, int R>
+__device__ __forceinline__ void dft_p2(typename O::C *v, int sign) {
+  using C = typename O::C;
+  if (R == 2) {
+    C a = v[0], b = v[1];
+    v[0] = O::add(a, b);
+    v[1] = O::sub(a, b);
+  } else if (R == 4) {
+    C t0 = O::add(v[0], v[2]), t1 = O::sub(v[0], v[2]);
+    C t2 = O::add(v[1], v[3]), t3 = O::sub(v[1], v[3]);
+    t3 = sign < 0 ? O::mulmi(t3) : O::muli(t3);
+    v[0] = O::add(t0, t2);
+    v[2] = O::sub(t0, t2);
+    v[1] = O::add(t1, t3);
+    v[3] = O::sub(t1, t3);
+  } else {  // R == 8
+    C e[4], o[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      e[k] = v[2 * k];
+      o[k] = v[2 * k + 1];
+    }
+    dft_p2<O, 4>(e, sign);
+    dft_p2<O, 4>(o, sign);
+    C o1 = O::rsqrt2(sign < 0 ? O::add(o[1], O::mulmi(o[1])) : O::add(o[1], O::muli(o[1])));
+    C o2 = sign < 0 ? O::mulmi(o[2]) : O::muli(o[2]);
+    C o3 = O::rsqrt2(sign < 0 ? O::sub(O::mulmi(o[3]), o[3]) : O::sub(O::muli(o[3]), o[3]));
+    v[0] = O::add(e[0], o[0]);
+    v[4] = O::sub(e[0], o[0]);
+    v[1] = O::add(e[1], o1);
+    v[5] = O::sub(e[1], o1);
+    v[2] = O::add(e[2], o2);
+    v[6] = O::sub(e[2], o2);
+    v[3] = O::add(e[3], o3);
+    v[7] = O::sub(e[3], o3);
+  }
+}
+
+}  // namespace p3d

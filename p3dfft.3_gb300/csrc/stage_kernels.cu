@@ -23,123 +23,11 @@
 #include <mutex>
 #include <vector>
 
-#include "df_arith.cuh"
+#include "fast_stage.cuh"
 #include "kernels.h"
+#include "stage_common.cuh"
 
 namespace p3d {
-
-// ------------------------------------------------------------------------------------------
-// Arithmetic policies
-template <class R>
-struct __align__(2 * sizeof(R)) cx {
-  R x, y;
-};
-
-__device__ __forceinline__ cx<double> ldg_c(const cx<double> *p) {
-  double2 v = __ldg(reinterpret_cast<const double2 *>(p));
-  cx<double> r;
-  r.x = v.x;
-  r.y = v.y;
-  return r;
-}
-__device__ __forceinline__ cx<float> ldg_c(const cx<float> *p) {
-  float2 v = __ldg(reinterpret_cast<const float2 *>(p));
-  cx<float> r;
-  r.x = v.x;
-  r.y = v.y;
-  return r;
-}
-
-template <class R>
-struct Native {
-  using G = R;       // global real type
-  using S = R;       // shared-memory real type
-  using C = cx<R>;   // working complex
-  using T = cx<R>;   // twiddle-table entry
-  static __device__ __forceinline__ C mk(S a, S b) { C c; c.x = a; c.y = b; return c; }
-  static __device__ __forceinline__ C add(C a, C b) { return mk(a.x + b.x, a.y + b.y); }
-  static __device__ __forceinline__ C sub(C a, C b) { return mk(a.x - b.x, a.y - b.y); }
-  static __device__ __forceinline__ C mul(C a, C b) {
-    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-  }
-  static __device__ __forceinline__ C muli(C a) { return mk(-a.y, a.x); }
-  static __device__ __forceinline__ C mulmi(C a) { return mk(a.y, -a.x); }
-  static __device__ __forceinline__ C conj(C a) { return mk(a.x, -a.y); }
-  static __device__ __forceinline__ C half(C a) { return mk(a.x * R(0.5), a.y * R(0.5)); }
-  static __device__ __forceinline__ C neg(C a) { return mk(-a.x, -a.y); }
-  static __device__ __forceinline__ C rsqrt2(C a) {
-    const R c = R(0.70710678118654752440084436210485);
-    return mk(a.x * c, a.y * c);
-  }
-  static __device__ __forceinline__ C iscale(C a, int k) {  // a * (i*k)
-    R kk = R(k);
-    return mk(-kk * a.y, kk * a.x);
-  }
-  static __device__ __forceinline__ S rzero() { return R(0); }
-  static __device__ __forceinline__ C zero() { return mk(R(0), R(0)); }
-  static __device__ __forceinline__ S negs(S a) { return -a; }
-  static __device__ __forceinline__ S halfs(S a) { return a * R(0.5); }
-  static __device__ __forceinline__ S ld(const G *p) { return __ldg(p); }
-  static __device__ __forceinline__ C ldc(const G *p) {
-    cx<R> v = ldg_c(reinterpret_cast<const cx<R> *>(p));
-    return mk(v.x, v.y);
-  }
-  static __device__ __forceinline__ void st(G *p, S v) { *p = v; }
-  static __device__ __forceinline__ void stc(G *p, C v) {
-    cx<R> w; w.x = v.x; w.y = v.y;
-    *reinterpret_cast<cx<R> *>(p) = w;
-  }
-  static __device__ __forceinline__ C tw(const T *t, int k) {
-    T v = ldg_c(t + k);
-    return mk(v.x, v.y);
-  }
-};
-
-// float-float arithmetic for FP64 data (see df_arith.cuh)
-struct DF {
-  using G = double;
-  using S = ff;
-  using C = cff;
-  using T = cff;
-  static __device__ __forceinline__ C mk(S a, S b) { C c; c.x = a; c.y = b; return c; }
-  static __device__ __forceinline__ C add(C a, C b) { return mk(ff_add(a.x, b.x), ff_add(a.y, b.y)); }
-  static __device__ __forceinline__ C sub(C a, C b) { return mk(ff_sub(a.x, b.x), ff_sub(a.y, b.y)); }
-  static __device__ __forceinline__ C mul(C a, C b) { return cff_mul(a, b); }
-  static __device__ __forceinline__ C muli(C a) { return mk(ff_neg(a.y), a.x); }
-  static __device__ __forceinline__ C mulmi(C a) { return mk(a.y, ff_neg(a.x)); }
-  static __device__ __forceinline__ C conj(C a) { return mk(a.x, ff_neg(a.y)); }
-  static __device__ __forceinline__ C half(C a) { return mk(ff_half(a.x), ff_half(a.y)); }
-  static __device__ __forceinline__ C neg(C a) { return mk(ff_neg(a.x), ff_neg(a.y)); }
-  static __device__ __forceinline__ C rsqrt2(C a) {
-    return mk(ff_mul_const(a.x, FF_RSQRT2_HI, FF_RSQRT2_LO), ff_mul_const(a.y, FF_RSQRT2_HI, FF_RSQRT2_LO));
-  }
-  static __device__ __forceinline__ C iscale(C a, int k) {
-    return mk(ff_neg(ff_mul_int(a.y, k)), ff_mul_int(a.x, k));
-  }
-  static __device__ __forceinline__ S rzero() { return ff{0.f, 0.f}; }
-  static __device__ __forceinline__ C zero() { return mk(rzero(), rzero()); }
-  static __device__ __forceinline__ S negs(S a) { return ff_neg(a); }
-  static __device__ __forceinline__ S halfs(S a) { return ff_half(a); }
-  static __device__ __forceinline__ S ld(const G *p) { return ff_from_double_bits(__ldg(reinterpret_cast<const long long *>(p))); }
-  static __device__ __forceinline__ C ldc(const G *p) {
-    longlong2 v = __ldg(reinterpret_cast<const longlong2 *>(p));
-    return mk(ff_from_double_bits(v.x), ff_from_double_bits(v.y));
-  }
-  static __device__ __forceinline__ void st(G *p, S v) { *reinterpret_cast<long long *>(p) = ff_to_double_bits(v); }
-  static __device__ __forceinline__ void stc(G *p, C v) {
-    longlong2 w;
-    w.x = ff_to_double_bits(v.x);
-    w.y = ff_to_double_bits(v.y);
-    *reinterpret_cast<longlong2 *>(p) = w;
-  }
-  static __device__ __forceinline__ C tw(const T *t, int k) {
-    float4 v = __ldg(reinterpret_cast<const float4 *>(t + k));
-    C c;
-    c.x = ff{v.x, v.y};
-    c.y = ff{v.z, v.w};
-    return c;
-  }
-};
 
 // ------------------------------------------------------------------------------------------
 struct KParams {
@@ -237,7 +125,7 @@ __device__ __forceinline__ void bfly(const typename O::C *src, typename O::C *ds
   dft_reg<O, R>(v, sign, p);
   int base = (j - k) * R + k;
 #pragma unroll
-  for (int r = 0; r < R; r++) dst[base + r * Ns] = v[r];
+  for (int r = 0; r < R; r++) dst[base + r * Ns] = O::norm(v[r]);
 }
 
 template <class O>
@@ -256,7 +144,7 @@ __device__ void bfly_generic(const typename O::C *src, typename O::C *dst, int j
       m %= p.nfft;
       acc = O::add(acc, O::mul(x, twid<O>(p, m, sign)));
     }
-    dst[base + q * Ns] = acc;
+    dst[base + q * Ns] = O::norm(acc);
   }
 }
 
@@ -318,12 +206,6 @@ __device__ __forceinline__ typename O::C apply_deriv(const KParams &p, typename 
   return O::iscale(v, kk);
 }
 
-// Shared-memory slot of line element i: one padding slot every 2^SH elements (SH = 0: none),
-// which keeps the Stockham scatter of the register engines free of bank conflicts.
-template <int SH>
-__device__ __forceinline__ int pad(int i) {
-  return SH ? i + (i >> SH) : i;
-}
 
 // ------------------------------------------------------------------------------------------
 // FFT engines.  An engine runs the complex FFT of length nfft on every line of the tile held in
@@ -369,7 +251,7 @@ __device__ __forceinline__ void fixed_pass(const KParams &p, typename O::C *line
       const int k = jj & (Ns - 1);
       const int base = (jj - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; r++) line[pad<3>(base + r * Ns)] = v[b * R + r];
+      for (int r = 0; r < R; r++) line[pad<3>(base + r * Ns)] = O::norm(v[b * R + r]);
     }
   }
   __syncthreads();
@@ -859,6 +741,49 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   p.oo = d.s2[o];
   p.dt = d.d1[t];
   p.dother = d.d1[o];
+
+  // vector loads/stores of complex elements need element-aligned base pointers
+  const uintptr_t align_need = (d.prec == 8) ? 16 : 8;
+  const bool aligned = (((uintptr_t)in | (uintptr_t)out) % align_need) == 0;
+  if (!aligned && (p.in_complex || p.out_complex)) return E_ALIGN;
+
+  // specialised kernels for C2C / even R2C / even C2R at power-of-two lengths
+  const bool even = (p.nlog % 2) == 0;
+  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even);
+  if (fast_kind && fast_supported(p.nfft) && aligned && !getenv("P3DFFT_GB300_GENERIC_ONLY")) {
+    FastArgs fa;
+    fa.kind = (d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C);
+    fa.n = p.nfft;
+    FParams &q = fa.p;
+    q.in = in;
+    q.out = out;
+    q.tw = p.tw;
+    q.iL = p.iL;
+    q.it = p.it;
+    q.io = p.io;
+    q.oL = p.oL;
+    q.ot = p.ot;
+    q.oo = p.oo;
+    q.dt = p.dt;
+    const int TB = fast_tile_lines(p.nfft);
+    q.ntile = (p.dt + TB - 1) / TB;
+    long long ntot = (long long)q.ntile * p.dother;
+    if (ntot > 0x7fffffffLL) return E_TOO_LARGE;
+    q.ntotal = (int)ntot;
+    q.sign = p.sign;
+    q.deriv = p.deriv;
+    q.dg = p.dg;
+    q.dmid = p.dmid;
+    q.load_Lmajor = p.load_Lmajor;
+    q.store_Lmajor = p.store_Lmajor;
+    if (q.ntotal == 0) return E_OK;
+    int rc;
+    if (d.prec == 4) rc = launch_fast_f32(fa, stream);
+    else if (arith == AR_DF) rc = launch_fast_df(fa, stream);
+    else rc = launch_fast_f64(fa, stream);
+    if (rc == E_OK && kernels_launched) (*kernels_launched)++;
+    return rc;
+  }
 
   const size_t csz = (d.prec == 4) ? 8 : 16;
   const bool fixed = fixed_engine_len(p.nfft) && !getenv("P3DFFT_GB300_GENERIC_ONLY");

@@ -33,7 +33,8 @@ for _f, _fam in enumerate(_FAMILIES):
         TYPE_IDS[f"{_fam}_{_suf}"] = 12 + 4 * _f + _v
 globals().update(TYPE_IDS)
 
-ERR_NAMES = {0: "OK", 1: "BAD_ARG", 2: "UNSUPPORTED", 3: "CUDA", 4: "NO_DEVICE", 5: "TOO_LARGE", 6: "PLAN"}
+ERR_NAMES = {0: "OK", 1: "BAD_ARG", 2: "UNSUPPORTED", 3: "CUDA", 4: "NO_DEVICE", 5: "TOO_LARGE", 6: "PLAN",
+             7: "ALIGN"}
 
 
 class P3DFFTError(RuntimeError):
