@@ -184,13 +184,29 @@ def cpu_baseline_sample():
 
 
 def load_traffic(kernel_key):
-    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes per launch of a kernel at this workload, from a `TRAFFIC <kernel> <bytes>` line
+    of a committed ncu summary under profiles/ (None when no summary covers it)."""
+    pdir = os.path.join(ROOT, "profiles")
     try:
-        with open(path) as f:
-            return json.load(f).get(kernel_key)
-    except Exception:
-        return None
+        for fn in sorted(os.listdir(pdir)):
+            if not fn.endswith((".md", ".txt")):
+                continue
+            with open(os.path.join(pdir, fn)) as f:
+                for line in f:
+                    p = line.split()
+                    if len(p) == 3 and p[0] == "TRAFFIC" and p[1] == kernel_key:
+                        return int(p[2])
+    except OSError:
+        pass
+    return None
+
+
+def kernel_id(stage, arith, n_dims):
+    """Name of the kernel instantiation that runs a stage (matches the ncu kernel names)."""
+    kind = {5: 1, 7: 2}.get(stage["type"], 0)  # R2C_D, C2R_D, else C2C
+    n = stage["gdims1"][stage["dim"]] if kind != 2 else stage["gdims2"][stage["dim"]]
+    nfft = n // 2 if kind else n
+    return f"k_fast<{'DF' if arith else 'Native<double>'},{kind},{nfft}>"
 
 
 def main():
@@ -289,16 +305,23 @@ def main():
             dt2 = 1 if st["type"] in (7,) else 2
             bytes_ = 8 * (dt1 * int(np.prod(st["gdims1"])) + dt2 * int(np.prod(st["gdims2"])))
             stages.append({"dim": st["dim"], "type": st["type"], "ms": msv[i], "bytes": bytes_,
-                           "gbs": bytes_ / (msv[i] * 1e-3) / 1e9 if msv[i] > 0 else None})
-    dom = max(range(len(stages)), key=lambda i: stages[i]["ms"])
+                           "kernel": kernel_id(st, arith, GD)})
+    # dominant kernel = the instantiation with the largest total time per step
+    per_kernel = {}
+    for s in stages:
+        agg = per_kernel.setdefault(s["kernel"], {"ms": 0.0, "bytes": 0, "launches": 0})
+        agg["ms"] += s["ms"]
+        agg["bytes"] += s["bytes"]
+        agg["launches"] += 1
+    kernel_key = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
+    dk = per_kernel[kernel_key]
     peak, peak_kind = measured_peak()
-    ds = stages[dom]
-    kernel_key = f"k_stage<{'DF' if arith else 'Native<double>'}> stage{dom} dim{ds['dim']} type{ds['type']}"
-    traffic = load_traffic(kernel_key)
-    roofline = {"bound": "hbm", "achieved": ds["gbs"], "peak": peak, "unit": "GB/s",
-                "frac": ds["gbs"] / peak if ds["gbs"] else None, "traffic": traffic,
-                "kernel": kernel_key, "peak_source": peak_kind,
-                "bytes_per_launch": ds["bytes"], "ms_per_launch": ds["ms"],
+    achieved = dk["bytes"] / (dk["ms"] * 1e-3) / 1e9
+    traffic = load_traffic(kernel_key) if GD == (512, 512, 512) else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": kernel_key, "peak_source": peak_kind,
+                "launches_per_step": dk["launches"], "bytes_per_launch": dk["bytes"] // dk["launches"],
+                "ms_per_launch": dk["ms"] / dk["launches"], "step_share": dk["ms"] / sum(s["ms"] for s in stages),
                 "whole_step_frac": value / world / peak,
                 "stages_ms": [round(s["ms"], 4) for s in stages]}
 
@@ -319,6 +342,39 @@ def main():
     e2e = {"value": ALG_BYTES * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": S_R,
            "d2h_bytes_per_step": S_R, "ms_per_step": e2e_ms}
     rt_err = float(np.linalg.norm(hout.array - y) / max(np.linalg.norm(y), 1e-300))
+    del hin, hout
+
+    # ---- the other FP64 arithmetic and the FP32 form, same workload, device-resident ----
+    def timed(fh, bh, din, dspec, dout, steps):
+        for _ in range(3):
+            p3d.check(L.p3dfft_gb300_exec3d(fh, ctypes.c_void_p(din), ctypes.c_void_p(dspec), IDIR, 0))
+            p3d.check(L.p3dfft_gb300_exec3d(bh, ctypes.c_void_p(dspec), ctypes.c_void_p(dout), -1, 0))
+        L.p3dfft_gb300_synchronize()
+        L.p3dfft_gb300_event_record(2)
+        for _ in range(steps):
+            p3d.check(L.p3dfft_gb300_exec3d(fh, ctypes.c_void_p(din), ctypes.c_void_p(dspec), IDIR, 0))
+            p3d.check(L.p3dfft_gb300_exec3d(bh, ctypes.c_void_p(dspec), ctypes.c_void_p(dout), -1, 0))
+        L.p3dfft_gb300_event_record(3)
+        return L.p3dfft_gb300_event_elapsed_ms(2, 3) / steps
+
+    forms = {}
+    p3d.set_fp64_arith(1 - arith)
+    ms_other = timed(f.handle, b.handle, d_in.ptr, d_spec.ptr, d_out.ptr, max(3, args.steps // 10))
+    y_other = d_out.download(np.empty_like(y))
+    p3d.set_fp64_arith(arith)
+    forms["fp64_native" if arith else "fp64_float_float"] = {
+        "ms_per_step": ms_other, "value": ALG_BYTES / (ms_other * 1e-3) / 1e9, "unit": "GB/s",
+        "rel_l2_vs_headline": float(np.linalg.norm(y_other - y) / np.linalg.norm(y))}
+    f32 = p3d.Transform3D((4, 8, 8), GD, MO1, GD2, MO2, -1, 0)
+    b32 = p3d.Transform3D((6, 10, 10), GD2, MO2, GD, MO1, 0, -1)
+    d_in32, d_spec32, d_out32 = p3d.DeviceArray(S_R // 2), p3d.DeviceArray(S_C // 2), p3d.DeviceArray(S_R // 2)
+    d_in32.upload(x.astype(np.float32))
+    ms32 = timed(f32.handle, b32.handle, d_in32.ptr, d_spec32.ptr, d_out32.ptr, args.steps)
+    y32 = d_out32.download(np.empty(y.shape, np.float32)).astype(np.float64)
+    forms["fp32"] = {"ms_per_step": ms32, "value": (ALG_BYTES // 2) / (ms32 * 1e-3) / 1e9, "unit": "GB/s",
+                     "round_trips_per_s": 1e3 / ms32, "speedup_vs_fp64_transforms_per_s": ms_step / ms32,
+                     "rel_l2_vs_fp64": float(np.linalg.norm(y32 - y) / np.linalg.norm(y))}
+    del d_in32, d_spec32, d_out32
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -330,7 +386,7 @@ def main():
                        "input": "numpy PCG64 U[-1,1) seed 512+rank", "parallelism": f"replicas x{world}",
                        "algorithmic_bytes_per_step": ALG_BYTES},
             "roofline": roofline, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
-            "host_vs_device_rel_diff": rt_err}
+            "host_vs_device_rel_diff": rt_err, "other_forms": forms}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0:
