@@ -32,8 +32,9 @@ void p3dfft_gb300_set_stream(void *cuda_stream);
 /* 1 (default): exec returns after the result is in `out`; 0: device-pointer execs return
  * once the work is queued on the stream (host-pointer execs always synchronise). */
 void p3dfft_gb300_set_sync(int sync);
-/* Arithmetic of FP64 stages: 0 = native FP64 (DFMA), 1 = float-float on the FP32 pipe
- * (~48-bit significand, magnitudes 2^-100..2^126).  Default from P3DFFT_GB300_FP64_ARITH. */
+/* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,
+ * ~1e-14 relative L2 per 3D transform), 0 = native FP64 DFMA (slow on GB300).  The initial value
+ * can be set with P3DFFT_GB300_FP64_ARITH=native. */
 void p3dfft_gb300_set_fp64_arith(int mode);
 int p3dfft_gb300_get_fp64_arith(void);
 

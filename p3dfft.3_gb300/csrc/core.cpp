@@ -210,8 +210,9 @@ static bool ensure_device() {
 
 static int arith_mode() {
   if (g_arith < 0) {
+    // float-float unless P3DFFT_GB300_FP64_ARITH selects native DFMA ("0" / "native")
     const char *s = getenv("P3DFFT_GB300_FP64_ARITH");
-    g_arith = (s && (s[0] == '1' || s[0] == 'd' || s[0] == 'D')) ? AR_DF : AR_NATIVE;
+    g_arith = (s && (s[0] == '0' || s[0] == 'n' || s[0] == 'N')) ? AR_NATIVE : AR_DF;
   }
   return g_arith;
 }
