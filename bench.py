@@ -209,6 +209,123 @@ def kernel_id(stage, arith, n_dims):
     return f"k_fast<{'DF' if arith else 'Native<double>'},{kind},{nfft}>"
 
 
+# ------------------------------------------------------------------------------------------
+# Batched uneven transforms: 48 independent R2C -> C2R round trips, sizes drawn from a seed among
+# five grids, half FP32 and half FP64, run as one CUDA graph; against 48 sequential plain FP64 calls.
+BATCH_SHAPES = [(64, 64, 64), (96, 128, 80), (128, 128, 128), (200, 200, 200), (256, 256, 256)]
+
+
+def batch_jobs(n_jobs=48, seed=4):
+    """(grid, precision) of each job: sizes uniform over BATCH_SHAPES, precisions a seeded
+    permutation of n/2 FP32 and n/2 FP64."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(0, len(BATCH_SHAPES), n_jobs)
+    precs = rng.permutation([4] * (n_jobs // 2) + [8] * (n_jobs - n_jobs // 2))
+    return [(BATCH_SHAPES[s], int(p)) for s, p in zip(sizes, precs)]
+
+
+def round_trip_bytes(gd, prec):
+    """3-pass algorithmic bytes of one R2C -> C2R round trip: 2*S_r + 10*S_c."""
+    s_r = prec * gd[0] * gd[1] * gd[2]
+    s_c = 2 * prec * (gd[0] // 2 + 1) * gd[1] * gd[2]
+    return 2 * s_r + 10 * s_c
+
+
+def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
+    """Times the batch (graph replay) and 48 sequential plain FP64 round trips; returns a dict."""
+    import ctypes
+    jobs = batch_jobs(seed=seed)
+    plans = {}
+
+    def plan_pair(gd, prec):
+        key = (gd, prec)
+        if key not in plans:
+            gd2 = (gd[0] // 2 + 1, gd[1], gd[2])
+            ft, bt = ((5, 9, 9), (7, 11, 11)) if prec == 8 else ((4, 8, 8), (6, 10, 10))
+            plans[key] = (p3d.Transform3D(ft, gd, MO1, gd2, MO2, -1, 0), p3d.Transform3D(bt, gd2, MO2, gd, MO1, 0, -1))
+        return plans[key]
+
+    def buffers(gd, prec, seed_):
+        n = gd[0] * gd[1] * gd[2]
+        nc = (gd[0] // 2 + 1) * gd[1] * gd[2]
+        d_x, d_s, d_y = p3d.DeviceArray(prec * n), p3d.DeviceArray(2 * prec * nc), p3d.DeviceArray(prec * n)
+        x = np.random.default_rng(seed_).uniform(-1.0, 1.0, n)
+        d_x.upload(x.astype(np.float64 if prec == 8 else np.float32))
+        return d_x, d_s, d_y
+
+    mixed = [(gd, prec, buffers(gd, prec, 4000 + i)) for i, (gd, prec) in enumerate(jobs)]
+    plain = [(gd, 8, buffers(gd, 8, 4000 + i)) for i, (gd, _) in enumerate(jobs)]
+
+    def make_batch(items, graph=True):
+        bt = p3d.Batch(nbranches=nbranches, graph=graph)
+        for j, (gd, prec, (d_x, d_s, d_y)) in enumerate(items):
+            f, b = plan_pair(gd, prec)
+            bt.add(j, f, d_x, d_s)
+            bt.add(j, b, d_s, d_y)
+        return bt
+
+    def time_batch(bt):
+        for _ in range(warmup):
+            bt.exec()
+        L.p3dfft_gb300_synchronize()
+        k0 = p3d.kernel_count()
+        L.p3dfft_gb300_event_record(4)
+        for _ in range(steps):
+            bt.exec()
+        L.p3dfft_gb300_event_record(5)
+        return L.p3dfft_gb300_event_elapsed_ms(4, 5) / steps, (p3d.kernel_count() - k0) // steps
+
+    p3d.set_sync(False)
+    b_mixed = make_batch(mixed)
+    ms_mixed, k_mixed = time_batch(b_mixed)
+    b_f64 = make_batch(plain)
+    ms_b64, _ = time_batch(b_f64)
+    b_nog = make_batch(mixed, graph=False)
+    ms_nog, _ = time_batch(b_nog)
+
+    # 48 sequential plain FP64 calls: the reference-style synchronous exec, one job after another
+    p3d.set_sync(True)
+
+    def sequential():
+        for gd, prec, (d_x, d_s, d_y) in plain:
+            f, b = plan_pair(gd, prec)
+            p3d.check(L.p3dfft_gb300_exec3d(f.handle, ctypes.c_void_p(d_x.ptr), ctypes.c_void_p(d_s.ptr), -1, 0))
+            p3d.check(L.p3dfft_gb300_exec3d(b.handle, ctypes.c_void_p(d_s.ptr), ctypes.c_void_p(d_y.ptr), -1, 0))
+
+    for _ in range(max(1, warmup // 2)):
+        sequential()
+    n_seq = max(2, steps // 2)
+    L.p3dfft_gb300_event_record(6)
+    for _ in range(n_seq):
+        sequential()
+    L.p3dfft_gb300_event_record(7)
+    ms_seq = L.p3dfft_gb300_event_elapsed_ms(6, 7) / n_seq
+    p3d.set_sync(False)
+
+    alg_mixed = sum(round_trip_bytes(gd, prec) for gd, prec in jobs)
+    alg_plain = sum(round_trip_bytes(gd, 8) for gd, _ in jobs)
+    n = len(jobs)
+    hist = {}
+    for gd, prec in jobs:
+        k = f"{gd[0]}x{gd[1]}x{gd[2]}/{'fp64' if prec == 8 else 'fp32'}"
+        hist[k] = hist.get(k, 0) + 1
+    out = {
+        "jobs": n, "seed": seed, "branches": nbranches, "mix": hist,
+        "batch_graph_mixed": {"ms": ms_mixed, "round_trips_per_s": n / (ms_mixed * 1e-3),
+                              "GB_per_s": alg_mixed / (ms_mixed * 1e-3) / 1e9, "kernels_per_exec": k_mixed,
+                              "graph_launches_per_exec": 1},
+        "batch_graph_all_fp64": {"ms": ms_b64, "round_trips_per_s": n / (ms_b64 * 1e-3),
+                                 "GB_per_s": alg_plain / (ms_b64 * 1e-3) / 1e9},
+        "batch_streams_no_graph_mixed": {"ms": ms_nog, "round_trips_per_s": n / (ms_nog * 1e-3)},
+        "sequential_plain_fp64": {"ms": ms_seq, "round_trips_per_s": n / (ms_seq * 1e-3),
+                                  "GB_per_s": alg_plain / (ms_seq * 1e-3) / 1e9},
+        "speedup_mixed_batch_vs_sequential_fp64": ms_seq / ms_mixed,
+    }
+    for bt in (b_mixed, b_f64, b_nog):
+        del bt
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,11 +335,22 @@ def main():
     ap.add_argument("--arith", default="auto", choices=["auto", "df", "native"],
                     help="FP64 arithmetic: float-float (df) or native DFMA; auto = df")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="roundtrip", choices=["roundtrip", "batch"],
+                    help="roundtrip: the 512^3 headline; batch: 48 uneven round trips only")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload summary")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "batch":
+        import p3dfft_gb300 as p3d
+        import build_lib
+        build_lib.build()
+        res = batch_workload(p3d, p3d.lib(), args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps({"workload": "batched uneven round trips", **res}), flush=True)
         return
 
     import ctypes
@@ -374,7 +502,10 @@ def main():
     forms["fp32"] = {"ms_per_step": ms32, "value": (ALG_BYTES // 2) / (ms32 * 1e-3) / 1e9, "unit": "GB/s",
                      "round_trips_per_s": 1e3 / ms32, "speedup_vs_fp64_transforms_per_s": ms_step / ms32,
                      "rel_l2_vs_fp64": float(np.linalg.norm(y32 - y) / np.linalg.norm(y))}
-    del d_in32, d_spec32, d_out32
+    del d_in32, d_spec32, d_out32, f32, b32
+    if not args.no_batch:
+        del d_in, d_spec, d_out  # free HBM for the batch buffers
+        forms["batched_uneven"] = batch_workload(p3d, L, max(3, min(args.steps, 10)), 3)
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

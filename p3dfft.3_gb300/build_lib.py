@@ -27,8 +27,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
 CFLAGS += os.environ.get("P3DFFT_GB300_NVCC_FLAGS", "").split()  # extra tuning defines
 
-SOURCES = ["stage_kernels.cu", "core.cpp", "noalloc.cu", "fast_df.cu", "fast_f64.cu", "fast_f32.cu"]
-HEADERS = ["kernels.h", "df_arith.cuh", "fx_arith.cuh", "stage_common.cuh", "fast_stage.cuh"]
+SOURCES = ["stage_kernels.cu", "core.cpp", "batch.cpp", "noalloc.cu"]
+# fast_inst.cu once per (arithmetic, kind): 0 float-float / 1 FP64 / 2 FP32 x C2C / R2C / C2R
+FAST_UNITS = [(a, k) for a in range(3) for k in range(3)]
+HEADERS = ["kernels.h", "runtime.h", "df_arith.cuh", "fx_arith.cuh", "stage_common.cuh", "fast_stage.cuh"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:
@@ -51,12 +53,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
         os.path.join(INC, h) for h in ("p3dfft.h", "Cwrap.h", "Fwrap.h", "p3dfft_gb300.h", "mpi.h")]
     jobs = []
     objs = []
-    for src in SOURCES:
+    units = [(src, src + ".o", []) for src in SOURCES]
+    units += [("fast_inst.cu", f"fast_inst_a{a}_k{k}.o", [f"-DP3D_FAST_ARITH={a}", f"-DP3D_FAST_KIND={k}"])
+              for a, k in FAST_UNITS]
+    for src, obj, defs in units:
         sp = os.path.join(CSRC, src)
-        op = os.path.join(OBJ, src + ".o")
+        op = os.path.join(OBJ, obj)
         objs.append(op)
         if force or not _newer(op, [sp] + hdrs + [__file__]):
-            jobs.append([NVCC] + ARCH + CFLAGS + ["-c", sp, "-o", op])
+            jobs.append([NVCC] + ARCH + CFLAGS + defs + ["-c", sp, "-o", op])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for _ in ex.map(_run, jobs):
             pass

@@ -1,0 +1,276 @@
+// Batched execution of many independent 3D transforms (no counterpart in the reference, whose
+// transform3D::exec runs one transform per call, build/exec.C:101-223).
+//
+// A batch is a set of jobs; a job is an ordered list of (plan, in, out, idir) steps on device
+// memory, e.g. an R2C forward followed by the C2R backward.  Jobs are spread over branch streams
+// by a longest-processing-time-first assignment on their HBM bytes; each branch owns one scratch
+// set, sized for the largest plan it runs, so jobs of a branch reuse it one after another.
+// The first exec runs the jobs eagerly (this resolves twiddle tables and scratch), then records
+// the whole fork / branches / join structure into one CUDA graph; every later exec is a single
+// cudaGraphLaunch on the library stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "kernels.h"
+#include "p3dfft_gb300.h"
+#include "runtime.h"
+
+namespace p3d {
+
+struct BatchStep {
+  int plan;
+  const void *in;
+  void *out;
+  int idir;
+};
+
+struct Batch {
+  int nbr = 8;
+  std::map<int, std::vector<BatchStep>> jobs;
+  std::vector<std::vector<int>> assign;  // branch -> job ids
+  std::vector<cudaStream_t> br;
+  std::vector<void *> sets;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr;
+  cudaStream_t origin = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool use_graph = true;
+  bool dirty = true;
+  int arith = -1;
+  long long kernels = 0;  // kernels one exec launches
+  double bytes = 0;       // field bytes one exec reads and writes (inputs + outputs of every step)
+
+  ~Batch() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto s : br) cudaStreamDestroy(s);
+    for (auto e : join) cudaEventDestroy(e);
+    for (auto p : sets) scratch_set_destroy(p);
+    if (fork) cudaEventDestroy(fork);
+    if (origin) cudaStreamDestroy(origin);
+  }
+};
+
+static std::mutex g_bmu;
+static std::vector<Batch *> g_batches;
+
+static Batch *get_batch(int h) {
+  std::lock_guard<std::mutex> g(g_bmu);
+  if (h < 0 || h >= (int)g_batches.size()) return nullptr;
+  return g_batches[h];
+}
+
+static int fail(int code, const char *msg) {
+  record_error(code, msg);
+  return code;
+}
+
+// Longest-processing-time-first assignment of jobs to branches, then one scratch set per branch.
+static int prepare(Batch *B) {
+  if (B->br.empty()) {
+    B->br.resize(B->nbr);
+    B->join.resize(B->nbr);
+    B->sets.resize(B->nbr, nullptr);
+    for (int i = 0; i < B->nbr; i++) {
+      if (cudaStreamCreateWithFlags(&B->br[i], cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&B->join[i], cudaEventDisableTiming) != cudaSuccess)
+        return fail(E_CUDA, "batch: stream or event creation failed");
+      B->sets[i] = scratch_set_create();
+    }
+    if (cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&B->origin, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(E_CUDA, "batch: stream or event creation failed");
+  }
+  std::vector<std::pair<double, int>> work;
+  std::map<int, size_t> scratch_of_job;
+  B->bytes = 0;
+  for (auto &kv : B->jobs) {
+    double w = 0;
+    size_t sc = 0;
+    for (auto &s : kv.second) {
+      size_t ib = 0, ob = 0, sb = 0;
+      int prec = 0;
+      if (plan3d_sizes(s.plan, &ib, &ob, &sb, &prec) != E_OK) return E_BAD_ARG;
+      w += (double)ib + (double)ob + 2.0 * sb;
+      sc = std::max(sc, sb);
+      B->bytes += (double)ib + (double)ob;
+    }
+    work.push_back({w, kv.first});
+    scratch_of_job[kv.first] = sc;
+  }
+  std::sort(work.begin(), work.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+    return a.first > b.first || (a.first == b.first && a.second < b.second);
+  });
+  B->assign.assign(B->nbr, {});
+  std::vector<double> load(B->nbr, 0.0);
+  for (auto &w : work) {
+    int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[k] += w.first;
+    B->assign[k].push_back(w.second);
+  }
+  for (int b = 0; b < B->nbr; b++) {
+    size_t need = 0;
+    for (int j : B->assign[b]) need = std::max(need, scratch_of_job[j]);
+    if (need && scratch_set_reserve(B->sets[b], need) != E_OK) return E_CUDA;
+  }
+  return E_OK;
+}
+
+// fork from `st`, run every branch's jobs, join back into `st`
+static int run_branches(Batch *B, cudaStream_t st, bool capturing) {
+  if (cudaEventRecord(B->fork, st) != cudaSuccess) return fail(E_CUDA, "batch: fork event failed");
+  int rc = E_OK;
+  for (int b = 0; b < B->nbr; b++) {
+    if (cudaStreamWaitEvent(B->br[b], B->fork, 0) != cudaSuccess) return fail(E_CUDA, "batch: fork wait failed");
+    for (int j : B->assign[b]) {
+      for (auto &s : B->jobs[j]) {
+        rc = exec_plan_on(s.plan, s.in, s.out, s.idir, B->br[b], B->sets[b], capturing);
+        if (rc != E_OK) break;
+      }
+      if (rc != E_OK) break;
+    }
+    // always join, so a failed capture still ends on the origin stream
+    if (cudaEventRecord(B->join[b], B->br[b]) != cudaSuccess || cudaStreamWaitEvent(st, B->join[b], 0) != cudaSuccess)
+      return fail(E_CUDA, "batch: join failed");
+    if (rc != E_OK) return rc;
+  }
+  return E_OK;
+}
+
+static int build_graph(Batch *B) {
+  if (B->gexec) {
+    cudaGraphExecDestroy(B->gexec);
+    B->gexec = nullptr;
+  }
+  const long long k0 = kernel_count_now();
+  if (cudaStreamBeginCapture(B->origin, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return fail(E_CUDA, "batch: stream capture could not begin");
+  int rc = run_branches(B, B->origin, true);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(B->origin, &graph);
+  add_kernel_count(-(kernel_count_now() - k0));  // recorded, not launched
+  if (rc != E_OK || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc != E_OK ? rc : fail(E_CUDA, "batch: stream capture failed");
+  }
+  e = cudaGraphInstantiate(&B->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    B->gexec = nullptr;
+    cudaGetLastError();
+    return fail(E_CUDA, "batch: graph instantiation failed");
+  }
+  return E_OK;
+}
+
+static int finish(cudaStream_t st) {
+  if (!library_sync()) return E_OK;
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(E_CUDA, cudaGetErrorString(e));
+  return E_OK;
+}
+
+}  // namespace p3d
+
+using namespace p3d;
+
+extern "C" {
+
+int p3dfft_gb300_batch_create(int nbranches) {
+  if (nbranches < 0 || nbranches > 64) {
+    record_error(E_BAD_ARG, "batch: branch count must be 0 (default 8) .. 64");
+    return -1;
+  }
+  Batch *B = new Batch();
+  B->nbr = nbranches ? nbranches : 8;
+  std::lock_guard<std::mutex> g(g_bmu);
+  g_batches.push_back(B);
+  return (int)g_batches.size() - 1;
+}
+
+int p3dfft_gb300_batch_add(int batch, int job, int plan, const void *in, void *out, int idir) {
+  Batch *B = get_batch(batch);
+  if (!B) return fail(E_BAD_ARG, "batch: invalid handle");
+  if (job < 0) return fail(E_BAD_ARG, "batch: job ids are >= 0");
+  if (idir > 2) return fail(E_BAD_ARG, "batch: derivative direction out of range");
+  if (!in || !out) return fail(E_BAD_ARG, "batch: null data pointer");
+  if (plan3d_sizes(plan, nullptr, nullptr, nullptr, nullptr) != E_OK) return E_BAD_ARG;
+  cudaPointerAttributes a1, a2;
+  if (cudaPointerGetAttributes(&a1, in) != cudaSuccess || cudaPointerGetAttributes(&a2, out) != cudaSuccess ||
+      a1.type != cudaMemoryTypeDevice || a2.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    return fail(E_BAD_ARG, "batch: jobs take device pointers only");
+  }
+  B->jobs[job].push_back({plan, in, out, idir});
+  B->dirty = true;
+  return E_OK;
+}
+
+int p3dfft_gb300_batch_set_graph(int batch, int on) {
+  Batch *B = get_batch(batch);
+  if (!B) return fail(E_BAD_ARG, "batch: invalid handle");
+  B->use_graph = on != 0;
+  B->dirty = true;
+  return E_OK;
+}
+
+int p3dfft_gb300_batch_exec(int batch) {
+  Batch *B = get_batch(batch);
+  if (!B) return fail(E_BAD_ARG, "batch: invalid handle");
+  if (!device_ready()) return E_NO_DEVICE;
+  if (B->jobs.empty()) return E_OK;
+  const cudaStream_t st = library_stream();
+  const int ar = current_arith();
+  if (B->dirty || ar != B->arith || (B->use_graph && !B->gexec)) {
+    int rc = prepare(B);
+    if (rc != E_OK) return rc;
+    const long long k0 = kernel_count_now();
+    rc = run_branches(B, st, false);  // eager run: resolves tables, produces this call's results
+    if (rc != E_OK) return rc;
+    B->kernels = kernel_count_now() - k0;
+    if (B->use_graph) {
+      rc = build_graph(B);
+      if (rc != E_OK) return rc;
+    }
+    B->dirty = false;
+    B->arith = ar;
+    return finish(st);
+  }
+  if (B->use_graph) {
+    if (cudaGraphLaunch(B->gexec, st) != cudaSuccess) return fail(E_CUDA, "batch: graph launch failed");
+    add_kernel_count(B->kernels);
+  } else {
+    int rc = run_branches(B, st, false);
+    if (rc != E_OK) return rc;
+  }
+  return finish(st);
+}
+
+long long p3dfft_gb300_batch_kernels(int batch) {
+  Batch *B = get_batch(batch);
+  return B ? B->kernels : -1;
+}
+
+double p3dfft_gb300_batch_field_bytes(int batch) {
+  Batch *B = get_batch(batch);
+  return B ? B->bytes : -1.0;
+}
+
+int p3dfft_gb300_batch_destroy(int batch) {
+  Batch *B;
+  {
+    std::lock_guard<std::mutex> g(g_bmu);
+    if (batch < 0 || batch >= (int)g_batches.size() || !g_batches[batch]) return E_BAD_ARG;
+    B = g_batches[batch];
+    g_batches[batch] = nullptr;
+  }
+  cudaStreamSynchronize(library_stream());
+  delete B;
+  return E_OK;
+}
+
+}  // extern "C"

@@ -1,16 +1,19 @@
-// Specialised stage kernels for the hot transform kinds (C2C, even-length R2C and C2R) at
-// power-of-two FFT lengths 32..4096, one instantiation per (arithmetic, kind, length).
+// Specialised stage kernels for the hot transform kinds (C2C, even-length R2C and C2R) at FFT
+// lengths N = 2^a 3^b 5^c from 16 to 512 and 1024, 2048: one instantiation per (arithmetic,
+// kind, length), with the radix plan and every index computed at compile time.
 //
 // Same contract as k_stage (one reference transplan stage: gather a tile of lines along the
 // transform dimension from the input memory order, transform, scatter into the output memory
 // order), organised for instruction economy:
-//   - one tile of TB lines per CTA; twiddles through the read-only cache
-//   - every thread owns V points of one line (the same points for load, FFT and store), so all
-//     index arithmetic is compile-time except the per-tile base offsets
+//   - one tile of TB lines per CTA, lines numbered across both batch dims (a tile may span two
+//     rows of the tile dim, so no lanes idle when that dim is short); twiddles through the
+//     read-only cache
+//   - every thread owns V = N/T points of one line (the same points for load, FFT and store)
 //   - loads go to registers first; float-float tiles are scaled by a power of two chosen from
 //     the tile's largest exponent (block-wide max) before conversion, which keeps any finite
 //     input in range
-//   - radix-8/4/2 butterflies in registers, one padded shared-memory scatter per pass
+//   - Stockham passes of radix 8/4/2 then 5/3 in registers, one padded shared-memory scatter
+//     per pass; in a pass of radix R each thread does ceil(N/R / T) butterflies
 //   - R2C / C2R half-length packing and the fused i*k derivative are done on the way in / out
 #pragma once
 #include <cuda_runtime.h>
@@ -27,7 +30,8 @@ struct FParams {
   void *out;
   const void *tw;  // W_{tabN}^m, tabN = N (C2C) or 2N (R2C / C2R), m < tabN
   long long iL, it, io, oL, ot, oo;  // element strides
-  int dt, ntile, ntotal;             // tile-dim size, tiles along it, tiles in total
+  int dt;                            // size of the tile dim; line g is (g % dt, g / dt)
+  int nlines, ntotal;                // lines in total, CTAs
   int sign;                          // C2C: -1 forward, +1 backward
   int deriv, dg, dmid;               // fused derivative (compute_deriv_loc wavenumbers)
   int load_Lmajor, store_Lmajor;
@@ -38,11 +42,65 @@ struct FParams {
 #define FAST_MIN_BLOCKS 4
 #endif
 
-template <int N, int V>
+// The FFT lengths with a specialised kernel.
+#define P3D_FAST_LENGTHS(X)                                                                              \
+  X(16) X(18) X(20) X(24) X(25) X(27) X(30) X(32) X(36) X(40) X(45) X(48) X(50) X(54) X(60) X(64) X(72)   \
+  X(75) X(80) X(81) X(90) X(96) X(100) X(108) X(120) X(125) X(128) X(135) X(144) X(150) X(160) X(162)    \
+  X(180) X(192) X(200) X(216) X(225) X(240) X(243) X(250) X(256) X(270) X(288) X(300) X(320) X(324)      \
+  X(360) X(375) X(384) X(400) X(405) X(432) X(450) X(480) X(486) X(500) X(512) X(1024) X(2048)
+
+// Radix plan: radix-8 passes, the leftover power of two (4 or 2), then 5s, then 3s.
+struct RadixList {
+  int n;  // passes, -1 if N has a prime factor above 5
+  int r[16];
+};
+__host__ __device__ constexpr RadixList fast_radices(int N) {
+  RadixList L{0, {0}};
+  int a = 0, m = N;
+  while (m > 1 && m % 2 == 0) {
+    m /= 2;
+    a++;
+  }
+  for (int i = 0; i < a / 3; i++) L.r[L.n++] = 8;
+  if (a % 3 == 2) L.r[L.n++] = 4;
+  if (a % 3 == 1) L.r[L.n++] = 2;
+  while (m > 1 && m % 5 == 0) {
+    m /= 5;
+    L.r[L.n++] = 5;
+  }
+  while (m > 1 && m % 3 == 0) {
+    m /= 3;
+    L.r[L.n++] = 3;
+  }
+  if (m != 1) L.n = -1;
+  return L;
+}
+// points per thread: the largest divisor of N up to 8
+__host__ __device__ constexpr int fast_points(int N) {
+  for (int d = 8; d > 1; d--)
+    if (N % d == 0) return d;
+  return 1;
+}
+// most values a thread holds in one pass
+__host__ __device__ constexpr int fast_max_values(int N) {
+  const RadixList L = fast_radices(N);
+  const int T = N / fast_points(N);
+  int m = 0;
+  for (int i = 0; i < L.n; i++) {
+    const int nb = (N / L.r[i] + T - 1) / T;
+    if (nb * L.r[i] > m) m = nb * L.r[i];
+  }
+  return m;
+}
+
+template <int N>
 struct FastShape {
-  static constexpr int T = N / V;                      // threads per line
-  static constexpr int TB = T >= 256 ? 1 : 256 / T;    // lines per tile
-  static constexpr int BLOCK = TB * T;
+  static constexpr int V = fast_points(N);          // points per thread
+  static constexpr int T = N / V;                   // threads per line
+  static constexpr int TB = T >= 256 ? 1 : 256 / T;  // lines per tile
+  static constexpr int USED = TB * T;               // threads with a line
+  static constexpr int BLOCK = (USED + 31) / 32 * 32;
+  static constexpr int MINB = fast_max_values(N) > 8 ? 3 : FAST_MIN_BLOCKS;
   // Padded line stride (complex slots, > N + N/8 so slot N fits): chosen so that the TB lines of
   // a t-major access (consecutive threads on consecutive lines) fall in distinct 16-byte bank
   // groups, LS = 8/TB mod 8 (odd when TB >= 8).
@@ -61,25 +119,37 @@ __device__ __forceinline__ typename O::C fk_tw(const typename O::T *tab, int m, 
   return sign < 0 ? w : O::conj(w);
 }
 
-// Stockham passes in registers with a padded shared-memory scatter per pass (cf. fixed_pass).
-template <class O, int N, int V, int TWSTEP, int Ns, int R, int... Rest>
+// Stockham pass I (radix R = plan[I], Ns = product of the earlier radices): butterfly jj reads
+// x[jj + r N/R], multiplies by W_{Ns R}^{r k} (k = jj mod Ns), applies DFT-R and writes slot
+// (jj - k) R + k + r Ns.  Values stay in registers across the barrier; one scatter per pass.
+template <class O, int N, int TWSTEP, int Ns, int I>
 __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T *tab, int j, bool active, int sign) {
   using C = typename O::C;
-  constexpr int T = N / V, NB = V / R, M = N / R;
-  C v[V];
+  constexpr RadixList RL = fast_radices(N);
+  constexpr int R = RL.r[I];
+  constexpr int T = FastShape<N>::T, M = N / R;
+  constexpr int NB = (M + T - 1) / T;  // butterflies per thread
+  constexpr bool GUARD = (M % T) != 0;
+  C v[NB * R];
+  C w1, w2;  // W_R^1, W_R^2 for the odd radices
+  if constexpr (R == 3 || R == 5) w1 = O::tw(tab, (N / R) * TWSTEP);
+  if constexpr (R == 5) w2 = O::tw(tab, 2 * (N / R) * TWSTEP);
   if (active) {
 #pragma unroll
     for (int b = 0; b < NB; b++) {
       const int jj = j + b * T;
+      if (GUARD && jj >= M) break;
 #pragma unroll
       for (int r = 0; r < R; r++) v[b * R + r] = line[pad<3>(jj + r * M)];
       if (Ns > 1) {
-        const int k = jj & (Ns - 1);
+        const int k = jj % Ns;
 #pragma unroll
         for (int r = 1; r < R; r++)
           v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(tab, r * k * (N / (Ns * R)) * TWSTEP, sign));
       }
-      dft_p2<O, R>(&v[b * R], sign);
+      if constexpr (R == 3) dft3<O>(&v[b * R], sign, w1);
+      else if constexpr (R == 5) dft5<O>(&v[b * R], sign, w1, w2);
+      else dft_p2<O, R>(&v[b * R], sign);
     }
   }
   __syncthreads();
@@ -87,14 +157,15 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
 #pragma unroll
     for (int b = 0; b < NB; b++) {
       const int jj = j + b * T;
-      const int k = jj & (Ns - 1);
+      if (GUARD && jj >= M) break;
+      const int k = jj % Ns;
       const int base = (jj - k) * R + k;
 #pragma unroll
       for (int r = 0; r < R; r++) line[pad<3>(base + r * Ns)] = O::norm(v[b * R + r]);
     }
   }
   __syncthreads();
-  if constexpr (sizeof...(Rest) > 0) fk_pass<O, N, V, TWSTEP, Ns * R, Rest...>(line, tab, j, active, sign);
+  if constexpr (I + 1 < RL.n) fk_pass<O, N, TWSTEP, Ns * R, I + 1>(line, tab, j, active, sign);
 }
 
 template <class O>
@@ -104,20 +175,21 @@ __device__ __forceinline__ typename O::C fk_deriv(const FParams &p, typename O::
   return O::iscale(v, (k < p.dmid) ? k : k - p.dg);
 }
 
-template <class O, int KIND, int N, int V, int... Rs>
-__global__ void __launch_bounds__(FastShape<N, V>::BLOCK, FAST_MIN_BLOCKS * 256 / FastShape<N, V>::BLOCK)
-    k_fast(FParams p) {
+template <class O, int KIND, int N>
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fast(FParams p) {
   using C = typename O::C;
   using T = typename O::T;
   using G = typename O::G;
   using RAW = typename O::RAW;
-  using SH = FastShape<N, V>;
+  using SH = FastShape<N>;
   constexpr int TWSTEP = (KIND == FK_C2C) ? 1 : 2;  // FFT twiddle W_N^m = tab[m * TWSTEP]
-  constexpr int LS = SH::LS, TB = SH::TB, TT = SH::T;
+  constexpr int LS = SH::LS, TB = SH::TB, TT = SH::T, V = SH::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf = reinterpret_cast<C *>(smem_raw);
   __shared__ int red[32];
   const T *tab = reinterpret_cast<const T *>(p.tw);
+  // threads past TB*T (BLOCK rounded up to whole warps) hold no line
+  const bool valid = SH::BLOCK == SH::USED || (int)threadIdx.x < SH::USED;
 
   // this thread's line and first point: the same V points j0 + e*TT for load, FFT and store
   int l, j0;
@@ -141,12 +213,11 @@ __global__ void __launch_bounds__(FastShape<N, V>::BLOCK, FAST_MIN_BLOCKS * 256 
 
   // One tile per CTA: a persistent loop over tiles was measured to keep ~80 more registers live.
   {
-    const int tile = blockIdx.x;
-    const int tt = tile % p.ntile, oth = tile / p.ntile;
-    const int t0 = tt * TB;
-    const int nlines = min(TB, p.dt - t0);
-    const bool act = l < nlines;
-    const long long ibase = (long long)(t0 + l) * p.it + (long long)oth * p.io;
+    const int g0 = blockIdx.x * TB;
+    const int gl = g0 + l;
+    const bool act = valid && gl < p.nlines;
+    const int lt = gl % p.dt, lo = gl / p.dt;
+    const long long ibase = (long long)lt * p.it + (long long)lo * p.io;
 
     // ---------------- load the tile into shared memory ----------------
     // Raw input values go straight to their slot (slot N holds X[N] for C2R).  Float-float tiles
@@ -236,13 +307,14 @@ __global__ void __launch_bounds__(FastShape<N, V>::BLOCK, FAST_MIN_BLOCKS * 256 
     __syncthreads();
 
     // ---------------- FFT ----------------
-    fk_pass<O, N, V, TWSTEP, 1, Rs...>(lb, tab, j0, act, KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1));
+    fk_pass<O, N, TWSTEP, 1, 0>(lb, tab, j0, act, KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1));
 
     // ---------------- post-processing + store ----------------
-    const bool sact = ls < nlines;
+    const int gs = g0 + ls;
+    const bool sact = valid && gs < p.nlines;
     if (sact) {
       const C *Y = buf + (size_t)ls * LS;
-      const long long obase = (long long)(t0 + ls) * p.ot + (long long)oth * p.oo;
+      const long long obase = (long long)(gs % p.dt) * p.ot + (long long)(gs / p.dt) * p.oo;
 #pragma unroll 2
       for (int e = 0; e < V; e++) {
         const int k = js + e * TT;
@@ -278,12 +350,13 @@ struct FastArgs {
   FParams p;
 };
 
-template <class O, int KIND, int N, int V, int... Rs>
+template <class O, int KIND, int N>
 static int fk_launch(const FParams &p, cudaStream_t st) {
-  using SH = FastShape<N, V>;
+  using SH = FastShape<N>;
+  static_assert(fast_radices(N).n > 0, "length must be 2^a 3^b 5^c");
   const size_t smem = sizeof(typename O::C) * (size_t)SH::TB * SH::LS;
   static bool configured = false;
-  auto kern = k_fast<O, KIND, N, V, Rs...>;
+  auto kern = k_fast<O, KIND, N>;
   if (!configured) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return E_CUDA;
     configured = true;
@@ -296,34 +369,55 @@ static int fk_launch(const FParams &p, cudaStream_t st) {
 template <class O, int KIND>
 static int fk_dispatch_n(int n, const FParams &p, cudaStream_t st) {
   switch (n) {
-    case 32: return fk_launch<O, KIND, 32, 8, 8, 4>(p, st);
-    case 64: return fk_launch<O, KIND, 64, 8, 8, 8>(p, st);
-    case 128: return fk_launch<O, KIND, 128, 8, 8, 8, 2>(p, st);
-    case 256: return fk_launch<O, KIND, 256, 8, 8, 8, 4>(p, st);
-    case 512: return fk_launch<O, KIND, 512, 8, 8, 8, 8>(p, st);
-    case 1024: return fk_launch<O, KIND, 1024, 8, 8, 8, 8, 2>(p, st);
-    case 2048: return fk_launch<O, KIND, 2048, 8, 8, 8, 8, 4>(p, st);
+#define P3D_FAST_CASE(L) \
+  case L: return fk_launch<O, KIND, L>(p, st);
+    P3D_FAST_LENGTHS(P3D_FAST_CASE)
+#undef P3D_FAST_CASE
     default: return E_UNSUPPORTED;
   }
 }
+
+// One (arithmetic, kind) pair per translation unit (fast_inst.cu), so they compile in parallel.
+template <class O, int KIND>
+int fast_launch_kind(int n, const FParams &p, cudaStream_t st);
+template <> int fast_launch_kind<DF, FK_C2C>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<DF, FK_R2C>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<DF, FK_C2R>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<Native<double>, FK_C2C>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<Native<double>, FK_R2C>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<Native<double>, FK_C2R>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<Native<float>, FK_C2C>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<Native<float>, FK_R2C>(int, const FParams &, cudaStream_t);
+template <> int fast_launch_kind<Native<float>, FK_C2R>(int, const FParams &, cudaStream_t);
 
 template <class O>
-static int fk_dispatch(const FastArgs &a, cudaStream_t st) {
+inline int fast_launch_arith(const FastArgs &a, cudaStream_t st) {
   switch (a.kind) {
-    case FK_C2C: return fk_dispatch_n<O, FK_C2C>(a.n, a.p, st);
-    case FK_R2C: return fk_dispatch_n<O, FK_R2C>(a.n, a.p, st);
-    case FK_C2R: return fk_dispatch_n<O, FK_C2R>(a.n, a.p, st);
+    case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, st);
+    case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, st);
+    case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, st);
     default: return E_UNSUPPORTED;
   }
 }
 
-int launch_fast_df(const FastArgs &a, cudaStream_t st);
-int launch_fast_f64(const FastArgs &a, cudaStream_t st);
-int launch_fast_f32(const FastArgs &a, cudaStream_t st);
+// prec 4: FP32; prec 8: float-float (arith AR_DF) or native FP64
+inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st) {
+  if (prec == 4) return fast_launch_arith<Native<float>>(a, st);
+  if (arith == AR_DF) return fast_launch_arith<DF>(a, st);
+  return fast_launch_arith<Native<double>>(a, st);
+}
 
-inline bool fast_supported(int n) { return n >= 32 && n <= 2048 && (n & (n - 1)) == 0; }
+inline bool fast_supported(int n) {
+  switch (n) {
+#define P3D_FAST_CASE(L) case L:
+    P3D_FAST_LENGTHS(P3D_FAST_CASE)
+#undef P3D_FAST_CASE
+    return true;
+    default: return false;
+  }
+}
 inline int fast_tile_lines(int n) {
-  const int T = n / 8;
+  const int T = n / fast_points(n);
   return T >= 256 ? 1 : 256 / T;
 }
 

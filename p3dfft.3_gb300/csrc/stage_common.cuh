@@ -54,6 +54,7 @@ struct Native {
     const R c = R(0.70710678118654752440084436210485);
     return mk(a.x * c, a.y * c);
   }
+  static __device__ __forceinline__ C rmul(C a, S c) { return mk(a.x * c, a.y * c); }  // real scalar
   static __device__ __forceinline__ C iscale(C a, int k) {  // a * (i*k)
     R kk = R(k);
     return mk(-kk * a.y, kk * a.x);
@@ -127,6 +128,9 @@ struct DF {
   }
   static __device__ __forceinline__ C iscale(C a, int k) {
     return mk(ff_neg(ff_mul_int(a.y, k)), ff_mul_int(a.x, k));
+  }
+  static __device__ __forceinline__ C rmul(C a, S c) {  // real scalar, unnormalised
+    return mk(ff_mul_const_nn(a.x, c.hi, c.lo), ff_mul_const_nn(a.y, c.hi, c.lo));
   }
   static __device__ __forceinline__ S rzero() { return ff{0.f, 0.f}; }
   static __device__ __forceinline__ C zero() { return mk(rzero(), rzero()); }
@@ -226,6 +230,42 @@ __device__ __forceinline__ void dft_p2(typename O::C *v, int sign) {
     v[3] = O::add(e[3], o3);
     v[7] = O::sub(e[3], o3);
   }
+}
+
+// Radix-3 and radix-5 DFTs (sign -1 forward, +1 backward).  The real constants cos/sin(2 pi q/R)
+// come from twiddle-table entries w1 = W_R^1 = (cos 2pi/R, -sin 2pi/R) and w2 = W_R^2, so they
+// carry the table's precision.  Pairing x_j with x_{R-j} leaves one real multiply per constant:
+//   y_q = x0 + sum_j cos(2pi jq/R) (x_j + x_{R-j}) + sign*i sum_j sin(2pi jq/R) (x_j - x_{R-j}).
+template <class O>
+__device__ __forceinline__ void dft3(typename O::C *v, int sign, typename O::C w1) {
+  using C = typename O::C;
+  const C a = O::add(v[1], v[2]), b = O::sub(v[1], v[2]);
+  const C m = O::sub(v[0], O::half(a));  // x0 + cos(2pi/3) a, cos(2pi/3) = -1/2
+  C t = O::rmul(b, O::negs(w1.y));        // sin(2pi/3) b
+  t = sign < 0 ? O::mulmi(t) : O::muli(t);
+  v[0] = O::add(v[0], a);
+  v[1] = O::add(m, t);
+  v[2] = O::sub(m, t);
+}
+
+template <class O>
+__device__ __forceinline__ void dft5(typename O::C *v, int sign, typename O::C w1, typename O::C w2) {
+  using C = typename O::C;
+  using S = typename O::S;
+  const S c1 = w1.x, s1 = O::negs(w1.y), c2 = w2.x, s2 = O::negs(w2.y);
+  const C a1 = O::add(v[1], v[4]), b1 = O::sub(v[1], v[4]);
+  const C a2 = O::add(v[2], v[3]), b2 = O::sub(v[2], v[3]);
+  const C m1 = O::add(v[0], O::add(O::rmul(a1, c1), O::rmul(a2, c2)));
+  const C m2 = O::add(v[0], O::add(O::rmul(a1, c2), O::rmul(a2, c1)));
+  C t1 = O::add(O::rmul(b1, s1), O::rmul(b2, s2));
+  C t2 = O::sub(O::rmul(b1, s2), O::rmul(b2, s1));
+  t1 = sign < 0 ? O::mulmi(t1) : O::muli(t1);
+  t2 = sign < 0 ? O::mulmi(t2) : O::muli(t2);
+  v[0] = O::add(v[0], O::add(a1, a2));
+  v[1] = O::add(m1, t1);
+  v[4] = O::sub(m1, t1);
+  v[2] = O::add(m2, t2);
+  v[3] = O::sub(m2, t2);
 }
 
 }  // namespace p3d

@@ -93,8 +93,12 @@ __device__ __forceinline__ void dft_reg(typename O::C *v, int sign, const KParam
     v[6] = O::sub(e[2], o2);
     v[3] = O::add(e[3], o3);
     v[7] = O::sub(e[3], o3);
+  } else if (R == 3) {
+    dft3<O>(v, sign, twid<O>(p, p.nfft / 3, -1));
+  } else if (R == 5) {
+    dft5<O>(v, sign, twid<O>(p, p.nfft / 5, -1), twid<O>(p, 2 * (p.nfft / 5), -1));
   } else {
-    // odd radix: direct sum with W_R^q from the table (index q * nfft/R)
+    // other odd radix: direct sum with W_R^q from the table (index q * nfft/R)
     C out[R];
     const int unit = p.nfft / R;
 #pragma unroll
@@ -766,10 +770,10 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.oo = p.oo;
     q.dt = p.dt;
     const int TB = fast_tile_lines(p.nfft);
-    q.ntile = (p.dt + TB - 1) / TB;
-    long long ntot = (long long)q.ntile * p.dother;
-    if (ntot > 0x7fffffffLL) return E_TOO_LARGE;
-    q.ntotal = (int)ntot;
+    const long long nl = (long long)p.dt * p.dother;
+    if (nl + TB > 0x7fffffffLL) return E_TOO_LARGE;
+    q.nlines = (int)nl;
+    q.ntotal = (int)((nl + TB - 1) / TB);
     q.sign = p.sign;
     q.deriv = p.deriv;
     q.dg = p.dg;
@@ -777,10 +781,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.load_Lmajor = p.load_Lmajor;
     q.store_Lmajor = p.store_Lmajor;
     if (q.ntotal == 0) return E_OK;
-    int rc;
-    if (d.prec == 4) rc = launch_fast_f32(fa, stream);
-    else if (arith == AR_DF) rc = launch_fast_df(fa, stream);
-    else rc = launch_fast_f64(fa, stream);
+    const int rc = launch_fast(d.prec, arith, fa, stream);
     if (rc == E_OK && kernels_launched) (*kernels_launched)++;
     return rc;
   }

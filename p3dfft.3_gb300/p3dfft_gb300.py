@@ -84,6 +84,13 @@ def lib():
         "p3dfft_gb300_event_elapsed_ms": ([ctypes.c_int, ctypes.c_int], ctypes.c_double),
         "p3dfft_gb300_profile_stages": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_double), ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_create": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_add": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_set_graph": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_exec": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_kernels": ([ctypes.c_int], ctypes.c_longlong),
+        "p3dfft_gb300_batch_field_bytes": ([ctypes.c_int], ctypes.c_double),
+        "p3dfft_gb300_batch_destroy": ([ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -300,5 +307,44 @@ class PinnedArray:
             if _lib is not None and self.ptr:
                 self.array = None
                 _lib.p3dfft_gb300_host_free_pinned(ctypes.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+class Batch:
+    """Independent jobs run concurrently and replayed as one CUDA graph (p3dfft_gb300_batch_*).
+
+    A job is an ordered list of steps (Transform3D, device input, device output, idir); the steps
+    of one job run in order, different jobs run on concurrent branch streams."""
+
+    def __init__(self, nbranches=0, graph=True):
+        setup()
+        h = lib().p3dfft_gb300_batch_create(int(nbranches))
+        if h < 0:
+            check(-1)
+        self.handle = h
+        self._keep = []
+        if not graph:
+            check(lib().p3dfft_gb300_batch_set_graph(h, 0))
+
+    def add(self, job, plan, inp, out, idir=-1):
+        pi, k1 = _ptr(inp)
+        po, k2 = _ptr(out)
+        self._keep += [plan, k1, k2]
+        check(lib().p3dfft_gb300_batch_add(self.handle, int(job), plan.handle, pi, po, int(idir)))
+
+    def exec(self):
+        check(lib().p3dfft_gb300_batch_exec(self.handle))
+
+    def kernels(self):
+        return int(lib().p3dfft_gb300_batch_kernels(self.handle))
+
+    def field_bytes(self):
+        return float(lib().p3dfft_gb300_batch_field_bytes(self.handle))
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", -1) >= 0 and _lib is not None:
+                _lib.p3dfft_gb300_batch_destroy(self.handle)
         except Exception:
             pass
