@@ -326,6 +326,129 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
     return out
 
 
+# ------------------------------------------------------------------------------------------
+# Serving stream: Poisson arrivals of jobs with axes log-uniform in [32, 512] rounded to
+# 2^a 3^b 5^c, 70/30 R2C/C2C, 60/40 FP32/FP64, each forward -> d/dx -> backward, admitted under a
+# 120 GB HBM budget; latency percentiles at three arrival rates (fractions of the measured
+# saturation throughput).  Fields are resident in HBM: each job copies its input from a device
+# source field into its own pool-allocated field and its result out to a device sink.
+def _smooth5_list():
+    out = []
+    for n in range(16, 1025):
+        m = n
+        for p in (2, 3, 5):
+            while m % p == 0:
+                m //= p
+        if m == 1:
+            out.append(n)
+    return out
+
+
+def serve_jobs(n_jobs, seed=5):
+    """(dims, kind, prec) per job: each axis exp(U[ln 32, ln 512]) rounded to the nearest
+    2^a 3^b 5^c (the R2C axis to the nearest even one, as C2R needs an even length)."""
+    sm = np.array(_smooth5_list())
+    even = sm[sm % 2 == 0]
+    rng = np.random.default_rng(seed)
+    raw = np.exp(rng.uniform(np.log(32), np.log(512), (n_jobs, 3)))
+    kinds = np.where(rng.random(n_jobs) < 0.7, "r2c", "c2c")
+    precs = np.where(rng.random(n_jobs) < 0.6, 4, 8)
+    jobs = []
+    for i in range(n_jobs):
+        d = []
+        for a in range(3):
+            cand = even if (a == 0 and kinds[i] == "r2c") else sm
+            d.append(int(cand[np.argmin(np.abs(cand - raw[i, a]))]))
+        jobs.append((tuple(d), str(kinds[i]), int(precs[i])))
+    return jobs
+
+
+def serve_job_bytes(gd, kind, prec):
+    """3-pass algorithmic bytes of one forward + backward (the fused derivative adds none)."""
+    n = gd[0] * gd[1] * gd[2]
+    if kind == "r2c":
+        return round_trip_bytes(gd, prec)
+    return 12 * 2 * prec * n
+
+
+def serve_workload(p3d, n_jobs=10000, seed=5, fractions=(0.5, 0.75, 0.9), nslots=16, budget=120 << 30):
+    jobs = serve_jobs(n_jobs, seed)
+    plans = {}
+
+    def plan_pair(gd, kind, prec):
+        key = (gd, kind, prec)
+        if key not in plans:
+            if kind == "r2c":
+                ft, bt, gd2, dcs = (5, 9, 9), (7, 11, 11), (gd[0] // 2 + 1, gd[1], gd[2]), 0
+            else:
+                ft, bt, gd2, dcs = (9, 9, 9), (11, 11, 11), gd, -1
+            if prec == 4:
+                ft, bt = tuple(t - 1 for t in ft), tuple(t - 1 for t in bt)
+            plans[key] = (p3d.Transform3D(ft, gd, MO1, gd2, MO2, -1, dcs), p3d.Transform3D(bt, gd2, MO2, gd, MO1, dcs, -1))
+        return plans[key]
+
+    t_plan = time.perf_counter()
+    pairs = [plan_pair(*j) for j in jobs]
+    t_plan = time.perf_counter() - t_plan
+    print(f"serve: {len(plans)} plans in {t_plan:.1f} s", file=sys.stderr, flush=True)
+    maxn = 512 ** 3
+    src, sink = {}, {}
+    for prec in (4, 8):
+        rdt = np.float32 if prec == 4 else np.float64
+        x = np.random.default_rng(55 + prec).uniform(-1, 1, 2 * maxn).astype(rdt)
+        src[prec] = p3d.DeviceArray(x.nbytes)
+        src[prec].upload(x)
+        sink[prec] = p3d.DeviceArray(x.nbytes)
+        del x
+    alg = np.array([serve_job_bytes(*j) for j in jobs], dtype=np.float64)
+
+    def run(arrivals, srv):
+        ids = []
+        for (gd, kind, prec), (f, b), ta in zip(jobs, pairs, arrivals):
+            ids.append(srv.submit(f, b, src[prec], sink[prec], idir=0, arrival=ta))
+        srv.drain()
+        t = np.array([srv.job_times(i)[1] for i in ids])
+        return t[:, 0], t[:, 1], t[:, 2], srv.stats()
+
+    out = {"jobs": n_jobs, "seed": seed, "slots": nslots, "budget_bytes": budget,
+           "mix": {"r2c": sum(j[1] == "r2c" for j in jobs), "c2c": sum(j[1] == "c2c" for j in jobs),
+                   "fp32": sum(j[2] == 4 for j in jobs), "fp64": sum(j[2] == 8 for j in jobs)},
+           "distinct_grids": len(plans), "plan_time_s": t_plan,
+           "mean_input_MB": float(np.mean([np.prod(j[0]) * j[2] * (1 if j[1] == "r2c" else 2) for j in jobs]) / 1e6)}
+    # warm-up + saturation throughput: a closed burst of every job at once
+    srv = p3d.Server(budget, nslots)
+    lead = 0.3 + 1e-4 * n_jobs
+    t0 = srv.clock() + lead
+    ta, tadm, td, st = run([t0] * n_jobs, srv)
+    srv.close()
+    makespan = td.max() - t0
+    cap = n_jobs / makespan
+    print(f"serve: saturation {cap:.0f} jobs/s", file=sys.stderr, flush=True)
+    out["saturation"] = {"jobs_per_s": cap, "GB_per_s": alg.sum() / makespan / 1e9,
+                         "max_running": st["max_running"], "peak_hbm_GB": st["peak_hbm_bytes"] / 1e9}
+    rng = np.random.default_rng(seed + 1)
+    out["rates"] = []
+    for frac in fractions:
+        rate = frac * cap
+        srv = p3d.Server(budget, nslots)
+        t0 = srv.clock() + lead
+        arr = t0 + np.cumsum(rng.exponential(1.0 / rate, n_jobs))
+        ta, tadm, td, st = run(arr, srv)
+        srv.close()
+        lat = (td - ta) * 1e3
+        wait = (tadm - ta) * 1e3
+        span = td.max() - ta.min()
+        out["rates"].append({
+            "offered_jobs_per_s": rate, "fraction_of_saturation": frac,
+            "throughput_jobs_per_s": n_jobs / span, "GB_per_s": alg.sum() / span / 1e9,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max()), "mean": float(lat.mean())},
+            "queue_wait_ms": {"p50": float(np.percentile(wait, 50)), "p99": float(np.percentile(wait, 99))},
+            "failed": st["failed"], "max_running": st["max_running"], "peak_hbm_GB": st["peak_hbm_bytes"] / 1e9})
+    del src, sink
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,9 +458,11 @@ def main():
     ap.add_argument("--arith", default="auto", choices=["auto", "df", "native"],
                     help="FP64 arithmetic: float-float (df) or native DFMA; auto = df")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="roundtrip", choices=["roundtrip", "batch"],
-                    help="roundtrip: the 512^3 headline; batch: 48 uneven round trips only")
+    ap.add_argument("--workload", default="roundtrip", choices=["roundtrip", "batch", "serve"],
+                    help="roundtrip: the 512^3 headline; batch: 48 uneven round trips; serve: the serving stream")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload summary")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream summary")
+    ap.add_argument("--serve-jobs", type=int, default=10000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -351,6 +476,14 @@ def main():
         res = batch_workload(p3d, p3d.lib(), args.steps, args.warmup)
         if rank == 0:
             print(json.dumps({"workload": "batched uneven round trips", **res}), flush=True)
+        return
+    if args.workload == "serve":
+        import p3dfft_gb300 as p3d
+        import build_lib
+        build_lib.build()
+        res = serve_workload(p3d, n_jobs=args.serve_jobs)
+        if rank == 0:
+            print(json.dumps({"workload": "serving stream", **res}), flush=True)
         return
 
     import ctypes
@@ -506,6 +639,8 @@ def main():
     if not args.no_batch:
         del d_in, d_spec, d_out  # free HBM for the batch buffers
         forms["batched_uneven"] = batch_workload(p3d, L, max(3, min(args.steps, 10)), 3)
+    if not args.no_serve:
+        forms["serving"] = serve_workload(p3d, n_jobs=args.serve_jobs)
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

@@ -93,7 +93,32 @@ long long p3dfft_gb300_batch_kernels(int batch);
 double p3dfft_gb300_batch_field_bytes(int batch);
 int p3dfft_gb300_batch_destroy(int batch);
 
+/* ---- serving loop (no counterpart in the reference) ----
+ * A server runs jobs (forward 3D plan, backward 3D plan, idir, in, out): `in` is copied into HBM,
+ * transformed forward with the derivative along idir fused (idir < 0: none), transformed back,
+ * and the result written to `out`.  in / out may be host memory (page-locked for overlap) or
+ * device memory; the job's HBM fields come from the server's memory pool.  Jobs are admitted in
+ * arrival order (bounded look-ahead) while a slot is free and their HBM need fits in the budget;
+ * up to `nslots` jobs run concurrently on their own streams.  arrival_s >= 0 schedules the job's
+ * arrival that many seconds after server creation (trace replay); < 0 means now. */
+int p3dfft_gb300_server_create(long long hbm_budget_bytes, int nslots);
+int p3dfft_gb300_server_submit(int srv, int plan_fwd, int plan_bwd, int idir, const void *in, void *out,
+                               double arrival_s);
+/* 0 done, 1 timeout (timeout_s < 0 waits indefinitely), < 0 failed with error -return */
+int p3dfft_gb300_server_wait(int srv, int job, double timeout_s);
+int p3dfft_gb300_server_drain(int srv);
+/* seconds since server creation */
+double p3dfft_gb300_server_clock(int srv);
+/* t[0] arrival, t[1] admission, t[2] completion, on the server clock */
+int p3dfft_gb300_server_job_times(int srv, int job, double *t);
+/* completed, failed, admitted, peak HBM bytes held by jobs, budget, most jobs running at once */
+int p3dfft_gb300_server_stats(int srv, double *stats, int n);
+int p3dfft_gb300_server_destroy(int srv);
+
 /* ---- introspection and timers ---- */
+/* loads every specialised stage kernel now instead of at its first launch (servers call this at
+ * start-up so that no job pays a module load) */
+int p3dfft_gb300_preload_kernels(void);
 /* number of kernels this library launched since the last reset */
 long long p3dfft_gb300_kernel_count(void);
 void p3dfft_gb300_reset_kernel_count(void);

@@ -146,9 +146,10 @@ struct Buffers {
   size_t scratch_bytes = 0;
   void *stage_in = nullptr, *stage_out = nullptr;
   size_t stage_in_bytes = 0, stage_out_bytes = 0;
+  bool owned = true;  // false: scratch[] belongs to the caller (never freed or reallocated here)
   void release() {
     for (int i = 0; i < 2; i++)
-      if (scratch[i]) cudaFree(scratch[i]);
+      if (scratch[i] && owned) cudaFree(scratch[i]);
     if (stage_in) cudaFree(stage_in);
     if (stage_out) cudaFree(stage_out);
     scratch[0] = scratch[1] = stage_in = stage_out = nullptr;
@@ -588,7 +589,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     if (!cand) {
       int k = (dst[s + 1] == B.scratch[0] && B.scratch[0]) ? 1 : 0;
       if (need > B.scratch_bytes || !B.scratch[k]) {
-        if (in_capture()) {  // a graph must not record an allocation
+        if (in_capture() || !B.owned) {  // a graph must not record an allocation
           set_err(E_PLAN, "scratch set too small for a captured plan (%zu bytes needed)", need);
           return E_PLAN;
         }
@@ -623,6 +624,10 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     if (stage_ev) cudaEventRecord(stage_ev[s], cur_stream());
     if (d == src) {  // single-stage in-place call: go through scratch, then copy back
       size_t bytes = stage_out_bytes(P, st);
+      if ((in_capture() || !B.owned) && (bytes > B.scratch_bytes || !B.scratch[0])) {
+        set_err(E_PLAN, "scratch set too small for an in-place stage (%zu bytes needed)", bytes);
+        return E_PLAN;
+      }
       if (!ensure_buf(&B.scratch[0], &B.scratch_bytes, std::max(bytes, B.scratch_bytes))) return E_CUDA;
       rc = run_stage(P, st, src, B.scratch[0], deriv);
       if (rc == E_OK && cudaMemcpyAsync(d, B.scratch[0], bytes, cudaMemcpyDeviceToDevice, cur_stream()) != cudaSuccess)
@@ -765,6 +770,15 @@ void scratch_set_destroy(void *b) {
 }
 
 size_t scratch_set_bytes(const void *b) { return b ? static_cast<const Buffers *>(b)->scratch_bytes : 0; }
+
+void *scratch_set_wrap(void *s0, void *s1, size_t bytes) {
+  Buffers *B = new Buffers();
+  B->scratch[0] = s0;
+  B->scratch[1] = s1;
+  B->scratch_bytes = bytes;
+  B->owned = false;
+  return B;
+}
 
 int scratch_set_reserve(void *b, size_t bytes) {
   Buffers *B = static_cast<Buffers *>(b);
@@ -1038,6 +1052,13 @@ int p3dfft_gb300_profile_stages(int plan, const void *in, void *out, int idir, i
   for (auto &e : ev) cudaEventDestroy(e);
   for (int s = 0; s < n && s < max_stages; s++) ms[s] = reps > 0 ? acc[s] / reps : 0.0;
   return rc == E_OK ? n : -1;
+}
+
+int p3dfft_gb300_preload_kernels(void) {
+  if (!ensure_device()) return t_err;
+  const int rc = preload_kernels();
+  if (rc != E_OK) set_err(rc, "kernel preload failed: %s", cudaGetErrorString(cudaGetLastError()));
+  return rc;
 }
 
 long long p3dfft_gb300_kernel_count(void) { return g_kcount.load(); }

@@ -351,23 +351,44 @@ struct FastArgs {
 };
 
 template <class O, int KIND, int N>
-static int fk_launch(const FParams &p, cudaStream_t st) {
-  using SH = FastShape<N>;
+constexpr size_t fk_smem() {
+  return sizeof(typename O::C) * (size_t)FastShape<N>::TB * FastShape<N>::LS;
+}
+
+// Sets the kernel's dynamic shared-memory limit once; this also loads the kernel's module (which
+// CUDA otherwise does lazily at the first launch).
+template <class O, int KIND, int N>
+static int fk_configure() {
   static_assert(fast_radices(N).n > 0, "length must be 2^a 3^b 5^c");
-  const size_t smem = sizeof(typename O::C) * (size_t)SH::TB * SH::LS;
   static bool configured = false;
-  auto kern = k_fast<O, KIND, N>;
   if (!configured) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return E_CUDA;
+    if (cudaFuncSetAttribute(k_fast<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fk_smem<O, KIND, N>()) != cudaSuccess)
+      return E_CUDA;
     configured = true;
   }
+  return E_OK;
+}
+
+template <class O, int KIND, int N>
+static int fk_launch(const FParams &p, cudaStream_t st) {
+  if (fk_configure<O, KIND, N>() != E_OK) return E_CUDA;
   if (p.ntotal <= 0) return E_OK;
-  kern<<<(unsigned)p.ntotal, SH::BLOCK, smem, st>>>(p);
+  k_fast<O, KIND, N><<<(unsigned)p.ntotal, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(p);
   return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
 }
 
+// n > 0: launch the length-n kernel; n == 0: configure (load) every length's kernel
 template <class O, int KIND>
 static int fk_dispatch_n(int n, const FParams &p, cudaStream_t st) {
+  if (n == 0) {
+    int rc = E_OK;
+#define P3D_FAST_CASE(L) \
+  if (fk_configure<O, KIND, L>() != E_OK) rc = E_CUDA;
+    P3D_FAST_LENGTHS(P3D_FAST_CASE)
+#undef P3D_FAST_CASE
+    return rc;
+  }
   switch (n) {
 #define P3D_FAST_CASE(L) \
   case L: return fk_launch<O, KIND, L>(p, st);
@@ -398,6 +419,22 @@ inline int fast_launch_arith(const FastArgs &a, cudaStream_t st) {
     case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, st);
     default: return E_UNSUPPORTED;
   }
+}
+
+// Loads every specialised kernel of one arithmetic (prec 4, or prec 8 with arith).
+inline int fast_preload(int prec, int arith) {
+  FastArgs a{};
+  int rc = E_OK;
+  for (int k = FK_C2C; k <= FK_C2R; k++) {
+    a.kind = k;
+    a.n = 0;
+    int r;
+    if (prec == 4) r = fast_launch_arith<Native<float>>(a, 0);
+    else if (arith == AR_DF) r = fast_launch_arith<DF>(a, 0);
+    else r = fast_launch_arith<Native<double>>(a, 0);
+    if (r != E_OK) rc = r;
+  }
+  return rc;
 }
 
 // prec 4: FP32; prec 8: float-float (arith AR_DF) or native FP64

@@ -44,6 +44,10 @@ struct StageDesc {
 
 struct DeviceTables;  // twiddle-table cache, one per device
 
+// Loads the module of every specialised stage kernel now (CUDA loads kernels lazily at their first
+// launch, which would otherwise land inside the first transform of each length).
+int preload_kernels();
+
 // Twiddle tables a stage needs: W_tabN^k (and W_auxN^k for the generic DCT/DST kinds, auxN 0
 // if none), in format fmt (0 double pairs, 1 float pairs, 2 float-float pairs).
 struct TableNeed {

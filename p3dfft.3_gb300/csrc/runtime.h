@@ -14,6 +14,8 @@ void scratch_set_destroy(void *set);
 size_t scratch_set_bytes(const void *set);
 // allocates both slots at `bytes` each (no-op when already that large)
 int scratch_set_reserve(void *set, size_t bytes);
+// a set over two caller-owned device buffers of `bytes` each (not freed by scratch_set_destroy)
+void *scratch_set_wrap(void *s0, void *s1, size_t bytes);
 
 // field sizes of a 3D plan, and the size of each scratch slot its stage chain needs
 int plan3d_sizes(int plan, size_t *in_bytes, size_t *out_bytes, size_t *scratch_bytes, int *prec);

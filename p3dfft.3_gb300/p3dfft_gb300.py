@@ -91,6 +91,16 @@ def lib():
         "p3dfft_gb300_batch_kernels": ([ctypes.c_int], ctypes.c_longlong),
         "p3dfft_gb300_batch_field_bytes": ([ctypes.c_int], ctypes.c_double),
         "p3dfft_gb300_batch_destroy": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_server_create": ([ctypes.c_longlong, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_preload_kernels": ([], ctypes.c_int),
+        "p3dfft_gb300_server_submit": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp,
+                                        ctypes.c_double], ctypes.c_int),
+        "p3dfft_gb300_server_wait": ([ctypes.c_int, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+        "p3dfft_gb300_server_drain": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_server_clock": ([ctypes.c_int], ctypes.c_double),
+        "p3dfft_gb300_server_job_times": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "p3dfft_gb300_server_stats": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_server_destroy": ([ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -346,5 +356,64 @@ class Batch:
         try:
             if getattr(self, "handle", -1) >= 0 and _lib is not None:
                 _lib.p3dfft_gb300_batch_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop (p3dfft_gb300_server_*): jobs admitted under an HBM budget as they arrive,
+    run concurrently on `nslots` streams."""
+
+    def __init__(self, hbm_budget_bytes, nslots=8):
+        setup()
+        h = lib().p3dfft_gb300_server_create(int(hbm_budget_bytes), int(nslots))
+        if h < 0:
+            check(-1)
+        self.handle = h
+        self._keep = {}
+
+    def clock(self):
+        return float(lib().p3dfft_gb300_server_clock(self.handle))
+
+    def submit(self, fwd, bwd, inp, out, idir=-1, arrival=-1.0):
+        """Returns the job id.  `arrival` (server-clock seconds) >= 0 replays a trace."""
+        pi, k1 = _ptr(inp)
+        po, k2 = _ptr(out)
+        j = lib().p3dfft_gb300_server_submit(self.handle, fwd.handle, bwd.handle, int(idir), pi, po, float(arrival))
+        if j < 0:
+            check(-1)
+        self._keep[j] = (fwd, bwd, k1, k2)
+        return j
+
+    def wait(self, job, timeout=-1.0):
+        rc = lib().p3dfft_gb300_server_wait(self.handle, int(job), float(timeout))
+        if rc < 0:
+            raise P3DFFTError(f"job {job} failed: {ERR_NAMES.get(-rc, -rc)}")
+        return rc == 0
+
+    def drain(self):
+        rc = lib().p3dfft_gb300_server_drain(self.handle)
+        self._keep.clear()
+        return rc
+
+    def job_times(self, job):
+        t = (ctypes.c_double * 3)()
+        rc = lib().p3dfft_gb300_server_job_times(self.handle, int(job), t)
+        return rc, (t[0], t[1], t[2])
+
+    def stats(self):
+        v = (ctypes.c_double * 6)()
+        lib().p3dfft_gb300_server_stats(self.handle, v, 6)
+        keys = ("completed", "failed", "admitted", "peak_hbm_bytes", "budget_bytes", "max_running")
+        return dict(zip(keys, [v[i] for i in range(6)]))
+
+    def close(self):
+        if getattr(self, "handle", -1) >= 0 and _lib is not None:
+            _lib.p3dfft_gb300_server_destroy(self.handle)
+            self.handle = -1
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
