@@ -61,6 +61,23 @@ int p3dfft_gb300_destroy1d(int plan);
 int p3dfft_gb300_compute_deriv(int prec, const void *in, void *out, const int gdims[3],
                                const int mo[3], int dcs, int idir);
 
+/* ---- autotuner (no counterpart in the reference) ----
+ * For every stage of a plan, times each kernel choice the stage admits (engine: 1 specialised
+ * kernel with a compile-time radix plan and tile shape, 2 register engine, 3 generic mixed-radix
+ * engine; talt: the tile's consecutive lines along the first (0) or second (1) batch dim) and keeps
+ * the fastest.  Choices are cached per stage (kind, precision, FP64 arithmetic, dims, strides), so
+ * plans that share a stage share its tuning.  is1d selects a 1D plan handle.  With set_autotune(1)
+ * every plan is tuned at its first exec.  The cache can be saved and loaded as a text file. */
+void p3dfft_gb300_set_autotune(int on);
+int p3dfft_gb300_autotune(int plan, int is1d);
+/* per stage: engine (0 = heuristic), talt, measured ms; returns the stage count */
+int p3dfft_gb300_plan_tuning(int plan, int is1d, int *engine, int *talt, double *ms, int max_stages);
+/* forces a stage's kernel choice (engine 0 = heuristic) */
+int p3dfft_gb300_plan_set_engine(int plan, int is1d, int stage, int engine, int talt);
+int p3dfft_gb300_tune_cache_save(const char *path);
+int p3dfft_gb300_tune_cache_load(const char *path);
+void p3dfft_gb300_tune_cache_clear(void);
+
 /* ---- allocation-free execution (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc (an application that gives all device memory to its own
  * allocator at start-up, a real-time loop that may not take cudaMalloc's implicit device

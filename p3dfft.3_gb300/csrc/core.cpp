@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -156,12 +157,19 @@ struct Buffers {
     scratch_bytes = stage_in_bytes = stage_out_bytes = 0;
   }
 };
+// Per-stage kernel choice: engine (Engine) and tile-dim flag, 0/0 = heuristic.
+struct StageTune {
+  int engine = 0, talt = 0;
+  float ms = 0.f;  // measured duration when chosen by the autotuner
+};
 struct Plan {
   std::vector<Stage> st;
   int L[3] = {0, 1, 2};
   int dt1 = 1, dt2 = 1, prec = 8;
   GridDesc g1, g2;
   Buffers buf;
+  std::vector<StageTune> tune;  // empty: heuristic for every stage
+  int tuned_arith = -1;         // FP64 arithmetic the tuning was made for
   bool live = true;
 };
 
@@ -505,6 +513,12 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
   strides(s.g1, d.s1);
   strides(s.g2, d.s2);
   d.deriv = deriv ? 1 : 0;
+  const size_t idx = (size_t)(&s - P->st.data());
+  d.engine = d.talt = 0;
+  if (P->tune.size() == P->st.size() && (P->prec == 4 || P->tuned_arith == arith_mode())) {
+    d.engine = P->tune[idx].engine;
+    d.talt = P->tune[idx].talt;
+  }
 }
 
 static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv,
@@ -545,7 +559,115 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
   return rc;
 }
 
+// ------------------------------------------------------------------------------------------
+// Autotuner.  For every stage of a plan it times each kernel choice the stage admits — the
+// specialised kernel (compile-time radix plan and tile shape), the register engine (power-of-two
+// lengths, tile lines chosen at run time), the generic mixed-radix engine — each with the tile's
+// consecutive lines taken along either batch dim, and keeps the fastest.  Choices are cached by
+// stage (transform kind, precision, FP64 arithmetic, dims and strides in and out), so a plan's key
+// (grid, transform types, dtype) decomposes into its stages' keys and plans sharing a stage share
+// its tuning; the cache can be saved to and loaded from a text file.
+static std::mutex g_tmu;
+static std::map<std::string, StageTune> g_tune_cache;
+static bool g_autotune = false;
+
+static std::string stage_key(const StageDesc &d, int arith) {
+  char b[400];
+  snprintf(b, sizeof b, "%d %d %d %d %d %d %d %d %d %d %d %d %d %lld %lld %lld %lld %lld %lld", d.kind, d.r2r, d.prec,
+           d.prec == 8 ? arith : 0, d.dt1, d.dt2, d.L, d.d1[0], d.d1[1], d.d1[2], d.d2[0], d.d2[1], d.d2[2], d.s1[0],
+           d.s1[1], d.s1[2], d.s2[0], d.s2[1], d.s2[2]);
+  return b;
+}
+
+static int autotune_plan(Plan *P) {
+  if (!ensure_device()) return t_err;
+  const int n = (int)P->st.size();
+  const int arith = arith_mode();
+  const int ar = P->prec == 8 ? arith : AR_NATIVE;
+  std::vector<StageTune> tune(n);
+  size_t maxb = 0;
+  for (auto &s : P->st) {
+    const TypeInfo &t = g_types[s.type];
+    maxb = std::max(maxb, std::max((size_t)elems(s.g1) * t.dt1, (size_t)elems(s.g2) * t.dt2) * P->prec);
+  }
+  void *bi = nullptr, *bo = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = E_OK;
+  P->tune.clear();  // fill_stage_desc below must see the heuristic
+  for (int si = 0; si < n && rc == E_OK; si++) {
+    const Stage &s = P->st[si];
+    if (g_types[s.type].kind == K_EMPTY) continue;
+    StageDesc d;
+    fill_stage_desc(P, s, false, d);
+    const std::string key = stage_key(d, arith);
+    {
+      std::lock_guard<std::mutex> g(g_tmu);
+      auto it = g_tune_cache.find(key);
+      if (it != g_tune_cache.end()) {
+        tune[si] = it->second;
+        continue;
+      }
+    }
+    if (!bi) {
+      if (cudaMalloc(&bi, maxb) != cudaSuccess || cudaMalloc(&bo, maxb) != cudaSuccess ||
+          cudaMemset(bi, 0, maxb) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+          cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        set_err(E_CUDA, "autotune: buffer allocation failed");
+        rc = E_CUDA;
+        break;
+      }
+    }
+    StageTune best;
+    best.ms = 1e30f;
+    for (int e : {ENG_FAST, ENG_FIXED, ENG_GENERIC}) {
+      for (int ta = 0; ta < 2; ta++) {
+        d.engine = e;
+        d.talt = ta;
+        if (launch_stage(d, bi, bo, ar, g_stream, g_tabs, nullptr) != E_OK) {  // not admissible
+          cudaGetLastError();
+          continue;
+        }
+        // repeat until ~0.3 ms of work is timed (at least 3, at most 50 launches)
+        float ms = 0.f;
+        int reps = 3;
+        for (int round = 0; round < 2; round++) {
+          cudaEventRecord(e0, g_stream);
+          for (int r = 0; r < reps; r++) launch_stage(d, bi, bo, ar, g_stream, g_tabs, nullptr);
+          cudaEventRecord(e1, g_stream);
+          cudaEventSynchronize(e1);
+          cudaEventElapsedTime(&ms, e0, e1);
+          ms /= reps;
+          if (round == 0 && ms > 0.f) reps = std::max(3, std::min(50, (int)(0.3f / ms)));
+        }
+        if (ms < best.ms) {
+          best.engine = e;
+          best.talt = ta;
+          best.ms = ms;
+        }
+      }
+    }
+    if (best.ms >= 1e30f) best = StageTune();  // nothing ran: keep the heuristic
+    tune[si] = best;
+    std::lock_guard<std::mutex> g(g_tmu);
+    g_tune_cache[key] = best;
+  }
+  if (bi) cudaFree(bi);
+  if (bo) cudaFree(bo);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc != E_OK) return rc;
+  P->tune = tune;
+  P->tuned_arith = arith;
+  return E_OK;
+}
+
 static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaEvent_t *stage_ev = nullptr) {
+  if (g_autotune && !in_capture() && (P->tune.empty() || (P->prec == 8 && P->tuned_arith != arith_mode()))) {
+    if (!ensure_device()) return t_err;
+    int rc = autotune_plan(P);
+    if (rc != E_OK) return rc;
+  }
   if (!ensure_device()) return t_err;
   if (!in || !out) {
     set_err(E_BAD_ARG, "null data pointer");
@@ -889,6 +1011,90 @@ int p3dfft_gb300_exec3d(int plan, const void *in, void *out, int idir, int OW) {
     return E_BAD_ARG;
   }
   return exec_plan(P, in, out, idir, OW);
+}
+
+// ---- autotuner ----
+void p3dfft_gb300_set_autotune(int on) { g_autotune = on != 0; }
+
+static Plan *plan_of(int plan, int is1d) { return get_plan(is1d ? g_plans1 : g_plans3, plan); }
+
+int p3dfft_gb300_autotune(int plan, int is1d) {
+  Plan *P = plan_of(plan, is1d);
+  if (!P) {
+    set_err(E_BAD_ARG, "invalid plan handle %d", plan);
+    return E_BAD_ARG;
+  }
+  return autotune_plan(P);
+}
+
+int p3dfft_gb300_plan_tuning(int plan, int is1d, int *engine, int *talt, double *ms, int max_stages) {
+  Plan *P = plan_of(plan, is1d);
+  if (!P) return -1;
+  const int n = (int)P->st.size();
+  for (int s = 0; s < n && s < max_stages; s++) {
+    const bool t = P->tune.size() == P->st.size();
+    if (engine) engine[s] = t ? P->tune[s].engine : 0;
+    if (talt) talt[s] = t ? P->tune[s].talt : 0;
+    if (ms) ms[s] = t ? P->tune[s].ms : 0.0;
+  }
+  return n;
+}
+
+int p3dfft_gb300_plan_set_engine(int plan, int is1d, int stage, int engine, int talt) {
+  Plan *P = plan_of(plan, is1d);
+  if (!P || stage < 0 || stage >= (int)P->st.size() || engine < 0 || engine > ENG_GENERIC) {
+    set_err(E_BAD_ARG, "invalid plan, stage or engine");
+    return E_BAD_ARG;
+  }
+  if (P->tune.size() != P->st.size()) P->tune.assign(P->st.size(), StageTune());
+  P->tune[stage].engine = engine;
+  P->tune[stage].talt = talt ? 1 : 0;
+  P->tuned_arith = arith_mode();
+  return E_OK;
+}
+
+int p3dfft_gb300_tune_cache_save(const char *path) {
+  FILE *f = path ? fopen(path, "w") : nullptr;
+  if (!f) {
+    set_err(E_BAD_ARG, "cannot write tuning cache %s", path ? path : "(null)");
+    return E_BAD_ARG;
+  }
+  std::lock_guard<std::mutex> g(g_tmu);
+  fprintf(f, "# p3dfft_gb300 tuning cache: stage key | engine talt ms\n");
+  for (auto &kv : g_tune_cache) fprintf(f, "%s | %d %d %.9g\n", kv.first.c_str(), kv.second.engine, kv.second.talt, (double)kv.second.ms);
+  fclose(f);
+  return E_OK;
+}
+
+// returns the number of entries read, or -1
+int p3dfft_gb300_tune_cache_load(const char *path) {
+  FILE *f = path ? fopen(path, "r") : nullptr;
+  if (!f) {
+    set_err(E_BAD_ARG, "cannot read tuning cache %s", path ? path : "(null)");
+    return -1;
+  }
+  char line[512];
+  int n = 0;
+  std::lock_guard<std::mutex> g(g_tmu);
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == '#') continue;
+    char *bar = strchr(line, '|');
+    if (!bar) continue;
+    *bar = 0;
+    std::string key(line);
+    while (!key.empty() && key.back() == ' ') key.pop_back();
+    StageTune t;
+    if (sscanf(bar + 1, "%d %d %f", &t.engine, &t.talt, &t.ms) != 3 || t.engine < 0 || t.engine > ENG_GENERIC) continue;
+    g_tune_cache[key] = t;
+    n++;
+  }
+  fclose(f);
+  return n;
+}
+
+void p3dfft_gb300_tune_cache_clear(void) {
+  std::lock_guard<std::mutex> g(g_tmu);
+  g_tune_cache.clear();
 }
 
 int p3dfft_gb300_destroy3d(int plan) {

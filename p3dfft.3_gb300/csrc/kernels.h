@@ -40,7 +40,12 @@ struct StageDesc {
   int d1[3], d2[3];
   long long s1[3], s2[3];
   int deriv;      // fuse the i*k multiply (compute_deriv_loc)
+  // tuning (0 = heuristic): engine 1 specialised kernel, 2 register engine, 3 generic engine;
+  // talt 1 takes consecutive lines of a tile along the other batch dim
+  int engine = 0;
+  int talt = 0;
 };
+enum Engine { ENG_AUTO = 0, ENG_FAST = 1, ENG_FIXED = 2, ENG_GENERIC = 3 };
 
 struct DeviceTables;  // twiddle-table cache, one per device
 

@@ -729,15 +729,10 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   // tile selection: t = batch dim along which consecutive lines are taken
   p.iL = d.s1[L];
   p.oL = d.s2[L];
-  int t, o;
-  if (d.s1[L] == 1) {
-    t = d.s1[a] <= d.s1[b] ? a : b;
-    p.load_Lmajor = 1;
-  } else {
-    t = d.s1[a] <= d.s1[b] ? a : b;
-    p.load_Lmajor = 0;
-  }
-  o = (t == a) ? b : a;
+  int t = d.s1[a] <= d.s1[b] ? a : b;  // the batch dim with the smaller input stride
+  if (d.talt) t = (t == a) ? b : a;
+  const int o = (t == a) ? b : a;
+  p.load_Lmajor = d.s1[L] == 1 ? 1 : 0;
   p.store_Lmajor = (d.s2[L] == 1) ? 1 : ((d.s2[t] == 1) ? 0 : 1);
   p.it = d.s1[t];
   p.io = d.s1[o];
@@ -754,7 +749,11 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   // specialised kernels for C2C / even R2C / even C2R at power-of-two lengths
   const bool even = (p.nlog % 2) == 0;
   const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even);
-  if (fast_kind && fast_supported(p.nfft) && aligned && !getenv("P3DFFT_GB300_GENERIC_ONLY")) {
+  const bool generic_only = getenv("P3DFFT_GB300_GENERIC_ONLY") != nullptr;
+  const bool fast_ok = fast_kind && fast_supported(p.nfft) && aligned;
+  if (d.engine == ENG_FAST && !fast_ok) return E_UNSUPPORTED;
+  if (d.engine == ENG_FIXED && !fixed_engine_len(p.nfft)) return E_UNSUPPORTED;
+  if (fast_ok && (d.engine == ENG_FAST || (d.engine == ENG_AUTO && !generic_only))) {
     FastArgs fa;
     fa.kind = (d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C);
     fa.n = p.nfft;
@@ -787,7 +786,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   }
 
   const size_t csz = (d.prec == 4) ? 8 : 16;
-  const bool fixed = fixed_engine_len(p.nfft) && !getenv("P3DFFT_GB300_GENERIC_ONLY");
+  const bool fixed = fixed_engine_len(p.nfft) && (d.engine == ENG_FIXED || (d.engine == ENG_AUTO && !generic_only));
   int slots = p.nfft;
   if (p.nin > slots) slots = p.nin;
   if (p.nout > slots) slots = p.nout;

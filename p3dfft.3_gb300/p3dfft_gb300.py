@@ -93,6 +93,14 @@ def lib():
         "p3dfft_gb300_batch_destroy": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_server_create": ([ctypes.c_longlong, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_preload_kernels": ([], ctypes.c_int),
+        "p3dfft_gb300_set_autotune": ([ctypes.c_int], None),
+        "p3dfft_gb300_autotune": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_plan_tuning": ([ctypes.c_int, ctypes.c_int, ip, ip, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_plan_set_engine": ([ctypes.c_int] * 5, ctypes.c_int),
+        "p3dfft_gb300_tune_cache_save": ([ctypes.c_char_p], ctypes.c_int),
+        "p3dfft_gb300_tune_cache_load": ([ctypes.c_char_p], ctypes.c_int),
+        "p3dfft_gb300_tune_cache_clear": ([], None),
         "p3dfft_gb300_server_submit": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp,
                                         ctypes.c_double], ctypes.c_int),
         "p3dfft_gb300_server_wait": ([ctypes.c_int, ctypes.c_int, ctypes.c_double], ctypes.c_int),
@@ -218,6 +226,21 @@ class Transform3D:
     def exec_deriv(self, inp, out=None, idir=0, OW=False):
         return self.exec(inp, out, OW=OW, idir=idir)
 
+    _is1d = 0
+
+    def autotune(self):
+        check(lib().p3dfft_gb300_autotune(self.handle, self._is1d))
+        return self.tuning()
+
+    def tuning(self):
+        """[(engine, talt, ms)] per stage; engine 0 = heuristic, 1 specialised, 2 register, 3 generic."""
+        e, t, m = (ctypes.c_int * 8)(), (ctypes.c_int * 8)(), (ctypes.c_double * 8)()
+        n = lib().p3dfft_gb300_plan_tuning(self.handle, self._is1d, e, t, m, 8)
+        return [(e[i], t[i], m[i]) for i in range(n)]
+
+    def set_engine(self, stage, engine, talt=0):
+        check(lib().p3dfft_gb300_plan_set_engine(self.handle, self._is1d, int(stage), int(engine), int(talt)))
+
     def __del__(self):
         try:
             if getattr(self, "handle", -1) >= 0 and _lib is not None:
@@ -246,6 +269,11 @@ class TransPlan:
         po, _k2 = _ptr(out)
         check(lib().p3dfft_gb300_exec1d(self.handle, pi, po, 1 if OW else 0))
         return out
+
+    _is1d = 1
+    autotune = Transform3D.autotune
+    tuning = Transform3D.tuning
+    set_engine = Transform3D.set_engine
 
     def __del__(self):
         try:
@@ -417,3 +445,22 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def set_autotune(on: bool):
+    lib().p3dfft_gb300_set_autotune(1 if on else 0)
+
+
+def tune_cache_save(path):
+    check(lib().p3dfft_gb300_tune_cache_save(os.fsencode(path)))
+
+
+def tune_cache_load(path):
+    n = lib().p3dfft_gb300_tune_cache_load(os.fsencode(path))
+    if n < 0:
+        check(-1)
+    return n
+
+
+def tune_cache_clear():
+    lib().p3dfft_gb300_tune_cache_clear()

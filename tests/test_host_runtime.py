@@ -1,0 +1,52 @@
+"""CPU: host-side runtime pieces that need no GPU — the tuning-cache file format, and the batch,
+serving and tuning entry points failing loudly (not silently computing on the CPU) without a
+device."""
+import ctypes
+
+import pytest
+
+
+def test_tune_cache_file_round_trip(p3d, tmp_path):
+    L = p3d.lib()
+    src = tmp_path / "in.txt"
+    src.write_text("# comment\n"
+                   "3 0 8 1 2 2 0 64 48 40 64 48 40 1 64 3072 1 64 3072 | 1 0 0.012500\n"
+                   "1 0 4 0 1 2 0 64 48 40 33 48 40 1 64 3072 1 33 1584 | 3 1 0.250000\n"
+                   "malformed line without separator\n"
+                   "1 0 4 0 1 2 0 8 8 8 5 8 8 1 8 64 1 5 40 | 9 0 1.0\n")
+    p3d.tune_cache_clear()
+    assert p3d.tune_cache_load(str(src)) == 2  # engine 9 is rejected
+    out = tmp_path / "out.txt"
+    p3d.tune_cache_save(str(out))
+    rows = {}
+    for line in out.read_text().splitlines():
+        if not line.startswith("#"):
+            key, val = line.split(" | ")
+            e, t, ms = val.split()
+            rows[key] = (int(e), int(t), float(ms))
+    assert set(rows) == {"3 0 8 1 2 2 0 64 48 40 64 48 40 1 64 3072 1 64 3072",
+                         "1 0 4 0 1 2 0 64 48 40 33 48 40 1 64 3072 1 33 1584"}
+    assert rows["3 0 8 1 2 2 0 64 48 40 64 48 40 1 64 3072 1 64 3072"][:2] == (1, 0)
+    assert abs(rows["1 0 4 0 1 2 0 64 48 40 33 48 40 1 64 3072 1 33 1584"][2] - 0.25) < 1e-7
+    p3d.tune_cache_clear()
+    with pytest.raises(p3d.P3DFFTError):
+        p3d.tune_cache_load(str(tmp_path / "missing.txt"))
+
+
+def test_runtimes_fail_loudly_without_device(p3d):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = p3d.lib()
+    assert L.p3dfft_gb300_server_create(1 << 30, 4) == -1
+    assert "device" in L.p3dfft_last_error_string().decode().lower()
+    L.p3dfft_clear_error()
+    b = L.p3dfft_gb300_batch_create(2)
+    assert b >= 0
+    assert L.p3dfft_gb300_batch_exec(b) in (0, 4)  # empty batch: nothing to run
+    f = p3d.Transform3D([p3d.R2CFFT_D, p3d.CFFT_FORWARD_D, p3d.CFFT_FORWARD_D], (8, 8, 8), (0, 1, 2), (5, 8, 8),
+                        (1, 2, 0), -1, 0)
+    assert L.p3dfft_gb300_autotune(f.handle, 0) == 4  # P3DFFT_ERR_NO_DEVICE
+    assert L.p3dfft_gb300_preload_kernels() == 4
+    L.p3dfft_clear_error()
+    L.p3dfft_gb300_batch_destroy(b)
