@@ -479,6 +479,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload summary")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream summary")
     ap.add_argument("--serve-jobs", type=int, default=10000)
+    ap.add_argument("--kernels-only", choices=["fp64", "fp32"], default=None,
+                    help="run only the device-resident round trip of that form (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -492,6 +494,33 @@ def main():
         res = batch_workload(p3d, p3d.lib(), args.steps, args.warmup)
         if rank == 0:
             print(json.dumps({"workload": "batched uneven round trips", **res}), flush=True)
+        return
+    if args.kernels_only:
+        import ctypes
+        import p3dfft_gb300 as p3d
+        import build_lib
+        build_lib.build()
+        L = p3d.lib()
+        p3d.set_fp64_arith(0 if args.arith == "native" else 1)
+        prec = 8 if args.kernels_only == "fp64" else 4
+        ft, bt = (FWD, BWD) if prec == 8 else (tuple(t - 1 for t in FWD), tuple(t - 1 for t in BWD))
+        f = p3d.Transform3D(ft, GD, MO1, GD2, MO2, -1, 0)
+        b = p3d.Transform3D(bt, GD2, MO2, GD, MO1, 0, -1)
+        d_in, d_spec, d_out = p3d.DeviceArray(S_R * prec // 8), p3d.DeviceArray(S_C * prec // 8), p3d.DeviceArray(S_R * prec // 8)
+        x = np.random.default_rng(512).uniform(-1.0, 1.0, p3d.storage_shape(GD, MO1))
+        d_in.upload(x.astype(np.float64 if prec == 8 else np.float32))
+        p3d.set_sync(False)
+        vp = ctypes.c_void_p
+        for k in range(args.warmup + args.steps):
+            if k == args.warmup:
+                L.p3dfft_gb300_synchronize()
+                L.p3dfft_gb300_event_record(0)
+            p3d.check(L.p3dfft_gb300_exec3d(f.handle, vp(d_in.ptr), vp(d_spec.ptr), IDIR, 0))
+            p3d.check(L.p3dfft_gb300_exec3d(b.handle, vp(d_spec.ptr), vp(d_out.ptr), -1, 0))
+        L.p3dfft_gb300_event_record(1)
+        ms = L.p3dfft_gb300_event_elapsed_ms(0, 1) / max(1, args.steps)
+        print(json.dumps({"kernels_only": args.kernels_only, "grid": list(GD), "ms_per_round_trip": ms,
+                          "GB_per_s": ALG_BYTES * prec // 8 / (ms * 1e-3) / 1e9}), flush=True)
         return
     if args.workload == "serve":
         import p3dfft_gb300 as p3d

@@ -101,14 +101,57 @@ struct FastShape {
   static constexpr int USED = TB * T;               // threads with a line
   static constexpr int BLOCK = (USED + 31) / 32 * 32;
   static constexpr int MINB = fast_max_values(N) > 8 ? 3 : FAST_MIN_BLOCKS;
-  // Padded line stride (complex slots, > N + N/8 so slot N fits): chosen so that the TB lines of
-  // a t-major access (consecutive threads on consecutive lines) fall in distinct 16-byte bank
-  // groups, LS = 8/TB mod 8 (odd when TB >= 8).
-  static constexpr int BASE = N + N / 8;
-  static constexpr int TGT = TB >= 8 ? 1 : 8 / TB;
-  static constexpr int ADJ = ((TGT - BASE % 8) % 8 + 8) % 8;
-  static constexpr int LS = BASE + (ADJ == 0 ? 8 : ADJ);
 };
+
+// Padding of a line in shared memory: one slot after every 2^PS data slots, PS = 3 for 16-byte
+// complex elements and 4 for 8-byte ones, i.e. one slot per 128 bytes of line data.
+template <int ESZ>
+__host__ __device__ constexpr int fast_pad_shift() {
+  return ESZ >= 16 ? 3 : 4;
+}
+
+// Bank-conflict cost of a shared-memory line stride LS (complex slots of ESZ bytes): a warp's
+// accesses are served 128 bytes at a time, i.e. by groups of U = 128/ESZ threads whose slots should
+// fall in distinct ESZ-byte bank groups (slot mod U).  Summed over the block, for both thread
+// mappings of the kernel (consecutive threads along a line, and across the TB lines).
+template <int N>
+__host__ __device__ constexpr int fast_ls_cost(int LS, int ESZ) {
+  using SH = FastShape<N>;
+  const int U = 128 / ESZ;
+  int cost = 0;
+  for (int map = 0; map < 2; map++) {
+    for (int g0 = 0; g0 < SH::USED; g0 += U) {
+      int cnt[32] = {0};
+      int worst = 0;
+      for (int t = g0; t < g0 + U && t < SH::USED; t++) {
+        const int l = map ? t % SH::TB : t / SH::T;
+        const int j = map ? t / SH::TB : t % SH::T;
+        const int slot = l * LS + j + (j >> (ESZ >= 16 ? 3 : 4));
+        const int c = ++cnt[slot % U];
+        worst = c > worst ? c : worst;
+      }
+      cost += worst;
+    }
+  }
+  return cost;
+}
+
+// Padded line stride: more than the padded slot of N (which C2R uses), the cheapest under
+// fast_ls_cost among the next 128/ESZ candidates.
+template <int N, int ESZ>
+__host__ __device__ constexpr int fast_ls() {
+  const int base = N + (N >> fast_pad_shift<ESZ>()) + 1;
+  const int U = 128 / ESZ;
+  int best = base, best_cost = 1 << 30;
+  for (int ls = base; ls < base + U; ls++) {
+    const int c = fast_ls_cost<N>(ls, ESZ);
+    if (c < best_cost) {
+      best_cost = c;
+      best = ls;
+    }
+  }
+  return best;
+}
 
 // Twiddles are read through the read-only data cache (the table is a few KB and stays L1
 // resident across the CTAs of an SM); a shared-memory copy per CTA was measured to cost more
@@ -125,6 +168,7 @@ __device__ __forceinline__ typename O::C fk_tw(const typename O::T *tab, int m, 
 template <class O, int N, int TWSTEP, int Ns, int I>
 __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T *tab, int j, bool active, int sign) {
   using C = typename O::C;
+  constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   constexpr RadixList RL = fast_radices(N);
   constexpr int R = RL.r[I];
   constexpr int T = FastShape<N>::T, M = N / R;
@@ -140,7 +184,7 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       const int jj = j + b * T;
       if (GUARD && jj >= M) break;
 #pragma unroll
-      for (int r = 0; r < R; r++) v[b * R + r] = line[pad<3>(jj + r * M)];
+      for (int r = 0; r < R; r++) v[b * R + r] = line[pad<PS>(jj + r * M)];
       if (Ns > 1) {
         const int k = jj % Ns;
 #pragma unroll
@@ -161,11 +205,23 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       const int k = jj % Ns;
       const int base = (jj - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; r++) line[pad<3>(base + r * Ns)] = O::norm(v[b * R + r]);
+      for (int r = 0; r < R; r++) line[pad<PS>(base + r * Ns)] = O::norm(v[b * R + r]);
     }
   }
   __syncthreads();
   if constexpr (I + 1 < RL.n) fk_pass<O, N, TWSTEP, Ns * R, I + 1>(line, tab, j, active, sign);
+}
+
+// f(e) for e = 0 .. V-1, U iterations unrolled per step of the outer loop
+template <int V, int U, class F>
+__device__ __forceinline__ void fk_for(F &&f) {
+  constexpr int UU = U < 1 ? 1 : (U > V ? V : U);
+#pragma unroll 1
+  for (int e0 = 0; e0 < V; e0 += UU) {
+#pragma unroll
+    for (int u = 0; u < UU; u++)
+      if (V % UU == 0 || e0 + u < V) f(e0 + u);
+  }
 }
 
 template <class O>
@@ -183,7 +239,8 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
   using RAW = typename O::RAW;
   using SH = FastShape<N>;
   constexpr int TWSTEP = (KIND == FK_C2C) ? 1 : 2;  // FFT twiddle W_N^m = tab[m * TWSTEP]
-  constexpr int LS = SH::LS, TB = SH::TB, TT = SH::T, V = SH::V;
+  constexpr int LS = fast_ls<N, (int)sizeof(C)>(), TB = SH::TB, TT = SH::T, V = SH::V;
+  constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf = reinterpret_cast<C *>(smem_raw);
   __shared__ int red[32];
@@ -227,8 +284,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
     int emax = 0;
     if (act) {
       const G *src = gin + (KIND == FK_R2C ? ibase : 2 * ibase);
-#pragma unroll 2
-      for (int e = 0; e < V; e++) {
+      fk_for<V, O::IO_UNROLL>([&](int e) {
         const int j = j0 + e * TT;
         RAW r;
         if (KIND == FK_R2C) {  // packed z[j] = x[2j] + i x[2j+1]
@@ -239,18 +295,18 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
         }
         if (O::SCALED) {
           emax = max(emax, O::rexp(r));
-          lr[pad<3>(j)] = r;
+          lr[pad<PS>(j)] = r;
         } else {
-          lb[pad<3>(j)] = O::from_raw(r, 0);
+          lb[pad<PS>(j)] = O::from_raw(r, 0);
         }
-      }
+      });
       if (KIND == FK_C2R && j0 == 0) {
         RAW r = O::ldraw(src + 2 * (long long)N * p.iL);
         if (O::SCALED) {
           emax = max(emax, O::rexp(r));
-          lr[pad<3>(N)] = r;
+          lr[pad<PS>(N)] = r;
         } else {
-          lb[pad<3>(N)] = O::from_raw(r, 0);
+          lb[pad<PS>(N)] = O::from_raw(r, 0);
         }
       }
     }
@@ -265,11 +321,10 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
       for (int w = 0; w < SH::BLOCK / 32; w++) emax = max(emax, red[w]);
       sc = 1043 - emax;
       if (act && KIND != FK_C2R) {
-#pragma unroll 2
-        for (int e = 0; e < V; e++) {
-          const int j = pad<3>(j0 + e * TT);
+        fk_for<V, O::IO_UNROLL>([&](int e) {
+          const int j = pad<PS>(j0 + e * TT);
           lb[j] = O::from_raw(lr[j], sc);
-        }
+        });
       }
     }
     if (KIND == FK_C2R) {
@@ -282,11 +337,11 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
           const int k = j0 + e * TT;
           C a, b;
           if (O::SCALED) {
-            a = O::from_raw(lr[pad<3>(k)], sc);
-            b = O::from_raw(lr[pad<3>(N - k)], sc);
+            a = O::from_raw(lr[pad<PS>(k)], sc);
+            b = O::from_raw(lr[pad<PS>(N - k)], sc);
           } else {
-            a = lb[pad<3>(k)];
-            b = lb[pad<3>(N - k)];
+            a = lb[pad<PS>(k)];
+            b = lb[pad<PS>(N - k)];
           }
           if (k == 0) {
             a.y = O::rzero();
@@ -301,7 +356,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
       __syncthreads();
       if (act) {
 #pragma unroll
-        for (int e = 0; e < V; e++) lb[pad<3>(j0 + e * TT)] = z[e];
+        for (int e = 0; e < V; e++) lb[pad<PS>(j0 + e * TT)] = z[e];
       }
     }
     __syncthreads();
@@ -315,28 +370,27 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
     if (sact) {
       const C *Y = buf + (size_t)ls * LS;
       const long long obase = (long long)(gs % p.dt) * p.ot + (long long)(gs / p.dt) * p.oo;
-#pragma unroll 2
-      for (int e = 0; e < V; e++) {
+      fk_for<V, O::IO_UNROLL>([&](int e) {
         const int k = js + e * TT;
         if (KIND == FK_C2C) {
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[pad<3>(k)], k), sc));
+          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[pad<PS>(k)], k), sc));
         } else if (KIND == FK_R2C) {
           // X[k] = 1/2 [(Z_k + conj Z_{N-k}) - i W_2N^k (Z_k - conj Z_{N-k})]
-          C a = Y[pad<3>(k)], b = O::conj(Y[pad<3>(k == 0 ? 0 : N - k)]);
+          C a = Y[pad<PS>(k)], b = O::conj(Y[pad<PS>(k == 0 ? 0 : N - k)]);
           C s = O::add(a, b), d = O::sub(a, b);
           C x = O::half(O::sub(s, O::muli(O::mul(O::tw(tab, k), d))));
           O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc));
           if (k == 0) {  // X[N] = Re Z_0 - Im Z_0
-            C z0 = Y[pad<3>(0)];
+            C z0 = Y[pad<PS>(0)];
             C xn = O::mk(O::norm(O::sub(O::mk(z0.x, O::rzero()), O::mk(z0.y, O::rzero()))).x, O::rzero());
             O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc));
           }
         } else {  // C2R: reals 2k, 2k+1 = z[k]
-          RAW r = O::to_raw(Y[pad<3>(k)], sc);
+          RAW r = O::to_raw(Y[pad<PS>(k)], sc);
           if (p.oL == 1) O::straw(gout + obase + 2 * k, r);
           else O::straw2(gout + obase + (long long)(2 * k) * p.oL, gout + obase + (long long)(2 * k + 1) * p.oL, r);
         }
-      }
+      });
     }
     __syncthreads();
   }
@@ -352,7 +406,7 @@ struct FastArgs {
 
 template <class O, int KIND, int N>
 constexpr size_t fk_smem() {
-  return sizeof(typename O::C) * (size_t)FastShape<N>::TB * FastShape<N>::LS;
+  return sizeof(typename O::C) * (size_t)FastShape<N>::TB * fast_ls<N, (int)sizeof(typename O::C)>();
 }
 
 // Sets the kernel's dynamic shared-memory limit once; this also loads the kernel's module (which

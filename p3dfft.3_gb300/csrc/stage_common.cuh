@@ -11,6 +11,16 @@
 
 namespace p3d {
 
+// Loads / stores per thread that the specialised kernels keep in flight together (loop unroll
+// of their global-memory I/O): all of them for the native types; fewer for float-float, whose
+// raw values are wide and whose kernels are bound by instruction issue rather than latency.
+#ifndef FAST_IO_UNROLL_NATIVE
+#define FAST_IO_UNROLL_NATIVE 8
+#endif
+#ifndef FAST_IO_UNROLL_DF
+#define FAST_IO_UNROLL_DF 4
+#endif
+
 // ------------------------------------------------------------------------------------------
 // Arithmetic policies
 template <class R>
@@ -81,6 +91,7 @@ struct Native {
   static __device__ __forceinline__ C tws(const T *t, int k) { return t[k]; }
   // register-level I/O of the specialised kernels (no tile scaling for native arithmetic)
   static constexpr bool SCALED = false;
+  static constexpr int IO_UNROLL = FAST_IO_UNROLL_NATIVE;
   using RAW = cx<R>;
   static __device__ __forceinline__ RAW ldraw(const G *p) { return ldg_c(reinterpret_cast<const cx<R> *>(p)); }
   static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
@@ -152,6 +163,7 @@ struct DF {
   }
   // register-level I/O of the specialised kernels: raw IEEE bits, tile scaled by 2^sc
   static constexpr bool SCALED = true;
+  static constexpr int IO_UNROLL = FAST_IO_UNROLL_DF;
   using RAW = longlong2;
   static __device__ __forceinline__ RAW ldraw(const G *p) { return __ldg(reinterpret_cast<const longlong2 *>(p)); }
   static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
