@@ -836,14 +836,15 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
     if (g_types[st.type].kind == K_EMPTY) continue;
     StageDesc d;
     fill_stage_desc(P, st, false, d);
-    TableNeed need{0, 0, 0};
+    TableNeed need{0, 0, 0, 0};
     int rc = launch_stage(d, nullptr, nullptr, P->prec == 8 ? arith_mode() : AR_NATIVE, cur_stream(), nullptr, nullptr,
                           nullptr, nullptr, &need);
     if (rc != E_OK) {
       set_err(rc, "stage %d cannot run (transform length unsupported)", s);
       return rc;
     }
-    size_t b1 = table_bytes(need.tabN, need.fmt), b2 = need.auxN ? table_bytes(need.auxN, need.fmt) : 0;
+    size_t b1 = table_bytes(need.tabN, need.fmt);
+    size_t b2 = need.auxN ? (need.aux_pass ? pass_table_bytes(need.auxN, need.fmt) : table_bytes(need.auxN, need.fmt)) : 0;
     if (off + b1 + b2 > tw_bytes) {
       set_err(E_TOO_LARGE, "twiddle tables exceed the %zu-byte static table region", tw_bytes);
       return E_TOO_LARGE;
@@ -852,7 +853,8 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
     tw[s] = static_cast<unsigned char *>(tw_dev) + off;
     off += (b1 + 255) & ~(size_t)255;
     if (b2) {
-      fill_table(need.auxN, need.fmt, host + off);
+      if (need.aux_pass) fill_pass_table(need.auxN, need.fmt, host + off);
+      else fill_table(need.auxN, need.fmt, host + off);
       aux[s] = static_cast<unsigned char *>(tw_dev) + off;
       off += (b2 + 255) & ~(size_t)255;
     }

@@ -28,7 +28,8 @@ enum FastKind { FK_C2C = 0, FK_R2C = 1, FK_C2R = 2 };
 struct FParams {
   const void *in;
   void *out;
-  const void *tw;  // W_{tabN}^m, tabN = N (C2C) or 2N (R2C / C2R), m < tabN
+  const void *tw;   // W_{tabN}^m, tabN = N (C2C) or 2N (R2C / C2R), m < tabN
+  const void *ptw;  // per-pass twiddle rows (fast_pass_offset)
   long long iL, it, io, oL, ot, oo;  // element strides
   int dt;                            // size of the tile dim; line g is (g % dt, g / dt)
   int nlines, ntotal;                // lines in total, CTAs
@@ -37,9 +38,13 @@ struct FParams {
   int load_Lmajor, store_Lmajor;
 };
 
-// resident 256-thread CTAs per SM the register allocation is sized for
+// resident 256-thread CTAs per SM the register allocation is sized for (FP64 and float-float;
+// FP32 kernels, with half-width values, can afford more resident CTAs)
 #ifndef FAST_MIN_BLOCKS
 #define FAST_MIN_BLOCKS 4
+#endif
+#ifndef FAST_MIN_BLOCKS_FP32
+#define FAST_MIN_BLOCKS_FP32 8
 #endif
 
 // The FFT lengths with a specialised kernel.
@@ -153,7 +158,29 @@ __host__ __device__ constexpr int fast_ls() {
   return best;
 }
 
-// Twiddles are read through the read-only data cache (the table is a few KB and stays L1
+// 1: twiddles of the Stockham passes from the per-pass tables below; 0: from the length-N table
+#ifndef FAST_PASS_TABLES
+#define FAST_PASS_TABLES 1
+#endif
+
+// Per-pass twiddle tables.  Pass I >= 1 of the radix plan (radix R, Ns = product of the earlier
+// radices) multiplies by W_{Ns R}^{r k}, r = 1 .. R-1, for its k = jj mod Ns.  They are stored per
+// pass as R-1 rows of Ns entries, row r-1 holding W_{Ns R}^{r k} at entry k: the threads of a warp
+// (consecutive jj, hence consecutive k) read consecutive entries for each r, so every twiddle load
+// of a pass is coalesced.  Pass I starts at fast_pass_offset(N, I) entries.
+__host__ __device__ constexpr int fast_pass_offset(int N, int I) {
+  const RadixList L = fast_radices(N);
+  int off = 0, ns = L.n > 0 ? L.r[0] : 1;
+  for (int j = 1; j < I && j < L.n; j++) {
+    off += ns * (L.r[j] - 1);
+    ns *= L.r[j];
+  }
+  return off;
+}
+// total entries of the per-pass tables of length N
+__host__ __device__ constexpr int fast_pass_entries(int N) { return fast_pass_offset(N, 32); }
+
+// Twiddles are read through the read-only data cache (the tables are a few KB and stay L1
 // resident across the CTAs of an SM); a shared-memory copy per CTA was measured to cost more
 // registers and L2 traffic than it saves.
 template <class O>
@@ -166,7 +193,8 @@ __device__ __forceinline__ typename O::C fk_tw(const typename O::T *tab, int m, 
 // x[jj + r N/R], multiplies by W_{Ns R}^{r k} (k = jj mod Ns), applies DFT-R and writes slot
 // (jj - k) R + k + r Ns.  Values stay in registers across the barrier; one scatter per pass.
 template <class O, int N, int TWSTEP, int Ns, int I>
-__device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T *tab, int j, bool active, int sign) {
+__device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T *tab, const typename O::T *ptab,
+                                        int j, bool active, int sign) {
   using C = typename O::C;
   constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   constexpr RadixList RL = fast_radices(N);
@@ -185,11 +213,17 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       if (GUARD && jj >= M) break;
 #pragma unroll
       for (int r = 0; r < R; r++) v[b * R + r] = line[pad<PS>(jj + r * M)];
-      if (Ns > 1) {
+      if constexpr (Ns > 1) {
+#if FAST_PASS_TABLES
+        const typename O::T *pt = ptab + fast_pass_offset(N, I) + jj % Ns;
+#pragma unroll
+        for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(pt, (r - 1) * Ns, sign));
+#else
         const int k = jj % Ns;
 #pragma unroll
         for (int r = 1; r < R; r++)
           v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(tab, r * k * (N / (Ns * R)) * TWSTEP, sign));
+#endif
       }
       if constexpr (R == 3) dft3<O>(&v[b * R], sign, w1);
       else if constexpr (R == 5) dft5<O>(&v[b * R], sign, w1, w2);
@@ -209,7 +243,7 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
     }
   }
   __syncthreads();
-  if constexpr (I + 1 < RL.n) fk_pass<O, N, TWSTEP, Ns * R, I + 1>(line, tab, j, active, sign);
+  if constexpr (I + 1 < RL.n) fk_pass<O, N, TWSTEP, Ns * R, I + 1>(line, tab, ptab, j, active, sign);
 }
 
 // f(e) for e = 0 .. V-1, U iterations unrolled per step of the outer loop
@@ -231,8 +265,14 @@ __device__ __forceinline__ typename O::C fk_deriv(const FParams &p, typename O::
   return O::iscale(v, (k < p.dmid) ? k : k - p.dg);
 }
 
+template <class O, int N>
+__host__ __device__ constexpr int fast_min_blocks() {
+  return sizeof(typename O::C) <= 8 ? (fast_max_values(N) > 8 ? FAST_MIN_BLOCKS_FP32 * 3 / 4 : FAST_MIN_BLOCKS_FP32)
+                                    : FastShape<N>::MINB;
+}
+
 template <class O, int KIND, int N>
-__global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fast(FParams p) {
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast(FParams p) {
   using C = typename O::C;
   using T = typename O::T;
   using G = typename O::G;
@@ -245,6 +285,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
   C *buf = reinterpret_cast<C *>(smem_raw);
   __shared__ int red[32];
   const T *tab = reinterpret_cast<const T *>(p.tw);
+  const T *ptab = reinterpret_cast<const T *>(p.ptw);
   // threads past TB*T (BLOCK rounded up to whole warps) hold no line
   const bool valid = SH::BLOCK == SH::USED || (int)threadIdx.x < SH::USED;
 
@@ -362,7 +403,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, FastShape<N>::MINB) k_fas
     __syncthreads();
 
     // ---------------- FFT ----------------
-    fk_pass<O, N, TWSTEP, 1, 0>(lb, tab, j0, act, KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1));
+    fk_pass<O, N, TWSTEP, 1, 0>(lb, tab, ptab, j0, act, KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1));
 
     // ---------------- post-processing + store ----------------
     const int gs = g0 + ls;

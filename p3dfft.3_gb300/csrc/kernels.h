@@ -57,9 +57,13 @@ int preload_kernels();
 // if none), in format fmt (0 double pairs, 1 float pairs, 2 float-float pairs).
 struct TableNeed {
   int fmt, tabN, auxN;
+  int aux_pass;  // 1: the aux table is the specialised kernels' per-pass twiddle rows of length auxN
 };
 size_t table_bytes(int N, int fmt);
 void fill_table(int N, int fmt, void *host_dst);
+// Per-pass twiddle rows of the specialised kernels for FFT length N (fast_stage.cuh)
+size_t pass_table_bytes(int N, int fmt);
+void fill_pass_table(int N, int fmt, void *host_dst);
 
 // Launch one stage on `stream`.  in != out is required (the host runtime guarantees it).
 // Tables come from `tabs` (allocated on first use) unless `tw_given` is non-null, in which case

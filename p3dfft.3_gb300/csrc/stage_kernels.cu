@@ -494,23 +494,46 @@ __global__ void k_deriv(const R *in, R *out, long long n, int sd0, int sd1, int 
 // double pairs (fmt 0), float pairs (fmt 1) or float-float pairs (fmt 2).
 size_t table_bytes(int N, int fmt) { return (size_t)N * (fmt == 1 ? 8 : 16); }
 
-void fill_table(int N, int fmt, void *dst) {
+// entry i of a table: W_M^m in format fmt
+static void put_twiddle(unsigned char *host, size_t i, long long m, long long M, int fmt) {
   const long double TWO_PI = 6.283185307179586476925286766559005768L;
+  const long double a = TWO_PI * (long double)(m % M) / (long double)M;
+  const long double c = cosl(a), s = -sinl(a);
+  if (fmt == 0) {
+    double v[2] = {(double)c, (double)s};
+    memcpy(&host[i * 16], v, 16);
+  } else if (fmt == 1) {
+    float v[2] = {(float)c, (float)s};
+    memcpy(&host[i * 8], v, 8);
+  } else {
+    float ch = (float)c, sh = (float)s;
+    float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
+    memcpy(&host[i * 16], v, 16);
+  }
+}
+
+void fill_table(int N, int fmt, void *dst) {
   unsigned char *host = static_cast<unsigned char *>(dst);
-  for (int k = 0; k < N; k++) {
-    long double a = TWO_PI * (long double)k / (long double)N;
-    long double c = cosl(a), s = -sinl(a);
-    if (fmt == 0) {
-      double v[2] = {(double)c, (double)s};
-      memcpy(&host[(size_t)k * 16], v, 16);
-    } else if (fmt == 1) {
-      float v[2] = {(float)c, (float)s};
-      memcpy(&host[(size_t)k * 8], v, 8);
-    } else {
-      float ch = (float)c, sh = (float)s;
-      float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
-      memcpy(&host[(size_t)k * 16], v, 16);
-    }
+  for (int k = 0; k < N; k++) put_twiddle(host, k, k, N, fmt);
+}
+
+size_t pass_table_bytes(int N, int fmt) {
+  return (size_t)std::max(1, fast_pass_entries(N)) * (fmt == 1 ? 8 : 16);
+}
+
+// Pass I >= 1: entry (r-1) Ns + k holds W_{Ns R}^{r k}, r = 1 .. R-1, k < Ns.
+void fill_pass_table(int N, int fmt, void *dst) {
+  unsigned char *host = static_cast<unsigned char *>(dst);
+  memset(host, 0, pass_table_bytes(N, fmt));
+  const RadixList L = fast_radices(N);
+  if (L.n <= 0) return;
+  int ns = L.r[0];
+  for (int i = 1; i < L.n; i++) {
+    const int R = L.r[i], off = fast_pass_offset(N, i);
+    for (int r = 1; r < R; r++)
+      for (int k = 0; k < ns; k++)
+        put_twiddle(host, (size_t)off + (size_t)(r - 1) * ns + k, (long long)r * k, (long long)ns * R, fmt);
+    ns *= R;
   }
 }
 
@@ -522,14 +545,16 @@ struct DeviceTables {
   ~DeviceTables() {
     for (auto &kv : tabs) cudaFree(kv.second);
   }
-  const void *get(int N, int fmt, int *err) {
+  // pass = 1: the specialised kernels' per-pass twiddle rows of FFT length N
+  const void *get(int N, int fmt, int *err, int pass = 0) {
     std::lock_guard<std::mutex> g(mu);
-    auto key = std::make_pair(N, fmt);
+    auto key = std::make_pair(N, fmt + 8 * pass);
     auto it = tabs.find(key);
     if (it != tabs.end()) return it->second;
-    size_t bytes = table_bytes(N, fmt);
+    size_t bytes = pass ? pass_table_bytes(N, fmt) : table_bytes(N, fmt);
     std::vector<unsigned char> host(bytes);
-    fill_table(N, fmt, host.data());
+    if (pass) fill_pass_table(N, fmt, host.data());
+    else fill_table(N, fmt, host.data());
     void *d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) {
       *err = E_CUDA;
@@ -702,11 +727,25 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   p.nrad = factorize(p.nfft, p.rad, 24);
   if (p.nrad < 0) return E_UNSUPPORTED;
 
+  // engine: the specialised kernels for C2C / even R2C / even C2R at their lengths, else the
+  // register engine (powers of two) or the generic engine; complex vector I/O needs element-aligned
+  // base pointers
+  const uintptr_t align_need = (d.prec == 8) ? 16 : 8;
+  const bool aligned = (((uintptr_t)in | (uintptr_t)out) % align_need) == 0;
+  const bool even = (p.nlog % 2) == 0;
+  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even);
+  const bool generic_only = getenv("P3DFFT_GB300_GENERIC_ONLY") != nullptr;
+  const bool fast_ok = fast_kind && fast_supported(p.nfft) && aligned;
+  if (d.engine == ENG_FAST && !fast_ok) return E_UNSUPPORTED;
+  if (d.engine == ENG_FIXED && !fixed_engine_len(p.nfft)) return E_UNSUPPORTED;
+  const bool use_fast = fast_ok && (d.engine == ENG_FAST || (d.engine == ENG_AUTO && !generic_only));
+
   const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? 2 : 0);
   if (tabs_out) {  // caller supplies the tables: report what is needed, launch nothing
     tabs_out->fmt = fmt;
     tabs_out->tabN = tabN;
-    tabs_out->auxN = (d.kind == K_R2R && p.r2r_np > 0) ? 8 * p.r2r_np : 0;
+    tabs_out->auxN = use_fast ? p.nfft : ((d.kind == K_R2R && p.r2r_np > 0) ? 8 * p.r2r_np : 0);
+    tabs_out->aux_pass = use_fast ? 1 : 0;
     return E_OK;
   }
   int err = E_OK;
@@ -716,7 +755,10 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   } else {
     p.tw = tabs->get(tabN, fmt, &err);
     if (!p.tw) return err;
-    if (d.kind == K_R2R && p.r2r_np > 0) {
+    if (use_fast) {
+      p.aux = tabs->get(p.nfft, fmt, &err, 1);
+      if (!p.aux) return err;
+    } else if (d.kind == K_R2R && p.r2r_np > 0) {
       p.aux = tabs->get(8 * p.r2r_np, fmt, &err);
       if (!p.aux) return err;
     }
@@ -741,19 +783,9 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   p.dt = d.d1[t];
   p.dother = d.d1[o];
 
-  // vector loads/stores of complex elements need element-aligned base pointers
-  const uintptr_t align_need = (d.prec == 8) ? 16 : 8;
-  const bool aligned = (((uintptr_t)in | (uintptr_t)out) % align_need) == 0;
   if (!aligned && (p.in_complex || p.out_complex)) return E_ALIGN;
 
-  // specialised kernels for C2C / even R2C / even C2R at power-of-two lengths
-  const bool even = (p.nlog % 2) == 0;
-  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even);
-  const bool generic_only = getenv("P3DFFT_GB300_GENERIC_ONLY") != nullptr;
-  const bool fast_ok = fast_kind && fast_supported(p.nfft) && aligned;
-  if (d.engine == ENG_FAST && !fast_ok) return E_UNSUPPORTED;
-  if (d.engine == ENG_FIXED && !fixed_engine_len(p.nfft)) return E_UNSUPPORTED;
-  if (fast_ok && (d.engine == ENG_FAST || (d.engine == ENG_AUTO && !generic_only))) {
+  if (use_fast) {
     FastArgs fa;
     fa.kind = (d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C);
     fa.n = p.nfft;
@@ -761,6 +793,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.in = in;
     q.out = out;
     q.tw = p.tw;
+    q.ptw = p.aux;
     q.iL = p.iL;
     q.it = p.it;
     q.io = p.io;
