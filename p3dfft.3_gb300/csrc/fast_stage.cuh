@@ -216,8 +216,25 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       if constexpr (Ns > 1) {
 #if FAST_PASS_TABLES
         const typename O::T *pt = ptab + fast_pass_offset(N, I) + jj % Ns;
+        if constexpr (O::TW_POWERS) {
+          // two table twiddles per butterfly, the others as products of at most two of them
+          C w[8];
+          w[1] = fk_tw<O>(pt, 0, sign);
+          if constexpr (R >= 3) w[2] = O::mul(w[1], w[1]);
+          if constexpr (R >= 4) w[3] = O::mul(w[2], w[1]);
+          if constexpr (R == 5) w[4] = O::mul(w[2], w[2]);
+          if constexpr (R == 8) {
+            w[4] = fk_tw<O>(pt, 3 * Ns, sign);
+            w[5] = O::mul(w[4], w[1]);
+            w[6] = O::mul(w[4], w[2]);
+            w[7] = O::mul(w[4], w[3]);
+          }
 #pragma unroll
-        for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(pt, (r - 1) * Ns, sign));
+          for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], w[r]);
+        } else {
+#pragma unroll
+          for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(pt, (r - 1) * Ns, sign));
+        }
 #else
         const int k = jj % Ns;
 #pragma unroll
@@ -317,10 +334,44 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
     const int lt = gl % p.dt, lo = gl / p.dt;
     const long long ibase = (long long)lt * p.it + (long long)lo * p.io;
 
+    C *lb = buf + (size_t)l * LS;
+    const int fsign = KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1);
+    constexpr RadixList RL = fast_radices(N);
+    // Native arithmetic, no C2R packing, and a first radix equal to the points per thread: the
+    // values a thread loads are exactly the inputs of its first butterfly, so the first pass runs
+    // on them in registers and the tile's first trip through shared memory is skipped.
+    constexpr bool FUSE1 = !O::SCALED && KIND != FK_C2R && RL.r[0] == V;
+    if constexpr (FUSE1) {
+      constexpr int R0 = RL.r[0];
+      C x[V];
+      if (act) {
+        const G *src = gin + (KIND == FK_R2C ? ibase : 2 * ibase);
+#pragma unroll
+        for (int e = 0; e < V; e++) {
+          const int j = j0 + e * TT;
+          RAW r;
+          if (KIND == FK_R2C) {
+            if (p.iL == 1) r = O::ldraw(src + 2 * j);
+            else r = O::ldraw2(src + (long long)(2 * j) * p.iL, src + (long long)(2 * j + 1) * p.iL);
+          } else {
+            r = O::ldraw(src + 2 * (long long)j * p.iL);
+          }
+          x[e] = O::from_raw(r, 0);
+        }
+        if constexpr (R0 == 3) dft3<O>(x, fsign, O::tw(tab, (N / 3) * TWSTEP));
+        else if constexpr (R0 == 5) dft5<O>(x, fsign, O::tw(tab, (N / 5) * TWSTEP), O::tw(tab, 2 * (N / 5) * TWSTEP));
+        else dft_p2<O, R0>(x, fsign);
+#pragma unroll
+        for (int r = 0; r < R0; r++) lb[pad<PS>(j0 * R0 + r)] = O::norm(x[r]);
+      }
+      __syncthreads();
+      if constexpr (RL.n > 1) fk_pass<O, N, TWSTEP, R0, 1>(lb, tab, ptab, j0, act, fsign);
+    }
+    int sc_out = 0;  // the tile's power-of-two scale (float-float)
+    if constexpr (!FUSE1) {
     // ---------------- load the tile into shared memory ----------------
     // Raw input values go straight to their slot (slot N holds X[N] for C2R).  Float-float tiles
     // are converted in place once the block-wide largest exponent is known.
-    C *lb = buf + (size_t)l * LS;
     RAW *lr = reinterpret_cast<RAW *>(lb);
     int emax = 0;
     if (act) {
@@ -352,7 +403,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
       }
     }
     int sc = 0;
-    if (O::SCALED) {
+    if constexpr (O::SCALED) {
       // block-wide max exponent -> scale 2^sc bringing the tile maximum near 2^20
       emax = __reduce_max_sync(0xffffffffu, emax);
       if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = emax;
@@ -403,7 +454,9 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
     __syncthreads();
 
     // ---------------- FFT ----------------
-    fk_pass<O, N, TWSTEP, 1, 0>(lb, tab, ptab, j0, act, KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1));
+    fk_pass<O, N, TWSTEP, 1, 0>(lb, tab, ptab, j0, act, fsign);
+    sc_out = sc;
+    }
 
     // ---------------- post-processing + store ----------------
     const int gs = g0 + ls;
@@ -414,20 +467,20 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int k = js + e * TT;
         if (KIND == FK_C2C) {
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[pad<PS>(k)], k), sc));
+          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[pad<PS>(k)], k), sc_out));
         } else if (KIND == FK_R2C) {
           // X[k] = 1/2 [(Z_k + conj Z_{N-k}) - i W_2N^k (Z_k - conj Z_{N-k})]
           C a = Y[pad<PS>(k)], b = O::conj(Y[pad<PS>(k == 0 ? 0 : N - k)]);
           C s = O::add(a, b), d = O::sub(a, b);
           C x = O::half(O::sub(s, O::muli(O::mul(O::tw(tab, k), d))));
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc));
+          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
           if (k == 0) {  // X[N] = Re Z_0 - Im Z_0
             C z0 = Y[pad<PS>(0)];
             C xn = O::mk(O::norm(O::sub(O::mk(z0.x, O::rzero()), O::mk(z0.y, O::rzero()))).x, O::rzero());
-            O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc));
+            O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc_out));
           }
         } else {  // C2R: reals 2k, 2k+1 = z[k]
-          RAW r = O::to_raw(Y[pad<PS>(k)], sc);
+          RAW r = O::to_raw(Y[pad<PS>(k)], sc_out);
           if (p.oL == 1) O::straw(gout + obase + 2 * k, r);
           else O::straw2(gout + obase + (long long)(2 * k) * p.oL, gout + obase + (long long)(2 * k + 1) * p.oL, r);
         }

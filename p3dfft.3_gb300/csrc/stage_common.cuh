@@ -20,6 +20,9 @@ namespace p3d {
 #ifndef FAST_IO_UNROLL_DF
 #define FAST_IO_UNROLL_DF 4
 #endif
+#ifndef FAST_TW_POWERS_FP32
+#define FAST_TW_POWERS_FP32 1
+#endif
 
 // ------------------------------------------------------------------------------------------
 // Arithmetic policies
@@ -92,6 +95,9 @@ struct Native {
   // register-level I/O of the specialised kernels (no tile scaling for native arithmetic)
   static constexpr bool SCALED = false;
   static constexpr int IO_UNROLL = FAST_IO_UNROLL_NATIVE;
+  // FP32: build most pass twiddles as products of two table entries (fewer loads through L1,
+  // the FP32 kernels' bottleneck; at most two roundings more per twiddle)
+  static constexpr bool TW_POWERS = sizeof(R) == 4 && FAST_TW_POWERS_FP32;
   using RAW = cx<R>;
   static __device__ __forceinline__ RAW ldraw(const G *p) { return ldg_c(reinterpret_cast<const cx<R> *>(p)); }
   static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
@@ -164,6 +170,7 @@ struct DF {
   // register-level I/O of the specialised kernels: raw IEEE bits, tile scaled by 2^sc
   static constexpr bool SCALED = true;
   static constexpr int IO_UNROLL = FAST_IO_UNROLL_DF;
+  static constexpr bool TW_POWERS = false;
   using RAW = longlong2;
   static __device__ __forceinline__ RAW ldraw(const G *p) { return __ldg(reinterpret_cast<const longlong2 *>(p)); }
   static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
