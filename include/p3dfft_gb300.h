@@ -51,6 +51,12 @@ int p3dfft_gb300_plan3d_types(int plan, int *dt1, int *dt2, int *prec);
 /* Stage list of a 3D plan: per stage 1+1+3+3+1+3+3+1 = 16 ints
  * (type, dim, gdims1[3], mo1[3], dcs1, gdims2[3], mo2[3], dcs2).  Returns the stage count. */
 int p3dfft_gb300_plan3d_stages(int plan, int *info, int max_stages);
+/* The schedule the executor runs, same format.  It applies the same 1D transform to each dim as
+ * the stage list above, between the same input and output grids, but may order the dims
+ * differently (R2C stays first, C2R last) and choose other intermediate memory orders so that
+ * every stage reads and writes long contiguous runs; P3DFFT_GB300_REFERENCE_SCHEDULE=1 runs the
+ * reference's stage list instead. */
+int p3dfft_gb300_plan3d_exec_stages(int plan, int *info, int max_stages);
 
 int p3dfft_gb300_plan1d(int type, const int gdims1[3], const int mo1[3], int dcs1,
                         const int gdims2[3], const int mo2[3], int dcs2, int dim);

@@ -163,7 +163,8 @@ struct StageTune {
   float ms = 0.f;  // measured duration when chosen by the autotuner
 };
 struct Plan {
-  std::vector<Stage> st;
+  std::vector<Stage> st;  // the reference planner's stage list (reported, tested for parity)
+  std::vector<Stage> ex;  // the schedule the executor runs (same transforms, see optimize_schedule)
   int L[3] = {0, 1, 2};
   int dt1 = 1, dt2 = 1, prec = 8;
   GridDesc g1, g2;
@@ -321,6 +322,8 @@ static bool find_order(const int types[3], const GridDesc &g1, const GridDesc &g
 
 static int empty_type(int dt, int prec) { return dt == 2 ? (prec == 4 ? 2 : 3) : (prec == 4 ? 0 : 1); }
 
+static void optimize_schedule(Plan *P);
+
 // transform3D ctor stage loop, templ.C:224-420
 static Plan *make_plan3(const int types[3], const GridDesc &g1, const GridDesc &g2) {
   for (int i = 0; i < 3; i++)
@@ -405,7 +408,100 @@ static Plan *make_plan3(const int types[3], const GridDesc &g1, const GridDesc &
     st.g2 = g2;
     P->st.push_back(st);
   }
+  optimize_schedule(P);
   return P;
+}
+
+// ------------------------------------------------------------------------------------------
+// Execution schedule.  The reference planner fixes the order of the 1D transforms and every
+// intermediate memory order (templ.C:224-420).  The result of the 3D transform depends only on the
+// input and output grids and on the 1D transform each dim gets: the intermediate layouts are
+// internal, and separable transforms commute (R2C must come first and C2R last, where the data
+// type changes).  On GB300 a stage whose lines are spread far apart in memory (a transform dim of
+// stride >= 16 Ki elements read or written through the tile dim) streams at ~70% of the rate of a
+// stage with contiguous lines, so the executor picks, over all admissible orders and the 36
+// choices of the two intermediate memory orders, the schedule with the cheapest accesses, keeping
+// the reference schedule on ties.  P3DFFT_GB300_REFERENCE_SCHEDULE=1 runs the reference schedule.
+// Cost of one side of a stage: 1 for contiguous lines, or for lines taken across a contiguous
+// tile dim t with the line's points near each other; 1.4 with the points >= 16 Ki elements
+// apart; 4 when neither the lines nor t are contiguous (uncoalesced).
+static double side_cost(const long long s[3], int L, int t) {
+  if (s[L] == 1) return 1.0;
+  if (s[t] != 1) return 4.0;
+  return s[L] >= 16384 ? 1.4 : 1.0;
+}
+
+// Load + store cost of a stage with the kernel's choice of tile dim (launch_stage): by output
+// stride when the input lines are contiguous, else by input stride.
+static double stage_cost(const Stage &st) {
+  long long s1[3], s2[3];
+  strides(st.g1, s1);
+  strides(st.g2, s2);
+  const int L = st.dim, a = (L + 1) % 3, b = (L + 2) % 3;
+  const int t = (s1[L] == 1) ? (s2[a] <= s2[b] ? a : b) : (s1[a] <= s1[b] ? a : b);
+  return side_cost(s1, L, t) + side_cost(s2, L, t);
+}
+
+static double schedule_cost(const std::vector<Stage> &v) {
+  double c = 0;
+  for (auto &st : v)
+    if (g_types[st.type].kind != K_EMPTY) c += stage_cost(st);
+  return c;
+}
+
+static void optimize_schedule(Plan *P) {
+  P->ex = P->st;
+  const char *ref = getenv("P3DFFT_GB300_REFERENCE_SCHEDULE");
+  if ((ref && ref[0] == '1') || P->st.size() != 3) return;
+  for (auto &st : P->st)
+    if (g_types[st.type].kind == K_EMPTY) return;
+  static const int MO[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  static const int PERM[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  double best = schedule_cost(P->ex) - 1e-9;
+  for (auto &pm : PERM) {
+    // the data type must chain: real-to-complex first, complex-to-real last
+    int dt = P->dt1;
+    bool ok = true;
+    for (int k = 0; k < 3 && ok; k++) {
+      const TypeInfo &t = g_types[P->st[pm[k]].type];
+      ok = t.dt1 == dt;
+      dt = t.dt2;
+    }
+    if (!ok) continue;
+    for (int a = 0; a < 6; a++)
+      for (int b = 0; b < 6; b++) {
+        std::vector<Stage> v(3);
+        GridDesc cur = P->g1;
+        for (int k = 0; k < 3; k++) {
+          const Stage &rs = P->st[pm[k]];
+          const TypeInfo &t = g_types[rs.type];
+          Stage st = rs;
+          st.g1 = cur;
+          GridDesc nx = cur;
+          if (t.dt1 < t.dt2) {  // R2C
+            nx.dcs = rs.dim;
+            nx.gdims[rs.dim] = nx.gdims[rs.dim] / 2 + 1;
+          } else if (t.dt2 < t.dt1) {  // C2R
+            nx.gdims[rs.dim] = (nx.gdims[rs.dim] - 1) * 2;
+            nx.dcs = -1;
+          }
+          const int *mo = k == 0 ? MO[a] : (k == 1 ? MO[b] : P->g2.mo);
+          for (int i = 0; i < 3; i++) nx.mo[i] = mo[i];
+          if (k == 2) nx = P->g2;
+          st.g2 = nx;
+          v[k] = st;
+          cur = nx;
+        }
+        bool dims_ok = true;
+        for (int i = 0; i < 3; i++) dims_ok &= v[2].g2.gdims[i] == P->g2.gdims[i];
+        if (!dims_ok) continue;
+        const double c = schedule_cost(v);
+        if (c < best) {
+          best = c - 1e-9;
+          P->ex = v;
+        }
+      }
+  }
 }
 
 static Plan *make_plan1(int type, const GridDesc &g1, const GridDesc &g2, int d) {
@@ -441,6 +537,7 @@ static Plan *make_plan1(int type, const GridDesc &g1, const GridDesc &g2, int d)
   st.g1 = g1;
   st.g2 = g2;
   P->st.push_back(st);
+  P->ex = P->st;
   return P;
 }
 
@@ -513,9 +610,9 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
   strides(s.g1, d.s1);
   strides(s.g2, d.s2);
   d.deriv = deriv ? 1 : 0;
-  const size_t idx = (size_t)(&s - P->st.data());
+  const size_t idx = (size_t)(&s - P->ex.data());
   d.engine = d.talt = 0;
-  if (P->tune.size() == P->st.size() && (P->prec == 4 || P->tuned_arith == arith_mode())) {
+  if (P->tune.size() == P->ex.size() && idx < P->ex.size() && (P->prec == 4 || P->tuned_arith == arith_mode())) {
     d.engine = P->tune[idx].engine;
     d.talt = P->tune[idx].talt;
   }
@@ -581,12 +678,12 @@ static std::string stage_key(const StageDesc &d, int arith) {
 
 static int autotune_plan(Plan *P) {
   if (!ensure_device()) return t_err;
-  const int n = (int)P->st.size();
+  const int n = (int)P->ex.size();
   const int arith = arith_mode();
   const int ar = P->prec == 8 ? arith : AR_NATIVE;
   std::vector<StageTune> tune(n);
   size_t maxb = 0;
-  for (auto &s : P->st) {
+  for (auto &s : P->ex) {
     const TypeInfo &t = g_types[s.type];
     maxb = std::max(maxb, std::max((size_t)elems(s.g1) * t.dt1, (size_t)elems(s.g2) * t.dt2) * P->prec);
   }
@@ -595,7 +692,7 @@ static int autotune_plan(Plan *P) {
   int rc = E_OK;
   P->tune.clear();  // fill_stage_desc below must see the heuristic
   for (int si = 0; si < n && rc == E_OK; si++) {
-    const Stage &s = P->st[si];
+    const Stage &s = P->ex[si];
     if (g_types[s.type].kind == K_EMPTY) continue;
     StageDesc d;
     fill_stage_desc(P, s, false, d);
@@ -697,15 +794,15 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     if (!ensure_buf(&B.stage_out, &B.stage_out_bytes, out_bytes)) return E_CUDA;
     dout = B.stage_out;
   }
-  const int n = (int)P->st.size();
+  const int n = (int)P->ex.size();
   // buffer assignment: consecutive stages never share a buffer and stage 0 never writes `in`
   size_t need = 0;
-  for (int s = 0; s < n - 1; s++) need = std::max(need, stage_out_bytes(P, P->st[s]));
+  for (int s = 0; s < n - 1; s++) need = std::max(need, stage_out_bytes(P, P->ex[s]));
   std::vector<void *> dst(n, nullptr);
   dst[n - 1] = dout;
   int nscratch_used = 0;
   for (int s = n - 2; s >= 0; s--) {
-    size_t bytes = stage_out_bytes(P, P->st[s]);
+    size_t bytes = stage_out_bytes(P, P->ex[s]);
     void *cand = nullptr;
     if (dout != dst[s + 1] && bytes <= out_bytes && !(s == 0 && dout == din) && dout != din) cand = dout;
     if (!cand) {
@@ -740,7 +837,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   const void *src = din;
   int rc = E_OK;
   for (int s = 0; s < n && rc == E_OK; s++) {
-    const Stage &st = P->st[s];
+    const Stage &st = P->ex[s];
     bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
     void *d = dst[s];
     if (stage_ev) cudaEventRecord(stage_ev[s], cur_stream());
@@ -808,13 +905,13 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
     set_err(E_BAD_ARG, "this entry point takes device pointers only (host data would need staging buffers)");
     return E_BAD_ARG;
   }
-  const int n = (int)P->st.size();
+  const int n = (int)P->ex.size();
   const size_t out_bytes = (size_t)elems(P->g2) * P->dt2 * P->prec;
   // buffer assignment as in exec_plan, with the two given scratch buffers
   void *dst[8];
   dst[n - 1] = out;
   for (int s = n - 2; s >= 0; s--) {
-    size_t bytes = stage_out_bytes(P, P->st[s]);
+    size_t bytes = stage_out_bytes(P, P->ex[s]);
     if (out != dst[s + 1] && out != in && bytes <= out_bytes) dst[s] = out;
     else dst[s] = (dst[s + 1] == scratch0) ? scratch1 : scratch0;
     if ((dst[s] == scratch0 || dst[s] == scratch1) && bytes > scratch_bytes) {
@@ -832,7 +929,7 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
   size_t off = 0;
   unsigned char *host = static_cast<unsigned char *>(tw_host);
   for (int s = 0; s < n; s++) {
-    const Stage &st = P->st[s];
+    const Stage &st = P->ex[s];
     if (g_types[st.type].kind == K_EMPTY) continue;
     StageDesc d;
     fill_stage_desc(P, st, false, d);
@@ -865,7 +962,7 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
   }
   const void *src = in;
   for (int s = 0; s < n; s++) {
-    const Stage &st = P->st[s];
+    const Stage &st = P->ex[s];
     bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
     int rc = run_stage(P, st, src, dst[s], deriv, tw[s], aux[s]);
     if (rc != E_OK) return rc;
@@ -931,7 +1028,7 @@ int plan3d_sizes(int plan, size_t *in_bytes, size_t *out_bytes, size_t *scratch_
     return E_BAD_ARG;
   }
   size_t need = 0;
-  for (size_t s = 0; s + 1 < P->st.size(); s++) need = std::max(need, stage_out_bytes(P, P->st[s]));
+  for (size_t s = 0; s + 1 < P->ex.size(); s++) need = std::max(need, stage_out_bytes(P, P->ex[s]));
   if (in_bytes) *in_bytes = (size_t)elems(P->g1) * P->dt1 * P->prec;
   if (out_bytes) *out_bytes = (size_t)elems(P->g2) * P->dt2 * P->prec;
   if (scratch_bytes) *scratch_bytes = need;
@@ -1032,9 +1129,9 @@ int p3dfft_gb300_autotune(int plan, int is1d) {
 int p3dfft_gb300_plan_tuning(int plan, int is1d, int *engine, int *talt, double *ms, int max_stages) {
   Plan *P = plan_of(plan, is1d);
   if (!P) return -1;
-  const int n = (int)P->st.size();
+  const int n = (int)P->ex.size();
   for (int s = 0; s < n && s < max_stages; s++) {
-    const bool t = P->tune.size() == P->st.size();
+    const bool t = P->tune.size() == P->ex.size();
     if (engine) engine[s] = t ? P->tune[s].engine : 0;
     if (talt) talt[s] = t ? P->tune[s].talt : 0;
     if (ms) ms[s] = t ? P->tune[s].ms : 0.0;
@@ -1044,11 +1141,11 @@ int p3dfft_gb300_plan_tuning(int plan, int is1d, int *engine, int *talt, double 
 
 int p3dfft_gb300_plan_set_engine(int plan, int is1d, int stage, int engine, int talt) {
   Plan *P = plan_of(plan, is1d);
-  if (!P || stage < 0 || stage >= (int)P->st.size() || engine < 0 || engine > ENG_GENERIC) {
+  if (!P || stage < 0 || stage >= (int)P->ex.size() || engine < 0 || engine > ENG_GENERIC) {
     set_err(E_BAD_ARG, "invalid plan, stage or engine");
     return E_BAD_ARG;
   }
-  if (P->tune.size() != P->st.size()) P->tune.assign(P->st.size(), StageTune());
+  if (P->tune.size() != P->ex.size()) P->tune.assign(P->ex.size(), StageTune());
   P->tune[stage].engine = engine;
   P->tune[stage].talt = talt ? 1 : 0;
   P->tuned_arith = arith_mode();
@@ -1117,10 +1214,10 @@ int p3dfft_gb300_plan3d_types(int plan, int *dt1, int *dt2, int *prec) {
   return E_OK;
 }
 
-static int stages_info(Plan *P, int *info, int max_stages) {
-  int n = (int)P->st.size();
+static int stages_info(const std::vector<Stage> &v, int *info, int max_stages) {
+  int n = (int)v.size();
   for (int s = 0; s < n && s < max_stages; s++) {
-    const Stage &st = P->st[s];
+    const Stage &st = v[s];
     int *q = info + 16 * s;
     q[0] = st.type;
     q[1] = st.dim;
@@ -1139,7 +1236,13 @@ static int stages_info(Plan *P, int *info, int max_stages) {
 int p3dfft_gb300_plan3d_stages(int plan, int *info, int max_stages) {
   Plan *P = get_plan(g_plans3, plan);
   if (!P) return -1;
-  return stages_info(P, info, max_stages);
+  return stages_info(P->st, info, max_stages);
+}
+
+int p3dfft_gb300_plan3d_exec_stages(int plan, int *info, int max_stages) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) return -1;
+  return stages_info(P->ex, info, max_stages);
 }
 
 int p3dfft_gb300_plan1d(int type, const int gdims1[3], const int mo1[3], int dcs1, const int gdims2[3],
@@ -1241,7 +1344,7 @@ int p3dfft_gb300_profile_stages(int plan, const void *in, void *out, int idir, i
     return -1;
   }
   if (!ensure_device()) return -1;
-  const int n = (int)P->st.size();
+  const int n = (int)P->ex.size();
   std::vector<cudaEvent_t> ev(n + 1);
   for (auto &e : ev) cudaEventCreate(&e);
   std::vector<double> acc(n, 0.0);

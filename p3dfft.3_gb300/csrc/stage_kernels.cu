@@ -771,7 +771,10 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   // tile selection: t = batch dim along which consecutive lines are taken
   p.iL = d.s1[L];
   p.oL = d.s2[L];
-  int t = d.s1[a] <= d.s1[b] ? a : b;  // the batch dim with the smaller input stride
+  // t: with lines contiguous on input (L-major load) the tile dim only matters for the store, so
+  // it is the batch dim with the smaller output stride (a t-major store when that dim is
+  // contiguous); otherwise the batch dim with the smaller input stride (t-major load)
+  int t = (d.s1[L] == 1) ? (d.s2[a] <= d.s2[b] ? a : b) : (d.s1[a] <= d.s1[b] ? a : b);
   if (d.talt) t = (t == a) ? b : a;
   const int o = (t == a) ? b : a;
   p.load_Lmajor = d.s1[L] == 1 ? 1 : 0;

@@ -66,6 +66,7 @@ def lib():
         "p3dfft_gb300_destroy3d": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_plan3d_types": ([ctypes.c_int, ip, ip, ip], ctypes.c_int),
         "p3dfft_gb300_plan3d_stages": ([ctypes.c_int, ip, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_plan3d_exec_stages": ([ctypes.c_int, ip, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_plan1d": ([ctypes.c_int, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_exec1d": ([ctypes.c_int, vp, vp, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_destroy1d": ([ctypes.c_int], ctypes.c_int),
@@ -192,9 +193,11 @@ class Transform3D:
         lib().p3dfft_gb300_plan3d_types(h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(p))
         self.dt1, self.dt2, self.prec = a.value, b.value, p.value
 
-    def stages(self):
+    def stages(self, executed=False):
+        """The reference planner's stage list, or (executed=True) the schedule the executor runs."""
         buf = (ctypes.c_int * (16 * 8))()
-        n = lib().p3dfft_gb300_plan3d_stages(self.handle, buf, 8)
+        fn = lib().p3dfft_gb300_plan3d_exec_stages if executed else lib().p3dfft_gb300_plan3d_stages
+        n = fn(self.handle, buf, 8)
         out = []
         for s in range(n):
             q = buf[16 * s:16 * s + 16]

@@ -96,3 +96,24 @@ def test_256cube_round_trip_with_derivative(gpu, oracle, arith):
     assert rel_l2(f.exec_deriv(x, idir=0), yo) < 1e-12
     zo = oracle.OraclePlan(b.types, gd2, (1, 2, 0), gd, (0, 1, 2), 0, -1).exec(yo)
     assert rel_l2(b.exec(yo), zo) < 1e-12
+
+
+def test_executed_schedule_matches_reference_schedule(gpu, monkeypatch):
+    """The executor's reordered schedule and the reference planner's stage list give the same
+    transform (to rounding) for the headline plan shape, forward with d/dz and backward."""
+    p3d = gpu
+    p3d.set_fp64_arith(1)
+    gd, gd2 = (256, 128, 32), (129, 128, 32)  # planes of >= 16 Ki complex elements
+    ft = [p3d.R2CFFT_D, p3d.CFFT_FORWARD_D, p3d.CFFT_FORWARD_D]
+    bt = [p3d.C2RFFT_D, p3d.CFFT_BACKWARD_D, p3d.CFFT_BACKWARD_D]
+    x = seeded_field((32, 128, 256), seed=11)
+    out = {}
+    for ref in ("1", "0"):
+        monkeypatch.setenv("P3DFFT_GB300_REFERENCE_SCHEDULE", ref)
+        f = p3d.Transform3D(ft, gd, (0, 1, 2), gd2, (1, 2, 0), -1, 0)
+        b = p3d.Transform3D(bt, gd2, (1, 2, 0), gd, (0, 1, 2), 0, -1)
+        assert (f.stages(executed=True) == f.stages()) == (ref == "1")
+        y = f.exec_deriv(x, idir=2)
+        out[ref] = (y, b.exec(y))
+    assert rel_l2(out["0"][0], out["1"][0]) < 1e-13
+    assert rel_l2(out["0"][1], out["1"][1]) < 1e-13
