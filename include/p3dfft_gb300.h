@@ -32,6 +32,11 @@ void p3dfft_gb300_set_stream(void *cuda_stream);
 /* 1 (default): exec returns after the result is in `out`; 0: device-pointer execs return
  * once the work is queued on the stream (host-pointer execs always synchronise). */
 void p3dfft_gb300_set_sync(int sync);
+/* 1 (default): page-locked host arrays (cudaHostAlloc, cudaHostRegister,
+ * p3dfft_gb300_host_alloc_pinned) are read by the first stage and written by the last stage
+ * directly over NVLink-C2C, without staging copies; 0: always stage host arrays through HBM.
+ * Pageable host arrays are always staged.  P3DFFT_GB300_HOST_DIRECT=0 sets 0 at start-up. */
+void p3dfft_gb300_set_host_direct(int on);
 /* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,
  * ~1e-14 relative L2 per 3D transform), 0 = native FP64 DFMA (slow on GB300).  The initial value
  * can be set with P3DFFT_GB300_FP64_ARITH=native. */

@@ -141,6 +141,7 @@ struct Stage {
   int type;
   int dim;
   GridDesc g1, g2;
+  int ex_index = -1;  // position in the executed schedule (selects the stage's tuning)
 };
 struct Buffers {
   void *scratch[2] = {nullptr, nullptr};
@@ -409,6 +410,7 @@ static Plan *make_plan3(const int types[3], const GridDesc &g1, const GridDesc &
     P->st.push_back(st);
   }
   optimize_schedule(P);
+  for (size_t i = 0; i < P->ex.size(); i++) P->ex[i].ex_index = (int)i;
   return P;
 }
 
@@ -538,6 +540,7 @@ static Plan *make_plan1(int type, const GridDesc &g1, const GridDesc &g2, int d)
   st.g2 = g2;
   P->st.push_back(st);
   P->ex = P->st;
+  P->ex[0].ex_index = 0;
   return P;
 }
 
@@ -552,6 +555,23 @@ static bool is_device_ptr(const void *p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister) is addressable by kernels over
+// NVLink-C2C; returns its device-side address, or nullptr for any other pointer.
+static int g_host_direct = -1;  // -1: from P3DFFT_GB300_HOST_DIRECT (default on) at first use
+static void *mapped_host_ptr(const void *p) {
+  if (g_host_direct < 0) {
+    const char *e = getenv("P3DFFT_GB300_HOST_DIRECT");
+    g_host_direct = (e && e[0] == '0') ? 0 : 1;
+  }
+  if (!p || !g_host_direct) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 static bool ensure_buf(void **p, size_t *have, size_t need) {
@@ -610,9 +630,10 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
   strides(s.g1, d.s1);
   strides(s.g2, d.s2);
   d.deriv = deriv ? 1 : 0;
-  const size_t idx = (size_t)(&s - P->ex.data());
+  const size_t idx = (size_t)s.ex_index;
   d.engine = d.talt = 0;
-  if (P->tune.size() == P->ex.size() && idx < P->ex.size() && (P->prec == 4 || P->tuned_arith == arith_mode())) {
+  if (s.ex_index >= 0 && P->tune.size() == P->ex.size() && idx < P->ex.size() &&
+      (P->prec == 4 || P->tuned_arith == arith_mode())) {
     d.engine = P->tune[idx].engine;
     d.talt = P->tune[idx].talt;
   }
@@ -628,7 +649,7 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
     size_t bytes = (size_t)elems(s.g1) * t.dt1 * P->prec;
     TimerScope ts(2);
     if (same) {
-      if (src != dst && cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, cur_stream()) != cudaSuccess)
+      if (src != dst && cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, cur_stream()) != cudaSuccess)
         rc = E_CUDA;
     } else {
       long long s1[3], s2[3];
@@ -652,6 +673,72 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
     else if (rc == E_ALIGN)
       set_err(E_ALIGN, "data pointers must be aligned to one complex element (16 bytes FP64, 8 bytes FP32)");
     else set_err(rc, "invalid stage description");
+  }
+  return rc;
+}
+
+// A dim that is the slowest of both the stage's input and output layouts and not its transform
+// dim: slabs along it are contiguous on both sides and the other dims' strides do not depend on it.
+static int slab_dim(const Stage &st) {
+  if (g_types[st.type].kind == K_EMPTY) return -1;
+  for (int d = 0; d < 3; d++)
+    if (d != st.dim && st.g1.mo[d] == 2 && st.g2.mo[d] == 2 && st.g1.gdims[d] >= 2) return d;
+  return -1;
+}
+
+static cudaStream_t g_copy_stream = nullptr;
+static cudaEvent_t g_slab_ev[17];
+
+// Runs one stage slab by slab along dim sd, overlapping the host copy of each slab on the copy
+// stream: side 0 copies host `host` into `src` (the stage's staged input) slab by slab before
+// the stage reads it; side 1 copies the stage's output `dst` to host `host` slab by slab after
+// the stage writes it.  All work is ordered on the library stream when this returns.
+static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *host, const void *src, void *dst,
+                           bool deriv, int side) {
+  const int NS = 8;
+  if (!g_copy_stream) {
+    if (cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking) != cudaSuccess) return E_CUDA;
+    for (auto &e : g_slab_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return E_CUDA;
+  }
+  const TypeInfo &t = g_types[st.type];
+  long long s1[3], s2[3];
+  strides(st.g1, s1);
+  strides(st.g2, s2);
+  const size_t u1 = (size_t)s1[sd] * t.dt1 * P->prec, u2 = (size_t)s2[sd] * t.dt2 * P->prec;  // bytes per slab row
+  const int len = st.g1.gdims[sd];
+  int f = 1;  // slab starts stay 16-byte aligned on both sides
+  while (f < 16 && ((f * u1) % 16 || (f * u2) % 16)) f++;
+  const int per = ((len + NS - 1) / NS + f - 1) / f * f;
+  cudaStream_t cs = g_copy_stream, ms = cur_stream();
+  // the copy stream starts after everything already queued on the library stream
+  if (cudaEventRecord(g_slab_ev[16], ms) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[16], 0) != cudaSuccess)
+    return E_CUDA;
+  int rc = E_OK;
+  for (int c = 0, k = 0; c < len && rc == E_OK; c += per, k++) {
+    const int m = std::min(per, len - c);
+    Stage sl = st;
+    sl.g1.gdims[sd] = sl.g2.gdims[sd] = m;
+    const unsigned char *sp = static_cast<const unsigned char *>(src) + (size_t)c * u1;
+    unsigned char *dp = static_cast<unsigned char *>(dst) + (size_t)c * u2;
+    if (side == 0) {
+      if (cudaMemcpyAsync(const_cast<unsigned char *>(sp), static_cast<const unsigned char *>(host) + (size_t)c * u1,
+                          (size_t)m * u1, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
+          cudaEventRecord(g_slab_ev[k], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[k], 0) != cudaSuccess)
+        return E_CUDA;
+      rc = run_stage(P, sl, sp, dp, deriv);
+    } else {
+      rc = run_stage(P, sl, sp, dp, deriv);
+      if (rc == E_OK &&
+          (cudaEventRecord(g_slab_ev[k], ms) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[k], 0) != cudaSuccess ||
+           cudaMemcpyAsync(static_cast<unsigned char *>(const_cast<void *>(host)) + (size_t)c * u2, dp, (size_t)m * u2,
+                           cudaMemcpyDeviceToHost, cs) != cudaSuccess))
+        return E_CUDA;
+    }
+  }
+  if (side == 1) {  // the library stream continues after the last copy
+    if (cudaEventRecord(g_slab_ev[16], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[16], 0) != cudaSuccess)
+      return E_CUDA;
   }
   return rc;
 }
@@ -781,20 +868,39 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     set_err(E_BAD_ARG, "batched execution takes device pointers only");
     return E_BAD_ARG;
   }
-  if (!din_dev) {
+  // Page-locked host arrays are read by the first stage and written by the last stage directly
+  // over NVLink-C2C, with no staging copy; pageable host arrays are staged through HBM.
+  void *in_mapped = din_dev ? nullptr : mapped_host_ptr(in);
+  void *out_mapped = dout_dev ? nullptr : mapped_host_ptr(out);
+  if (in_mapped && in != out) din = in_mapped;
+  const bool out_direct = out_mapped && in != out;
+  if (out_direct) dout = out_mapped;
+  const int n = (int)P->ex.size();
+  // Host staging overlapped with the first / last stage: the copy of slab c runs on the copy
+  // stream while the stage works on slab c-1 (slabs along a dim that is the slowest of the
+  // stage's input and output layouts, so each slab is contiguous on both sides).
+  const bool stage_host_in = !din_dev && din == in, stage_host_out = !dout_dev && !out_direct;
+  // (only for fields of 32 MB and more: below that, one copy costs less than the extra launches)
+  const size_t kSlabMin = 32u << 20;
+  const int sd_in = (stage_host_in && in_bytes >= kSlabMin && n >= 2 && !stage_ev && !g_timers_on)
+                        ? slab_dim(P->ex[0]) : -1;
+  const int sd_out = (stage_host_out && out_bytes >= kSlabMin && n >= 2 && !stage_ev && !g_timers_on && in != out)
+                         ? slab_dim(P->ex[n - 1]) : -1;
+  if (stage_host_in) {
     if (!ensure_buf(&B.stage_in, &B.stage_in_bytes, in_bytes)) return E_CUDA;
-    TimerScope ts(4);
-    if (cudaMemcpyAsync(B.stage_in, in, in_bytes, cudaMemcpyHostToDevice, cur_stream()) != cudaSuccess) {
-      set_err(E_CUDA, "host-to-device copy failed");
-      return E_CUDA;
+    if (sd_in < 0) {
+      TimerScope ts(4);
+      if (cudaMemcpyAsync(B.stage_in, in, in_bytes, cudaMemcpyHostToDevice, cur_stream()) != cudaSuccess) {
+        set_err(E_CUDA, "host-to-device copy failed");
+        return E_CUDA;
+      }
     }
     din = B.stage_in;
   }
-  if (!dout_dev) {
+  if (stage_host_out) {
     if (!ensure_buf(&B.stage_out, &B.stage_out_bytes, out_bytes)) return E_CUDA;
     dout = B.stage_out;
   }
-  const int n = (int)P->ex.size();
   // buffer assignment: consecutive stages never share a buffer and stage 0 never writes `in`
   size_t need = 0;
   for (int s = 0; s < n - 1; s++) need = std::max(need, stage_out_bytes(P, P->ex[s]));
@@ -804,7 +910,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   for (int s = n - 2; s >= 0; s--) {
     size_t bytes = stage_out_bytes(P, P->ex[s]);
     void *cand = nullptr;
-    if (dout != dst[s + 1] && bytes <= out_bytes && !(s == 0 && dout == din) && dout != din) cand = dout;
+    if (!out_direct && dout != dst[s + 1] && bytes <= out_bytes && !(s == 0 && dout == din) && dout != din) cand = dout;
     if (!cand) {
       int k = (dst[s + 1] == B.scratch[0] && B.scratch[0]) ? 1 : 0;
       if (need > B.scratch_bytes || !B.scratch[k]) {
@@ -841,7 +947,11 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
     void *d = dst[s];
     if (stage_ev) cudaEventRecord(stage_ev[s], cur_stream());
-    if (d == src) {  // single-stage in-place call: go through scratch, then copy back
+    if (s == 0 && sd_in >= 0) {
+      rc = run_stage_slabs(P, st, sd_in, in, din, d, deriv, 0);
+    } else if (s == n - 1 && sd_out >= 0) {
+      rc = run_stage_slabs(P, st, sd_out, out, src, d, deriv, 1);
+    } else if (d == src) {  // single-stage in-place call: go through scratch, then copy back
       size_t bytes = stage_out_bytes(P, st);
       if ((in_capture() || !B.owned) && (bytes > B.scratch_bytes || !B.scratch[0])) {
         set_err(E_PLAN, "scratch set too small for an in-place stage (%zu bytes needed)", bytes);
@@ -858,7 +968,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   }
   if (stage_ev) cudaEventRecord(stage_ev[n], cur_stream());
   if (rc != E_OK) return rc;
-  if (!dout_dev) {
+  if (stage_host_out && sd_out < 0) {
     TimerScope ts(5);
     if (cudaMemcpyAsync(out, dout, out_bytes, cudaMemcpyDeviceToHost, cur_stream()) != cudaSuccess) {
       set_err(E_CUDA, "device-to-host copy failed");
@@ -1085,6 +1195,7 @@ void p3dfft_clear_error(void) {
 }
 void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
+void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on ? 1 : 0; }
 void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }
 int p3dfft_gb300_get_fp64_arith(void) { return arith_mode(); }
 const char *p3dfft_gb300_version(void) { return "p3dfft-gb300 0.1 (sm_103a)"; }

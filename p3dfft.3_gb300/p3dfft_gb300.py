@@ -60,6 +60,7 @@ def lib():
         "p3dfft_last_error": ([], ctypes.c_int), "p3dfft_last_error_string": ([], ctypes.c_char_p),
         "p3dfft_clear_error": ([], None),
         "p3dfft_gb300_set_stream": ([vp], None), "p3dfft_gb300_set_sync": ([ctypes.c_int], None),
+        "p3dfft_gb300_set_host_direct": ([ctypes.c_int], None),
         "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
         "p3dfft_gb300_plan3d": ([ip, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_exec3d": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
@@ -146,6 +147,11 @@ def set_fp64_arith(mode: int):
 
 def set_sync(sync: bool):
     lib().p3dfft_gb300_set_sync(1 if sync else 0)
+
+
+def set_host_direct(on: bool):
+    """Page-locked host arrays read / written by the kernels over NVLink-C2C (True) or staged."""
+    lib().p3dfft_gb300_set_host_direct(1 if on else 0)
 
 
 def set_stream(stream_ptr: int):
