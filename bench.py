@@ -441,7 +441,9 @@ def serve_workload(p3d, n_jobs=10000, seed=5, fractions=(0.5, 0.75, 0.9), nslots
     cap = n_jobs / makespan
     print(f"serve: saturation {cap:.0f} jobs/s", file=sys.stderr, flush=True)
     out["saturation"] = {"jobs_per_s": cap, "GB_per_s": alg.sum() / makespan / 1e9,
-                         "max_running": st["max_running"], "peak_hbm_GB": st["peak_hbm_bytes"] / 1e9}
+                         "max_running": st["max_running"], "peak_hbm_GB": st["peak_hbm_bytes"] / 1e9,
+                         "dispatcher_us_per_job": {"queue_work": st["host_launch_s"] / n_jobs * 1e6,
+                                                   "release": st["host_release_s"] / n_jobs * 1e6}}
     rng = np.random.default_rng(seed + 1)
     out["rates"] = []
     for frac in fractions:
@@ -479,6 +481,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload summary")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream summary")
     ap.add_argument("--serve-jobs", type=int, default=10000)
+    ap.add_argument("--serve-slots", type=int, default=16)
     ap.add_argument("--kernels-only", choices=["fp64", "fp32"], default=None,
                     help="run only the device-resident round trip of that form (profiling runs)")
     args = ap.parse_args()
@@ -526,7 +529,7 @@ def main():
         import p3dfft_gb300 as p3d
         import build_lib
         build_lib.build()
-        res = serve_workload(p3d, n_jobs=args.serve_jobs)
+        res = serve_workload(p3d, n_jobs=args.serve_jobs, nslots=args.serve_slots)
         if rank == 0:
             print(json.dumps({"workload": "serving stream", **res}), flush=True)
         return
@@ -697,7 +700,7 @@ def main():
         del d_in, d_spec, d_out  # free HBM for the batch buffers
         forms["batched_uneven"] = batch_workload(p3d, L, max(3, min(args.steps, 10)), 3)
     if not args.no_serve:
-        forms["serving"] = serve_workload(p3d, n_jobs=args.serve_jobs)
+        forms["serving"] = serve_workload(p3d, n_jobs=args.serve_jobs, nslots=args.serve_slots)
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

@@ -139,7 +139,8 @@ int p3dfft_gb300_server_drain(int srv);
 double p3dfft_gb300_server_clock(int srv);
 /* t[0] arrival, t[1] admission, t[2] completion, on the server clock */
 int p3dfft_gb300_server_job_times(int srv, int job, double *t);
-/* completed, failed, admitted, peak HBM bytes held by jobs, budget, most jobs running at once */
+/* completed, failed, admitted, peak HBM bytes held by jobs, budget, most jobs running at once,
+ * dispatcher seconds spent queueing jobs' work, and releasing their memory (up to n values) */
 int p3dfft_gb300_server_stats(int srv, double *stats, int n);
 int p3dfft_gb300_server_destroy(int srv);
 

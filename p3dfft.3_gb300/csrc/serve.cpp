@@ -78,6 +78,7 @@ struct Server {
   std::vector<SJob *> jobs;              // all jobs by id
   std::atomic<int> callbacks{0};         // completions not yet retired
   long long completed = 0, failed = 0, admitted = 0;
+  double host_launch_s = 0, host_release_s = 0;  // dispatcher time spent queueing / releasing jobs
   int max_running = 0;
   bool admit_dirty = false;  // queue, slots or budget changed since the last admission pass
   bool stop = false;
@@ -232,7 +233,9 @@ static void dispatcher(Server *S) {
       continue;
     }
     lk.unlock();
+    const double h0 = S->now();
     for (SJob *j : done) release_job_memory(j, S->streams[j->slot]);
+    const double h1 = S->now();
     std::vector<std::pair<SJob *, int>> failed;
     for (SJob *j : start) {
       const int rc = launch_job(S, j);
@@ -242,7 +245,10 @@ static void dispatcher(Server *S) {
         failed.push_back({j, rc});
       }
     }
+    const double h2 = S->now();
     lk.lock();
+    S->host_release_s += h1 - h0;
+    S->host_launch_s += h2 - h1;
     for (SJob *j : done) {
       S->in_use -= j->need;
       j->state = J_DONE;
@@ -391,14 +397,15 @@ int p3dfft_gb300_server_job_times(int srv, int job, double *t) {
   return j->state == J_DONE ? E_OK : (j->state == J_FAILED ? -j->err : E_PLAN);
 }
 
-// stats: completed, failed, admitted, peak HBM bytes in use, budget bytes, most jobs running at once
+// stats: completed, failed, admitted, peak HBM bytes in use, budget bytes, most jobs running at
+// once, dispatcher seconds spent queueing jobs' work, and releasing their memory
 int p3dfft_gb300_server_stats(int srv, double *stats, int n) {
   Server *S = get_server(srv);
   if (!S || !stats) return E_BAD_ARG;
   std::lock_guard<std::mutex> g(S->mu);
-  const double v[6] = {(double)S->completed, (double)S->failed, (double)S->admitted, (double)S->peak,
-                       (double)S->budget, (double)S->max_running};
-  for (int i = 0; i < n && i < 6; i++) stats[i] = v[i];
+  const double v[8] = {(double)S->completed, (double)S->failed, (double)S->admitted, (double)S->peak,
+                       (double)S->budget, (double)S->max_running, S->host_launch_s, S->host_release_s};
+  for (int i = 0; i < n && i < 8; i++) stats[i] = v[i];
   return E_OK;
 }
 

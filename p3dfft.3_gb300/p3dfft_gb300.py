@@ -439,10 +439,11 @@ class Server:
         return rc, (t[0], t[1], t[2])
 
     def stats(self):
-        v = (ctypes.c_double * 6)()
-        lib().p3dfft_gb300_server_stats(self.handle, v, 6)
-        keys = ("completed", "failed", "admitted", "peak_hbm_bytes", "budget_bytes", "max_running")
-        return dict(zip(keys, [v[i] for i in range(6)]))
+        v = (ctypes.c_double * 8)()
+        lib().p3dfft_gb300_server_stats(self.handle, v, 8)
+        keys = ("completed", "failed", "admitted", "peak_hbm_bytes", "budget_bytes", "max_running",
+                "host_launch_s", "host_release_s")
+        return dict(zip(keys, [v[i] for i in range(8)]))
 
     def close(self):
         if getattr(self, "handle", -1) >= 0 and _lib is not None:
