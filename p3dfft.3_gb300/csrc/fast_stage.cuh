@@ -158,6 +158,12 @@ __host__ __device__ constexpr int fast_ls() {
   return best;
 }
 
+// 1: values are normalised before every shared-memory store between passes (float-float: one
+// Fast2Sum per component); 0: stored as computed (the next pass's TwoSum adds accept them)
+#ifndef FAST_STORE_NORM
+#define FAST_STORE_NORM 1
+#endif
+
 // 1: twiddles of the Stockham passes from the per-pass tables below; 0: from the length-N table
 #ifndef FAST_PASS_TABLES
 #define FAST_PASS_TABLES 1
@@ -211,8 +217,11 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
     for (int b = 0; b < NB; b++) {
       const int jj = j + b * T;
       if (GUARD && jj >= M) break;
+      // padded slots: pad(jj + r M) = pad(jj) + r (M + M/2^PS) when M is a multiple of 2^PS
+      const int pj = pad<PS>(jj);
 #pragma unroll
-      for (int r = 0; r < R; r++) v[b * R + r] = line[pad<PS>(jj + r * M)];
+      for (int r = 0; r < R; r++)
+        v[b * R + r] = line[(M % (1 << PS) == 0) ? pj + r * (M + (M >> PS)) : pad<PS>(jj + r * M)];
       if constexpr (Ns > 1) {
 #if FAST_PASS_TABLES
         const typename O::T *pt = ptab + fast_pass_offset(N, I) + jj % Ns;
@@ -255,8 +264,17 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       if (GUARD && jj >= M) break;
       const int k = jj % Ns;
       const int base = (jj - k) * R + k;
+      // pad(base + r Ns) = pad(base) + r (Ns + Ns/2^PS) for Ns a multiple of 2^PS, and
+      // pad(base) + r in the first pass when R is a power of two up to 2^PS (base = jj R then
+      // stays in one padding block)
+      constexpr bool NS_AL = Ns % (1 << PS) == 0;
+      constexpr bool FIRST_AL = Ns == 1 && (R & (R - 1)) == 0 && R <= (1 << PS);
+      const int pb = pad<PS>(base);
 #pragma unroll
-      for (int r = 0; r < R; r++) line[pad<PS>(base + r * Ns)] = O::norm(v[b * R + r]);
+      for (int r = 0; r < R; r++) {
+        const int slot = NS_AL ? pb + r * (Ns + (Ns >> PS)) : (FIRST_AL ? pb + r : pad<PS>(base + r * Ns));
+        line[slot] = FAST_STORE_NORM ? O::norm(v[b * R + r]) : v[b * R + r];
+      }
     }
   }
   __syncthreads();
@@ -273,6 +291,19 @@ __device__ __forceinline__ void fk_for(F &&f) {
     for (int u = 0; u < UU; u++)
       if (V % UU == 0 || e0 + u < V) f(e0 + u);
   }
+}
+
+// Padded slot of point j0 + e*TT given pj0 = pad(j0): constant steps when TT is a multiple of 2^PS.
+template <int PS, int TT>
+__device__ __forceinline__ int fk_slot(int j0, int pj0, int e) {
+  if constexpr (TT % (1 << PS) == 0) return pj0 + e * (TT + (TT >> PS));
+  else return pad<PS>(j0 + e * TT);
+}
+// Padded slot of point N - (j0 + e*TT) given pn = pad(N - j0), for 0 < j0 + e*TT <= N.
+template <int PS, int TT, int N>
+__device__ __forceinline__ int fk_slot_rev(int j0, int pn, int e) {
+  if constexpr (TT % (1 << PS) == 0 && N % (1 << PS) == 0) return pn - e * (TT + (TT >> PS));
+  else return pad<PS>(N - j0 - e * TT);
 }
 
 template <class O>
@@ -361,8 +392,10 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
         if constexpr (R0 == 3) dft3<O>(x, fsign, O::tw(tab, (N / 3) * TWSTEP));
         else if constexpr (R0 == 5) dft5<O>(x, fsign, O::tw(tab, (N / 5) * TWSTEP), O::tw(tab, 2 * (N / 5) * TWSTEP));
         else dft_p2<O, R0>(x, fsign);
+        const int pb = pad<PS>(j0 * R0);
 #pragma unroll
-        for (int r = 0; r < R0; r++) lb[pad<PS>(j0 * R0 + r)] = O::norm(x[r]);
+        for (int r = 0; r < R0; r++)
+          lb[((R0 & (R0 - 1)) == 0 && R0 <= (1 << PS)) ? pb + r : pad<PS>(j0 * R0 + r)] = O::norm(x[r]);
       }
       __syncthreads();
       if constexpr (RL.n > 1) fk_pass<O, N, TWSTEP, R0, 1>(lb, tab, ptab, j0, act, fsign);
@@ -374,10 +407,12 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
     // are converted in place once the block-wide largest exponent is known.
     RAW *lr = reinterpret_cast<RAW *>(lb);
     int emax = 0;
+    const int pj0 = pad<PS>(j0);
     if (act) {
       const G *src = gin + (KIND == FK_R2C ? ibase : 2 * ibase);
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int j = j0 + e * TT;
+        const int sj = fk_slot<PS, TT>(j0, pj0, e);
         RAW r;
         if (KIND == FK_R2C) {  // packed z[j] = x[2j] + i x[2j+1]
           if (p.iL == 1) r = O::ldraw(src + 2 * j);
@@ -387,9 +422,9 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
         }
         if (O::SCALED) {
           emax = max(emax, O::rexp(r));
-          lr[pad<PS>(j)] = r;
+          lr[sj] = r;
         } else {
-          lb[pad<PS>(j)] = O::from_raw(r, 0);
+          lb[sj] = O::from_raw(r, 0);
         }
       });
       if (KIND == FK_C2R && j0 == 0) {
@@ -414,7 +449,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
       sc = 1043 - emax;
       if (act && KIND != FK_C2R) {
         fk_for<V, O::IO_UNROLL>([&](int e) {
-          const int j = pad<PS>(j0 + e * TT);
+          const int j = fk_slot<PS, TT>(j0, pj0, e);
           lb[j] = O::from_raw(lr[j], sc);
         });
       }
@@ -425,15 +460,17 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
       C z[V];
       if (act) {
 #pragma unroll
+        const int pn0 = pad<PS>(N - j0);
         for (int e = 0; e < V; e++) {
           const int k = j0 + e * TT;
+          const int sa = fk_slot<PS, TT>(j0, pj0, e), sb = fk_slot_rev<PS, TT, N>(j0, pn0, e);
           C a, b;
           if (O::SCALED) {
-            a = O::from_raw(lr[pad<PS>(k)], sc);
-            b = O::from_raw(lr[pad<PS>(N - k)], sc);
+            a = O::from_raw(lr[sa], sc);
+            b = O::from_raw(lr[sb], sc);
           } else {
-            a = lb[pad<PS>(k)];
-            b = lb[pad<PS>(N - k)];
+            a = lb[sa];
+            b = lb[sb];
           }
           if (k == 0) {
             a.y = O::rzero();
@@ -448,7 +485,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
       __syncthreads();
       if (act) {
 #pragma unroll
-        for (int e = 0; e < V; e++) lb[pad<PS>(j0 + e * TT)] = z[e];
+        for (int e = 0; e < V; e++) lb[fk_slot<PS, TT>(j0, pj0, e)] = z[e];
       }
     }
     __syncthreads();
@@ -464,13 +501,15 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
     if (sact) {
       const C *Y = buf + (size_t)ls * LS;
       const long long obase = (long long)(gs % p.dt) * p.ot + (long long)(gs / p.dt) * p.oo;
+      const int pjs = pad<PS>(js), pns = pad<PS>(N - js);
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int k = js + e * TT;
+        const int sk = fk_slot<PS, TT>(js, pjs, e);
         if (KIND == FK_C2C) {
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[pad<PS>(k)], k), sc_out));
+          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[sk], k), sc_out));
         } else if (KIND == FK_R2C) {
           // X[k] = 1/2 [(Z_k + conj Z_{N-k}) - i W_2N^k (Z_k - conj Z_{N-k})]
-          C a = Y[pad<PS>(k)], b = O::conj(Y[pad<PS>(k == 0 ? 0 : N - k)]);
+          C a = Y[sk], b = O::conj(Y[k == 0 ? 0 : fk_slot_rev<PS, TT, N>(js, pns, e)]);
           C s = O::add(a, b), d = O::sub(a, b);
           C x = O::half(O::sub(s, O::muli(O::mul(O::tw(tab, k), d))));
           O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
@@ -480,7 +519,7 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
             O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc_out));
           }
         } else {  // C2R: reals 2k, 2k+1 = z[k]
-          RAW r = O::to_raw(Y[pad<PS>(k)], sc_out);
+          RAW r = O::to_raw(Y[sk], sc_out);
           if (p.oL == 1) O::straw(gout + obase + 2 * k, r);
           else O::straw2(gout + obase + (long long)(2 * k) * p.oL, gout + obase + (long long)(2 * k + 1) * p.oL, r);
         }
