@@ -55,6 +55,48 @@ def dist_env():
     return rank, world, local
 
 
+class Replicas:
+    """Independent replicas, one process per GPU (the path has no inter-GPU exchange): a barrier
+    and max-over-ranks timing through torch.distributed (NCCL on GPUs, gloo on CPU hosts)."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.torch = self.tdist = None
+        self.dev = "cpu"
+        if self.world > 1:
+            import torch
+            import torch.distributed as tdist
+            use_cuda = torch.cuda.is_available()
+            if use_cuda:
+                torch.cuda.set_device(self.local)
+                self.dev = "cuda"
+            tdist.init_process_group("nccl" if use_cuda else "gloo")
+            self.torch, self.tdist = torch, tdist
+
+    def barrier(self):
+        if self.tdist:
+            if self.dev == "cuda":
+                self.torch.cuda.synchronize()
+            self.tdist.barrier()
+
+    def _reduce(self, v, op):
+        if not self.tdist:
+            return v
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64, device=self.dev)
+        self.tdist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, v):
+        return self._reduce(v, self.tdist.ReduceOp.MAX if self.tdist else None)
+
+    def sum(self, v):
+        return self._reduce(v, self.tdist.ReduceOp.SUM if self.tdist else None)
+
+    def close(self):
+        if self.tdist:
+            self.tdist.destroy_process_group()
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -540,15 +582,7 @@ def main():
     import build_lib
     build_lib.build()
     L = p3d.lib()
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as tdist
-        torch.cuda.set_device(local)
-        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        dist = (torch, tdist)
-    else:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", "0"))
+    reps = Replicas()
 
     arith = 0 if args.arith == "native" else 1
     p3d.set_fp64_arith(arith)
@@ -564,17 +598,8 @@ def main():
         p3d.check(L.p3dfft_gb300_exec3d(f.handle, ctypes.c_void_p(fin), ctypes.c_void_p(d_spec.ptr), IDIR, 0))
         p3d.check(L.p3dfft_gb300_exec3d(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(fout), -1, 0))
 
-    def barrier():
-        if dist:
-            dist[0].cuda.synchronize()
-            dist[1].barrier()
-
-    def max_over_ranks(v):
-        if not dist:
-            return v
-        t = dist[0].tensor([v], dtype=dist[0].float64, device="cuda")
-        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
-        return float(t.item())
+    barrier = reps.barrier
+    max_over_ranks = reps.max
 
     # ---- device-resident timed region ----
     p3d.set_sync(False)
@@ -717,8 +742,7 @@ def main():
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist[1].destroy_process_group()
+    reps.close()
 
 
 if __name__ == "__main__":
