@@ -300,8 +300,8 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
     for gd, prec in set(jobs) | {(gd, 8) for gd, _ in jobs}:
         plan_pair(gd, prec)
 
-    def make_batch(items, graph=True):
-        bt = p3d.Batch(nbranches=nbranches, graph=graph)
+    def make_batch(items, graph=True, grouped=True):
+        bt = p3d.Batch(nbranches=nbranches, graph=graph, grouped=grouped)
         for j, (gd, prec, (d_x, d_s, d_y)) in enumerate(items):
             f, b = plan_pair(gd, prec)
             bt.add(j, f, d_x, d_s)
@@ -337,6 +337,8 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
     ms_b64, _ = time_batch(b_f64)
     b_nog = make_batch(mixed, graph=False)
     ms_nog, _ = time_batch(b_nog)
+    b_br = make_batch(mixed, grouped=False)
+    ms_br, k_br = time_batch(b_br)
 
     # 48 sequential plain FP64 calls: the reference-style synchronous exec, one job after another
     p3d.set_sync(True)
@@ -368,7 +370,10 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
         "jobs": n, "seed": seed, "branches": nbranches, "mix": hist,
         "batch_graph_mixed": {"ms": ms_mixed, "round_trips_per_s": n / (ms_mixed * 1e-3),
                               "GB_per_s": alg_mixed / (ms_mixed * 1e-3) / 1e9, "kernels_per_exec": k_mixed,
-                              "graph_launches_per_exec": 1},
+                              "grouped_launches": b_mixed.groups(), "graph_launches_per_exec": 1,
+                              "mode": "grouped: one launch per (cohort of same-plan jobs, stage) over all their tiles; cohorts on concurrent streams"},
+        "batch_graph_branches_mixed": {"ms": ms_br, "round_trips_per_s": n / (ms_br * 1e-3), "kernels_per_exec": k_br,
+                                       "mode": f"{nbranches} concurrent branch streams, one launch per stage"},
         "batch_graph_all_fp64": {"ms": ms_b64, "round_trips_per_s": n / (ms_b64 * 1e-3),
                                  "GB_per_s": alg_plain / (ms_b64 * 1e-3) / 1e9},
         "batch_streams_no_graph_mixed": {"ms": ms_nog, "round_trips_per_s": n / (ms_nog * 1e-3)},
@@ -379,7 +384,7 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
         "autotune": {"seconds": t_tune, "engines": "1 specialised, 2 register, 3 generic; [engine, alt tile dim, ms]",
                      "choices": tuning},
     }
-    for bt in (b_mixed, b_f64, b_nog):
+    for bt in (b_mixed, b_f64, b_nog, b_br):
         del bt
     return out
 

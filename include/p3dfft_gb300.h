@@ -107,14 +107,21 @@ long long p3dfft_gb300_noalloc_max_field_bytes(void);
 
 /* ---- batched execution of independent transforms (no counterpart in the reference) ----
  * A batch holds jobs; a job is an ordered list of steps (3D plan, device in, device out, idir), e.g. an
- * R2C forward then its C2R backward.  Jobs are independent: they are spread over `nbranches`
- * concurrent streams (0 = 8), each with its own scratch fields.  The first batch_exec runs the
+ * R2C forward then its C2R backward.  Jobs are independent: by default they run as grouped
+ * launches (see batch_set_grouped), else on `nbranches` concurrent streams (0 = 8), each with its
+ * own scratch fields.  The first batch_exec runs the
  * jobs and records them into one CUDA graph; later execs replay the graph with one launch on the
  * library stream.  Pointers are captured: keep the buffers allocated while the batch exists.
  * batch_add after an exec, a change of FP64 arithmetic or batch_set_graph re-records the graph. */
 int p3dfft_gb300_batch_create(int nbranches);
 int p3dfft_gb300_batch_add(int batch, int job, int plan, const void *in, void *out, int idir);
 int p3dfft_gb300_batch_set_graph(int batch, int on);
+/* 1 (default): jobs with the same steps form a cohort; each stage of a cohort is one launch of its
+ * specialised kernel over all the cohort's jobs' tiles; cohorts run on `nbranches` concurrent
+ * streams.  0: every job's stages launched separately, jobs spread over the streams. */
+int p3dfft_gb300_batch_set_grouped(int batch, int on);
+/* grouped launches one exec makes (0 in branch mode) */
+int p3dfft_gb300_batch_groups(int batch);
 int p3dfft_gb300_batch_exec(int batch);
 /* kernels one batch_exec launches, and the field bytes its steps read and write */
 long long p3dfft_gb300_batch_kernels(int batch);

@@ -2,12 +2,17 @@
 // transform3D::exec runs one transform per call, build/exec.C:101-223).
 //
 // A batch is a set of jobs; a job is an ordered list of (plan, in, out, idir) steps on device
-// memory, e.g. an R2C forward followed by the C2R backward.  Jobs are spread over branch streams
-// by a longest-processing-time-first assignment on their HBM bytes; each branch owns one scratch
-// set, sized for the largest plan it runs, so jobs of a branch reuse it one after another.
+// memory, e.g. an R2C forward followed by the C2R backward.  Two ways to run them:
+//   - grouped (default): jobs with the same steps form a cohort, and each stage of a cohort runs
+//     as ONE launch of its specialised kernel over the tiles of all the cohort's jobs, so the
+//     batch is a few large launches instead of many small ones; cohorts run concurrently on the
+//     branch streams.  Each job has its own scratch set.
+//   - branches: jobs are spread over branch streams by a longest-processing-time-first
+//     assignment on their HBM bytes; each branch owns one scratch set, sized for the largest plan
+//     it runs, and runs its jobs one after another.
 // The first exec runs the jobs eagerly (this resolves twiddle tables and scratch), then records
-// the whole fork / branches / join structure into one CUDA graph; every later exec is a single
-// cudaGraphLaunch on the library stream.
+// the whole structure into one CUDA graph; every later exec is a single cudaGraphLaunch on the
+// library stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,6 +44,11 @@ struct Batch {
   cudaStream_t origin = nullptr;
   cudaGraphExec_t gexec = nullptr;
   bool use_graph = true;
+  bool grouped = true;          // level-synchronous grouped launches (else one stream per branch)
+  std::vector<void *> job_sets;          // grouped mode: one scratch set per job
+  std::vector<LaunchSet *> lsets;         // grouped mode: one launch set per cohort
+  std::vector<std::vector<int>> cassign;  // grouped mode: branch -> cohorts
+  int ngroups = 0;
   bool dirty = true;
   int arith = -1;
   long long kernels = 0;  // kernels one exec launches
@@ -46,6 +56,8 @@ struct Batch {
 
   ~Batch() {
     if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto l : lsets) launch_set_destroy(l);
+    for (auto p : job_sets) scratch_set_destroy(p);
     for (auto s : br) cudaStreamDestroy(s);
     for (auto e : join) cudaEventDestroy(e);
     for (auto p : sets) scratch_set_destroy(p);
@@ -111,6 +123,7 @@ static int prepare(Batch *B) {
     load[k] += w.first;
     B->assign[k].push_back(w.second);
   }
+  if (B->grouped) return E_OK;  // grouped mode gives every job its own scratch set instead
   for (int b = 0; b < B->nbr; b++) {
     size_t need = 0;
     for (int j : B->assign[b]) need = std::max(need, scratch_of_job[j]);
@@ -119,8 +132,112 @@ static int prepare(Batch *B) {
   return E_OK;
 }
 
+// Grouped mode.  Jobs with the same steps (plans and derivative directions) form a cohort; every
+// job's stages are recorded with their buffers (each job has its own scratch set, since a
+// cohort's jobs are in flight together), and for each stage the cohort's jobs run as ONE launch
+// of the stage's specialised kernel over all their tiles.  Cohorts are independent: they are
+// spread over the branch streams by longest-processing-time first, with no barrier between them.
+// Measured on GB300: a shared launch helps jobs too small to fill the GPU (e.g. 16 x 64^3 FP64:
+// 0.153 vs 0.160 ms) and costs large ones their overlap with other streams (8 x 256^3 FP32:
+// 1.49 vs 1.24 ms), hence the size limit below.
+static int prepare_grouped(Batch *B) {
+  for (auto l : B->lsets) launch_set_destroy(l);
+  B->lsets.clear();
+  B->ngroups = 0;
+  // record every job; its cohort key is the sequence of its stages' descriptions (kind, grids,
+  // strides, precision, arithmetic, derivative) without the buffers, so equal plans made
+  // separately still share launches
+  std::map<std::vector<long long>, std::vector<std::pair<int, std::vector<StageLaunch>>>> cohorts;
+  std::map<int, double> job_bytes;
+  size_t js = 0;
+  for (auto &kv : B->jobs) {
+    if (js >= B->job_sets.size()) B->job_sets.push_back(scratch_set_create());
+    std::vector<StageLaunch> rec;
+    double w = 0;
+    for (auto &s : kv.second) {
+      const int rc = record_plan(s.plan, s.in, s.out, s.idir, B->job_sets[js], &rec);
+      if (rc != E_OK) return rc;
+      size_t ib = 0, ob = 0;
+      plan3d_sizes(s.plan, &ib, &ob, nullptr, nullptr);
+      w += (double)ib + (double)ob;
+    }
+    js++;
+    std::vector<long long> key;
+    for (auto &r : rec) {
+      const StageDesc &d = r.d;
+      for (long long v : {(long long)d.kind, (long long)d.r2r, (long long)d.prec, (long long)d.dt1, (long long)d.dt2,
+                          (long long)d.L, (long long)d.deriv, (long long)d.engine, (long long)d.talt,
+                          (long long)r.arith})
+        key.push_back(v);
+      for (int i = 0; i < 3; i++) {
+        key.push_back(d.d1[i]);
+        key.push_back(d.d2[i]);
+        key.push_back(d.s1[i]);
+        key.push_back(d.s2[i]);
+      }
+    }
+    cohorts[key].push_back({kv.first, rec});
+    job_bytes[kv.first] = w;
+  }
+  // Jobs large enough to fill the GPU on their own (>= 24 MB of steps' fields) gain nothing from a
+  // shared launch and run better spread over the streams: they form cohorts of one.
+  std::vector<std::vector<std::pair<int, std::vector<StageLaunch>>>> groups;
+  for (auto &c : cohorts) {
+    if (c.second.size() > 1 && job_bytes[c.second[0].first] >= 24.0 * (1 << 20)) {
+      for (auto &jr : c.second) groups.push_back({jr});
+    } else {
+      groups.push_back(c.second);
+    }
+  }
+  std::vector<std::pair<double, int>> work;
+  for (auto &c : groups) {
+    std::vector<std::vector<StageLaunch>> levels;
+    double w = 0;
+    for (auto &jr : c) {
+      const std::vector<StageLaunch> &rec = jr.second;
+      w += job_bytes[jr.first];
+      if (levels.size() < rec.size()) levels.resize(rec.size());
+      for (size_t k = 0; k < rec.size(); k++) levels[k].push_back(rec[k]);
+    }
+    int err = E_OK;
+    LaunchSet *ls = launch_set_build(levels, device_tables(), &err);
+    if (!ls) return fail(err ? err : E_CUDA, "batch: grouped launch set could not be built");
+    B->ngroups += launch_set_groups(ls);
+    work.push_back({w, (int)B->lsets.size()});
+    B->lsets.push_back(ls);
+  }
+  std::sort(work.begin(), work.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+    return a.first > b.first || (a.first == b.first && a.second < b.second);
+  });
+  B->cassign.assign(B->nbr, {});
+  std::vector<double> load(B->nbr, 0.0);
+  for (auto &w : work) {
+    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[k] += w.first;
+    B->cassign[k].push_back(w.second);
+  }
+  return E_OK;
+}
+
+static int run_grouped(Batch *B, cudaStream_t st) {
+  int launched = 0, rc = E_OK;
+  if (cudaEventRecord(B->fork, st) != cudaSuccess) return fail(E_CUDA, "batch: fork event failed");
+  for (int b = 0; b < B->nbr; b++) {
+    if (B->cassign[b].empty()) continue;
+    if (cudaStreamWaitEvent(B->br[b], B->fork, 0) != cudaSuccess) return fail(E_CUDA, "batch: fork wait failed");
+    for (int c : B->cassign[b])
+      if (rc == E_OK) rc = launch_set_run(B->lsets[c], B->br[b], &launched);
+    if (cudaEventRecord(B->join[b], B->br[b]) != cudaSuccess || cudaStreamWaitEvent(st, B->join[b], 0) != cudaSuccess)
+      return fail(E_CUDA, "batch: join failed");
+  }
+  add_kernel_count(launched);
+  if (rc != E_OK) return fail(rc, "batch: grouped launch failed");
+  return E_OK;
+}
+
 // fork from `st`, run every branch's jobs, join back into `st`
 static int run_branches(Batch *B, cudaStream_t st, bool capturing) {
+  if (B->grouped) return run_grouped(B, st);
   if (cudaEventRecord(B->fork, st) != cudaSuccess) return fail(E_CUDA, "batch: fork event failed");
   int rc = E_OK;
   for (int b = 0; b < B->nbr; b++) {
@@ -218,6 +335,19 @@ int p3dfft_gb300_batch_set_graph(int batch, int on) {
   return E_OK;
 }
 
+int p3dfft_gb300_batch_set_grouped(int batch, int on) {
+  Batch *B = get_batch(batch);
+  if (!B) return fail(E_BAD_ARG, "batch: invalid handle");
+  B->grouped = on != 0;
+  B->dirty = true;
+  return E_OK;
+}
+
+int p3dfft_gb300_batch_groups(int batch) {
+  Batch *B = get_batch(batch);
+  return B ? (B->grouped ? B->ngroups : 0) : -1;
+}
+
 int p3dfft_gb300_batch_exec(int batch) {
   Batch *B = get_batch(batch);
   if (!B) return fail(E_BAD_ARG, "batch: invalid handle");
@@ -228,6 +358,10 @@ int p3dfft_gb300_batch_exec(int batch) {
   if (B->dirty || ar != B->arith || (B->use_graph && !B->gexec)) {
     int rc = prepare(B);
     if (rc != E_OK) return rc;
+    if (B->grouped) {
+      rc = prepare_grouped(B);
+      if (rc != E_OK) return rc;
+    }
     const long long k0 = kernel_count_now();
     rc = run_branches(B, st, false);  // eager run: resolves tables, produces this call's results
     if (rc != E_OK) return rc;

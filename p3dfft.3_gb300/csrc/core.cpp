@@ -204,7 +204,8 @@ static int g_sync = 1;
 struct ExecCtx {
   cudaStream_t st;
   Buffers *buf;
-  bool capturing;  // no synchronising call may be made
+  bool capturing;                  // no synchronising call may be made
+  std::vector<StageLaunch> *rec;   // non-null: record the stages instead of launching them
 };
 static thread_local const ExecCtx *t_ctx = nullptr;
 static cudaStream_t cur_stream() { return t_ctx ? t_ctx->st : g_stream; }
@@ -642,6 +643,15 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
 static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv,
                      const void *tw_given = nullptr, const void *aux_given = nullptr) {
   const TypeInfo &t = g_types[s.type];
+  if (t_ctx && t_ctx->rec) {  // recording for a grouped launch set
+    StageLaunch sl;
+    fill_stage_desc(P, s, deriv, sl.d);
+    sl.src = src;
+    sl.dst = dst;
+    sl.arith = P->prec == 8 ? arith_mode() : AR_NATIVE;
+    t_ctx->rec->push_back(sl);
+    return E_OK;
+  }
   int launched = 0;
   int rc = E_OK;
   if (t.kind == K_EMPTY) {
@@ -951,6 +961,9 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
       rc = run_stage_slabs(P, st, sd_in, in, din, d, deriv, 0);
     } else if (s == n - 1 && sd_out >= 0) {
       rc = run_stage_slabs(P, st, sd_out, out, src, d, deriv, 1);
+    } else if (d == src && t_ctx && t_ctx->rec) {
+      set_err(E_UNSUPPORTED, "an in-place single-stage plan cannot be recorded for a grouped launch");
+      return E_UNSUPPORTED;
     } else if (d == src) {  // single-stage in-place call: go through scratch, then copy back
       size_t bytes = stage_out_bytes(P, st);
       if ((in_capture() || !B.owned) && (bytes > B.scratch_bytes || !B.scratch[0])) {
@@ -1156,13 +1169,29 @@ int exec_plan_on(int plan, const void *in, void *out, int idir, cudaStream_t st,
     set_err(E_BAD_ARG, "derivative direction %d out of range", idir);
     return E_BAD_ARG;
   }
-  ExecCtx ctx{st, static_cast<Buffers *>(scratch_set), capturing};
+  ExecCtx ctx{st, static_cast<Buffers *>(scratch_set), capturing, nullptr};
   const ExecCtx *prev = t_ctx;
   t_ctx = &ctx;
   int rc = exec_plan(P, in, out, idir, 0);
   t_ctx = prev;
   return rc;
 }
+
+int record_plan(int plan, const void *in, void *out, int idir, void *scratch_set, std::vector<StageLaunch> *rec) {
+  Plan *P = get_plan(g_plans3, plan);
+  if (!P) {
+    set_err(E_BAD_ARG, "invalid 3D plan handle %d", plan);
+    return E_BAD_ARG;
+  }
+  ExecCtx ctx{g_stream, static_cast<Buffers *>(scratch_set), false, rec};
+  const ExecCtx *prev = t_ctx;
+  t_ctx = &ctx;
+  int rc = exec_plan(P, in, out, idir, 0);
+  t_ctx = prev;
+  return rc;
+}
+
+DeviceTables *device_tables() { return g_tabs; }
 
 bool device_ready() { return ensure_device(); }
 cudaStream_t library_stream() { return g_stream; }

@@ -17,7 +17,7 @@ using FastArith = Native<float>;
 #endif
 
 template <>
-int fast_launch_kind<FastArith, P3D_FAST_KIND>(int n, const FParams &p, cudaStream_t st) {
-  return fk_dispatch_n<FastArith, P3D_FAST_KIND>(n, p, st);
+int fast_launch_kind<FastArith, P3D_FAST_KIND>(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
+  return fk_dispatch_n<FastArith, P3D_FAST_KIND>(n, p, g, ctas, st);
 }
 }  // namespace p3d

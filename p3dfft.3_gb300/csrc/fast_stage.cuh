@@ -319,8 +319,17 @@ __host__ __device__ constexpr int fast_min_blocks() {
                                     : FastShape<N>::MINB;
 }
 
+// A launch over the tiles of several stages that are the same but for their buffers (same
+// kernel, grids, strides and tables) from independent transforms: CTA b works on tile
+// b mod ntotal of stage b / ntotal, whose input and output are io[2j], io[2j+1].
+struct FGroup {
+  const void *const *io;  // 2 nj buffer addresses (device memory)
+  int nj;
+};
+
+// One tile of one stage (the body of k_fast and k_fast_group).
 template <class O, int KIND, int N>
-__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast(FParams p) {
+__device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const void *in, void *out) {
   using C = typename O::C;
   using T = typename O::T;
   using G = typename O::G;
@@ -354,12 +363,12 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
     ls = threadIdx.x % TB;
     js = threadIdx.x / TB;
   }
-  const G *gin = reinterpret_cast<const G *>(p.in);
-  G *gout = reinterpret_cast<G *>(p.out);
+  const G *gin = reinterpret_cast<const G *>(in);
+  G *gout = reinterpret_cast<G *>(out);
 
   // One tile per CTA: a persistent loop over tiles was measured to keep ~80 more registers live.
   {
-    const int g0 = blockIdx.x * TB;
+    const int g0 = tile * TB;
     const int gl = g0 + l;
     const bool act = valid && gl < p.nlines;
     const int lt = gl % p.dt, lo = gl / p.dt;
@@ -529,6 +538,17 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
   }
 }
 
+template <class O, int KIND, int N>
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast(FParams p) {
+  fk_tile<O, KIND, N>(p, blockIdx.x, p.in, p.out);
+}
+
+template <class O, int KIND, int N>
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast_group(FParams p, FGroup g) {
+  const int j = (int)blockIdx.x / p.ntotal;
+  fk_tile<O, KIND, N>(p, (int)blockIdx.x - j * p.ntotal, g.io[2 * j], const_cast<void *>(g.io[2 * j + 1]));
+}
+
 // ------------------------------------------------------------------------------------------
 // host side
 struct FastArgs {
@@ -550,6 +570,8 @@ static int fk_configure() {
   static bool configured = false;
   if (!configured) {
     if (cudaFuncSetAttribute(k_fast<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fk_smem<O, KIND, N>()) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fast_group<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)fk_smem<O, KIND, N>()) != cudaSuccess)
       return E_CUDA;
     configured = true;
@@ -558,16 +580,22 @@ static int fk_configure() {
 }
 
 template <class O, int KIND, int N>
-static int fk_launch(const FParams &p, cudaStream_t st) {
+static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
   if (fk_configure<O, KIND, N>() != E_OK) return E_CUDA;
-  if (p.ntotal <= 0) return E_OK;
-  k_fast<O, KIND, N><<<(unsigned)p.ntotal, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(p);
+  if (g) {
+    if (ctas <= 0) return E_OK;
+    k_fast_group<O, KIND, N><<<(unsigned)ctas, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(p, *g);
+  } else {
+    if (p.ntotal <= 0) return E_OK;
+    k_fast<O, KIND, N><<<(unsigned)p.ntotal, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(p);
+  }
   return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
 }
 
-// n > 0: launch the length-n kernel; n == 0: configure (load) every length's kernel
+// n > 0: launch the length-n kernel (one stage, or a group of stages when g is set);
+// n == 0: configure (load) every length's kernels
 template <class O, int KIND>
-static int fk_dispatch_n(int n, const FParams &p, cudaStream_t st) {
+static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
   if (n == 0) {
     int rc = E_OK;
 #define P3D_FAST_CASE(L) \
@@ -578,7 +606,7 @@ static int fk_dispatch_n(int n, const FParams &p, cudaStream_t st) {
   }
   switch (n) {
 #define P3D_FAST_CASE(L) \
-  case L: return fk_launch<O, KIND, L>(p, st);
+  case L: return fk_launch<O, KIND, L>(p, g, ctas, st);
     P3D_FAST_LENGTHS(P3D_FAST_CASE)
 #undef P3D_FAST_CASE
     default: return E_UNSUPPORTED;
@@ -587,23 +615,27 @@ static int fk_dispatch_n(int n, const FParams &p, cudaStream_t st) {
 
 // One (arithmetic, kind) pair per translation unit (fast_inst.cu), so they compile in parallel.
 template <class O, int KIND>
-int fast_launch_kind(int n, const FParams &p, cudaStream_t st);
-template <> int fast_launch_kind<DF, FK_C2C>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<DF, FK_R2C>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<DF, FK_C2R>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<Native<double>, FK_C2C>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<Native<double>, FK_R2C>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<Native<double>, FK_C2R>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<Native<float>, FK_C2C>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<Native<float>, FK_R2C>(int, const FParams &, cudaStream_t);
-template <> int fast_launch_kind<Native<float>, FK_C2R>(int, const FParams &, cudaStream_t);
+int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st);
+#define P3D_FAST_DECL(O, K) \
+  template <>               \
+  int fast_launch_kind<O, K>(int, const FParams &, const FGroup *, int, cudaStream_t);
+P3D_FAST_DECL(DF, FK_C2C)
+P3D_FAST_DECL(DF, FK_R2C)
+P3D_FAST_DECL(DF, FK_C2R)
+P3D_FAST_DECL(Native<double>, FK_C2C)
+P3D_FAST_DECL(Native<double>, FK_R2C)
+P3D_FAST_DECL(Native<double>, FK_C2R)
+P3D_FAST_DECL(Native<float>, FK_C2C)
+P3D_FAST_DECL(Native<float>, FK_R2C)
+P3D_FAST_DECL(Native<float>, FK_C2R)
+#undef P3D_FAST_DECL
 
 template <class O>
-inline int fast_launch_arith(const FastArgs &a, cudaStream_t st) {
+inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaStream_t st) {
   switch (a.kind) {
-    case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, st);
-    case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, st);
-    case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, st);
+    case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, g, ctas, st);
+    case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, g, ctas, st);
+    case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, g, ctas, st);
     default: return E_UNSUPPORTED;
   }
 }
@@ -616,19 +648,21 @@ inline int fast_preload(int prec, int arith) {
     a.kind = k;
     a.n = 0;
     int r;
-    if (prec == 4) r = fast_launch_arith<Native<float>>(a, 0);
-    else if (arith == AR_DF) r = fast_launch_arith<DF>(a, 0);
-    else r = fast_launch_arith<Native<double>>(a, 0);
+    if (prec == 4) r = fast_launch_arith<Native<float>>(a, nullptr, 0, 0);
+    else if (arith == AR_DF) r = fast_launch_arith<DF>(a, nullptr, 0, 0);
+    else r = fast_launch_arith<Native<double>>(a, nullptr, 0, 0);
     if (r != E_OK) rc = r;
   }
   return rc;
 }
 
-// prec 4: FP32; prec 8: float-float (arith AR_DF) or native FP64
-inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st) {
-  if (prec == 4) return fast_launch_arith<Native<float>>(a, st);
-  if (arith == AR_DF) return fast_launch_arith<DF>(a, st);
-  return fast_launch_arith<Native<double>>(a, st);
+// prec 4: FP32; prec 8: float-float (arith AR_DF) or native FP64.  With g set, one launch of
+// `ctas` CTAs covers the group of stages g describes (a.kind and a.n select the kernel).
+inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, const FGroup *g = nullptr,
+                       int ctas = 0) {
+  if (prec == 4) return fast_launch_arith<Native<float>>(a, g, ctas, st);
+  if (arith == AR_DF) return fast_launch_arith<DF>(a, g, ctas, st);
+  return fast_launch_arith<Native<double>>(a, g, ctas, st);
 }
 
 inline bool fast_supported(int n) {

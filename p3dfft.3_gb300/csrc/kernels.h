@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace p3d {
 
 // 1D transform kinds (the reference's trans_type1D flavours, build/init.C:121-731)
@@ -69,9 +71,34 @@ void fill_pass_table(int N, int fmt, void *host_dst);
 // Tables come from `tabs` (allocated on first use) unless `tw_given` is non-null, in which case
 // tw_given / aux_given are used as they are.  With `tabs_out` non-null nothing is launched: the
 // call only reports the tables the stage needs.
+struct FastArgs;  // a specialised-kernel launch (fast_stage.cuh)
+// With `fast_prep` non-null nothing is launched either: when the stage runs on a specialised
+// kernel its launch is described in *fast_prep and E_OK returned, otherwise E_UNSUPPORTED.
 int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
                  DeviceTables *tabs, int *kernels_launched, const void *tw_given = nullptr,
-                 const void *aux_given = nullptr, TableNeed *tabs_out = nullptr);
+                 const void *aux_given = nullptr, TableNeed *tabs_out = nullptr, FastArgs *fast_prep = nullptr);
+
+// ---- grouped launches (batch runtime) ----
+// One stage of one transform with its buffers, as the executor would launch it.
+struct StageLaunch {
+  StageDesc d;
+  const void *src;
+  void *dst;
+  int arith;
+};
+// levels[k] holds the k-th stage of every transform of a set (e.g. a batch cohort).  A launch set
+// runs level after level on one stream; within a level, stages that differ only in their buffers
+// and run on a specialised kernel become one grouped launch over all their tiles, the others one
+// launch each.  Building uploads the groups' buffer addresses.
+struct LaunchSet;
+LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err);
+int launch_set_run(LaunchSet *set, cudaStream_t stream, int *kernels_launched);
+// the launches of level l, largest first (items 0 .. launch_set_items(set, l) - 1)
+int launch_set_levels(const LaunchSet *set);
+int launch_set_items(const LaunchSet *set, int level);
+int launch_set_run_item(LaunchSet *set, int level, int item, cudaStream_t stream, int *kernels_launched);
+int launch_set_groups(const LaunchSet *set);
+void launch_set_destroy(LaunchSet *set);
 // Pure permutation copy of an element size `esize` bytes field (EMPTY stages).
 int launch_permute(const int d[3], const long long s1[3], const long long s2[3], int esize,
                    const void *in, void *out, cudaStream_t stream, int *kernels_launched);

@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <vector>
+
+#include "kernels.h"
 
 namespace p3d {
 
@@ -24,6 +27,11 @@ int plan3d_sizes(int plan, size_t *in_bytes, size_t *out_bytes, size_t *scratch_
 // without synchronising.  With `capturing` set no allocation or synchronising call is made, so the
 // launches can be recorded into a CUDA graph.
 int exec_plan_on(int plan, const void *in, void *out, int idir, cudaStream_t st, void *scratch_set, bool capturing);
+
+// Runs the executor's buffer assignment for a 3D plan (device pointers, intermediates in
+// `scratch_set`, allocated here if needed) and appends its stages to *rec instead of launching them.
+int record_plan(int plan, const void *in, void *out, int idir, void *scratch_set, std::vector<StageLaunch> *rec);
+DeviceTables *device_tables();
 
 bool device_ready();
 cudaStream_t library_stream();

@@ -15,11 +15,13 @@
 //   DF              FP64 data, float-float arithmetic on the FP32 pipe (df_arith.cuh)
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <vector>
 
@@ -639,7 +641,7 @@ static int launch_any(const KParams &p, bool fixed, size_t smem, int grid, int t
 
 int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
                  DeviceTables *tabs, int *kernels_launched, const void *tw_given, const void *aux_given,
-                 TableNeed *tabs_out) {
+                 TableNeed *tabs_out, FastArgs *fast_prep) {
   const int L = d.L;
   const int a = (L + 1) % 3, b = (L + 2) % 3;
   if (d.d1[a] != d.d2[a] || d.d1[b] != d.d2[b]) return E_BAD_ARG;
@@ -815,11 +817,16 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.dmid = p.dmid;
     q.load_Lmajor = p.load_Lmajor;
     q.store_Lmajor = p.store_Lmajor;
+    if (fast_prep) {
+      *fast_prep = fa;
+      return E_OK;
+    }
     if (q.ntotal == 0) return E_OK;
     const int rc = launch_fast(d.prec, arith, fa, stream);
     if (rc == E_OK && kernels_launched) (*kernels_launched)++;
     return rc;
   }
+  if (fast_prep) return E_UNSUPPORTED;
 
   const size_t csz = (d.prec == 4) ? 8 : 16;
   const bool fixed = fixed_engine_len(p.nfft) && (d.engine == ENG_FIXED || (d.engine == ENG_AUTO && !generic_only));
@@ -885,6 +892,144 @@ static int permute_t(const int d[3], const long long s1[3], const long long s2[3
   k_permute<E><<<(unsigned)grid, blk, 0, st>>>((const E *)in, (E *)out, d[a], d[b], s1[a], s1[b], s1[c], s2[a],
                                                s2[b], s2[c], ta, tb);
   return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+}
+
+// ------------------------------------------------------------------------------------------
+// Grouped launches
+struct LaunchItem {
+  int group;  // >= 0: member of group `group`; -1: launched alone
+  StageLaunch st;
+};
+struct LaunchGroupInfo {
+  FastArgs fa;  // the first member's launch; the members differ only in their buffers
+  int prec, arith;
+  int first, count;  // buffer pairs [first, first + count)
+};
+struct LaunchSet {
+  std::vector<std::vector<LaunchItem>> levels;
+  std::vector<LaunchGroupInfo> groups;
+  void **dev_io = nullptr;  // 2 addresses per group member
+  DeviceTables *tabs = nullptr;
+};
+
+// everything of a specialised launch but its buffers
+static std::vector<long long> fast_key(const StageLaunch &st, const FastArgs &fa) {
+  const FParams &q = fa.p;
+  return {st.d.prec, st.d.prec == 8 ? st.arith : 0, fa.kind, fa.n, (long long)(uintptr_t)q.tw,
+          (long long)(uintptr_t)q.ptw, q.iL, q.it, q.io, q.oL, q.ot, q.oo, q.dt, q.nlines, q.ntotal, q.sign,
+          q.deriv, q.dg, q.dmid, q.load_Lmajor, q.store_Lmajor};
+}
+
+LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err) {
+  LaunchSet *S = new LaunchSet();
+  S->tabs = tabs;
+  std::vector<void *> io;
+  for (const auto &lv : levels) {
+    std::vector<LaunchItem> items;
+    std::map<std::vector<long long>, std::vector<std::pair<FastArgs, StageLaunch>>> by_kernel;
+    for (const auto &st : lv) {
+      FastArgs fa;
+      int rc = E_UNSUPPORTED;
+      if (st.d.kind != K_EMPTY)
+        rc = launch_stage(st.d, st.src, st.dst, st.arith, 0, tabs, nullptr, nullptr, nullptr, nullptr, &fa);
+      if (rc == E_OK && fa.p.ntotal > 0) {
+        by_kernel[fast_key(st, fa)].push_back({fa, st});
+      } else if (rc == E_OK || rc == E_UNSUPPORTED) {
+        items.push_back({-1, st});
+      } else {
+        *err = rc;
+        delete S;
+        return nullptr;
+      }
+    }
+    for (auto &kv : by_kernel) {
+      if (kv.second.size() == 1) {  // nothing to group
+        items.push_back({-1, kv.second[0].second});
+        continue;
+      }
+      LaunchGroupInfo g;
+      g.fa = kv.second[0].first;
+      g.prec = (int)kv.first[0];
+      g.arith = (int)kv.first[1];
+      g.first = (int)io.size() / 2;
+      g.count = (int)kv.second.size();
+      for (auto &m : kv.second) {
+        io.push_back(const_cast<void *>(m.first.p.in));
+        io.push_back(m.first.p.out);
+      }
+      items.push_back({(int)S->groups.size(), kv.second[0].second});
+      S->groups.push_back(g);
+    }
+    // largest launches first, so that concurrent streams finish together
+    auto work = [&](const LaunchItem &it) -> double {
+      const StageDesc &d = it.st.d;
+      const double n = (double)d.d1[0] * d.d1[1] * d.d1[2];
+      return it.group >= 0 ? n * S->groups[it.group].count : n;
+    };
+    std::stable_sort(items.begin(), items.end(),
+                     [&](const LaunchItem &a, const LaunchItem &b) { return work(a) > work(b); });
+    S->levels.push_back(items);
+  }
+  if (!io.empty()) {
+    const size_t bytes = io.size() * sizeof(void *);
+    if (cudaMalloc(&S->dev_io, bytes) != cudaSuccess ||
+        cudaMemcpy(S->dev_io, io.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      if (S->dev_io) cudaFree(S->dev_io);
+      *err = E_CUDA;
+      delete S;
+      return nullptr;
+    }
+  }
+  return S;
+}
+
+static int run_launch_item(LaunchSet *S, const LaunchItem &it, cudaStream_t st, int *kernels);
+
+int launch_set_run(LaunchSet *S, cudaStream_t st, int *kernels) {
+  for (size_t l = 0; l < S->levels.size(); l++)
+    for (const LaunchItem &it : S->levels[l]) {
+      const int rc = run_launch_item(S, it, st, kernels);
+      if (rc != E_OK) return rc;
+    }
+  return E_OK;
+}
+
+int launch_set_levels(const LaunchSet *S) { return (int)S->levels.size(); }
+int launch_set_items(const LaunchSet *S, int l) { return (int)S->levels[l].size(); }
+int launch_set_run_item(LaunchSet *S, int l, int i, cudaStream_t st, int *kernels) {
+  return run_launch_item(S, S->levels[l][i], st, kernels);
+}
+
+static int run_launch_item(LaunchSet *S, const LaunchItem &it, cudaStream_t st, int *kernels) {
+  if (it.group >= 0) {
+    const LaunchGroupInfo &g = S->groups[it.group];
+    FGroup fg;
+    fg.io = S->dev_io + 2 * (size_t)g.first;
+    fg.nj = g.count;
+    const long long ctas = (long long)g.count * g.fa.p.ntotal;
+    if (ctas > 0x7fffffffLL) return E_TOO_LARGE;
+    const int rc = launch_fast(g.prec, g.arith, g.fa, st, &fg, (int)ctas);
+    if (rc == E_OK && kernels) (*kernels)++;
+    return rc;
+  }
+  const StageDesc &d = it.st.d;
+  if (d.kind == K_EMPTY) {
+    const bool same = d.s1[0] == d.s2[0] && d.s1[1] == d.s2[1] && d.s1[2] == d.s2[2];
+    const size_t bytes = (size_t)d.d1[0] * d.d1[1] * d.d1[2] * d.dt1 * d.prec;
+    if (!same) return launch_permute(d.d1, d.s1, d.s2, d.dt1 * d.prec, it.st.src, it.st.dst, st, kernels);
+    if (it.st.src == it.st.dst) return E_OK;
+    return cudaMemcpyAsync(it.st.dst, it.st.src, bytes, cudaMemcpyDefault, st) == cudaSuccess ? E_OK : E_CUDA;
+  }
+  return launch_stage(d, it.st.src, it.st.dst, it.st.arith, st, S->tabs, kernels);
+}
+
+int launch_set_groups(const LaunchSet *S) { return (int)S->groups.size(); }
+
+void launch_set_destroy(LaunchSet *S) {
+  if (!S) return;
+  if (S->dev_io) cudaFree(S->dev_io);
+  delete S;
 }
 
 int preload_kernels() {

@@ -89,6 +89,8 @@ def lib():
         "p3dfft_gb300_batch_create": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_batch_add": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_batch_set_graph": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_set_grouped": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_batch_groups": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_batch_exec": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_batch_kernels": ([ctypes.c_int], ctypes.c_longlong),
         "p3dfft_gb300_batch_field_bytes": ([ctypes.c_int], ctypes.c_double),
@@ -364,7 +366,7 @@ class Batch:
     A job is an ordered list of steps (Transform3D, device input, device output, idir); the steps
     of one job run in order, different jobs run on concurrent branch streams."""
 
-    def __init__(self, nbranches=0, graph=True):
+    def __init__(self, nbranches=0, graph=True, grouped=True):
         setup()
         h = lib().p3dfft_gb300_batch_create(int(nbranches))
         if h < 0:
@@ -373,6 +375,11 @@ class Batch:
         self._keep = []
         if not graph:
             check(lib().p3dfft_gb300_batch_set_graph(h, 0))
+        if not grouped:
+            check(lib().p3dfft_gb300_batch_set_grouped(h, 0))
+
+    def groups(self):
+        return int(lib().p3dfft_gb300_batch_groups(self.handle))
 
     def add(self, job, plan, inp, out, idir=-1):
         pi, k1 = _ptr(inp)

@@ -63,22 +63,27 @@ def _jobs(p3d, n_each=1, idir=-1):
     return jobs
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_batch_bit_identical_to_alone_and_matches_oracle(gpu, oracle, graph):
+@pytest.mark.parametrize("graph,grouped", [(True, True), (False, True), (True, False), (False, False)])
+def test_batch_bit_identical_to_alone_and_matches_oracle(gpu, oracle, graph, grouped):
     p3d = gpu
     p3d.set_fp64_arith(1)
-    jobs = _jobs(p3d)
+    jobs = _jobs(p3d, n_each=2)  # two jobs per (grid, precision): cohorts of two
     alone = [j.alone() for j in jobs]
     for j in jobs:  # clear outputs so the batch must write them
         j.d_s.upload(np.zeros_like(j.spec))
         j.d_y.upload(np.zeros_like(j.back))
-    batch = p3d.Batch(nbranches=4, graph=graph)
+    batch = p3d.Batch(nbranches=4, graph=graph, grouped=grouped)
     for i, j in enumerate(jobs):
         j.add_to(batch, i)
     k0 = p3d.kernel_count()
     batch.exec()  # eager run (+ graph recording)
     k1 = p3d.kernel_count()
-    assert batch.kernels() == k1 - k0 == sum(len(j.f.stages()) + len(j.b.stages()) for j in jobs)
+    stages = sum(len(j.f.stages()) + len(j.b.stages()) for j in jobs)
+    assert batch.kernels() == k1 - k0
+    if grouped:  # cohorts of two: one launch per stage on a specialised kernel, two otherwise
+        assert 0 < batch.groups() and stages // 2 <= batch.kernels() < stages
+    else:
+        assert batch.kernels() == stages and batch.groups() == 0
     for j, (s0, y0) in zip(jobs, alone):
         s, y = j.download()
         assert np.array_equal(s, s0) and np.array_equal(y, y0)
