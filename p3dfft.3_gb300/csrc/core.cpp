@@ -814,7 +814,7 @@ static int autotune_plan(Plan *P) {
     }
     StageTune best;
     best.ms = 1e30f;
-    for (int e : {ENG_FAST, ENG_FIXED, ENG_GENERIC}) {
+    for (int e : {ENG_FAST, ENG_FIXED, ENG_GENERIC, ENG_BLUESTEIN}) {
       for (int ta = 0; ta < 2; ta++) {
         d.engine = e;
         d.talt = ta;
@@ -1281,7 +1281,7 @@ int p3dfft_gb300_plan_tuning(int plan, int is1d, int *engine, int *talt, double 
 
 int p3dfft_gb300_plan_set_engine(int plan, int is1d, int stage, int engine, int talt) {
   Plan *P = plan_of(plan, is1d);
-  if (!P || stage < 0 || stage >= (int)P->ex.size() || engine < 0 || engine > ENG_GENERIC) {
+  if (!P || stage < 0 || stage >= (int)P->ex.size() || engine < 0 || engine > ENG_BLUESTEIN) {
     set_err(E_BAD_ARG, "invalid plan, stage or engine");
     return E_BAD_ARG;
   }
@@ -1323,7 +1323,7 @@ int p3dfft_gb300_tune_cache_load(const char *path) {
     std::string key(line);
     while (!key.empty() && key.back() == ' ') key.pop_back();
     StageTune t;
-    if (sscanf(bar + 1, "%d %d %f", &t.engine, &t.talt, &t.ms) != 3 || t.engine < 0 || t.engine > ENG_GENERIC) continue;
+    if (sscanf(bar + 1, "%d %d %f", &t.engine, &t.talt, &t.ms) != 3 || t.engine < 0 || t.engine > ENG_BLUESTEIN) continue;
     g_tune_cache[key] = t;
     n++;
   }

@@ -42,12 +42,13 @@ struct StageDesc {
   int d1[3], d2[3];
   long long s1[3], s2[3];
   int deriv;      // fuse the i*k multiply (compute_deriv_loc)
-  // tuning (0 = heuristic): engine 1 specialised kernel, 2 register engine, 3 generic engine;
+  // tuning (0 = heuristic): engine 1 specialised kernel, 2 register engine, 3 generic engine
+  // (radix passes only), 4 Bluestein engine;
   // talt 1 takes consecutive lines of a tile along the other batch dim
   int engine = 0;
   int talt = 0;
 };
-enum Engine { ENG_AUTO = 0, ENG_FAST = 1, ENG_FIXED = 2, ENG_GENERIC = 3 };
+enum Engine { ENG_AUTO = 0, ENG_FAST = 1, ENG_FIXED = 2, ENG_GENERIC = 3, ENG_BLUESTEIN = 4 };
 
 struct DeviceTables;  // twiddle-table cache, one per device
 
@@ -66,6 +67,9 @@ void fill_table(int N, int fmt, void *host_dst);
 // Per-pass twiddle rows of the specialised kernels for FFT length N (fast_stage.cuh)
 size_t pass_table_bytes(int N, int fmt);
 void fill_pass_table(int N, int fmt, void *host_dst);
+// Tables of the Bluestein engine for FFT length n
+size_t blue_table_bytes(int n, int fmt);
+void fill_blue_table(int n, int fmt, void *host_dst);
 
 // Launch one stage on `stream`.  in != out is required (the host runtime guarantees it).
 // Tables come from `tabs` (allocated on first use) unless `tw_given` is non-null, in which case

@@ -68,6 +68,7 @@ struct Native {
     return mk(a.x * c, a.y * c);
   }
   static __device__ __forceinline__ C rmul(C a, S c) { return mk(a.x * c, a.y * c); }  // real scalar
+  static __device__ __forceinline__ C scalef(C a, float f) { return mk(a.x * (R)f, a.y * (R)f); }  // power of 2
   static __device__ __forceinline__ C iscale(C a, int k) {  // a * (i*k)
     R kk = R(k);
     return mk(-kk * a.y, kk * a.x);
@@ -145,6 +146,9 @@ struct DF {
   }
   static __device__ __forceinline__ C iscale(C a, int k) {
     return mk(ff_neg(ff_mul_int(a.y, k)), ff_mul_int(a.x, k));
+  }
+  static __device__ __forceinline__ C scalef(C a, float f) {  // by a power of two: exact
+    return mk(ff{a.x.hi * f, a.x.lo * f}, ff{a.y.hi * f, a.y.lo * f});
   }
   static __device__ __forceinline__ C rmul(C a, S c) {  // real scalar, unnormalised
     return mk(ff_mul_const_nn(a.x, c.hi, c.lo), ff_mul_const_nn(a.y, c.hi, c.lo));

@@ -50,17 +50,25 @@ struct KParams {
   int deriv, dg, dmid;
   int r2r_np, r2r_a2, r2r_b2, r2r_sin, r2r_halffirst, r2r_halflast;
   int in_complex, out_complex;
+  // Bluestein engine: convolution length bM (power of two), its radix plan, and its tables
+  // [W_bM^k, k < bM][chirp W_m, m < nfft][transform of the forward chirp kernel][of the backward]
+  int bM, bnrad;
+  int brad[12];
+  const void *baux;
 };
 
-template <class O>
+// B selects the Bluestein engine's convolution FFT (length bM, its own twiddle table).
+template <class O, bool B = false>
 __device__ __forceinline__ typename O::C twid(const KParams &p, int m, int sign) {
-  typename O::C w = O::tw(reinterpret_cast<const typename O::T *>(p.tw), m * p.twstep);
+  typename O::C w = B ? O::tw(reinterpret_cast<const typename O::T *>(p.baux), m)
+                      : O::tw(reinterpret_cast<const typename O::T *>(p.tw), m * p.twstep);
   return sign < 0 ? w : O::conj(w);
 }
 
 // DFT of radix R in registers, sign -1 forward.  Odd R uses the twiddle table for W_R^q.
-template <class O, int R>
+template <class O, int R, bool B = false>
 __device__ __forceinline__ void dft_reg(typename O::C *v, int sign, const KParams &p) {
+  const int nf = B ? p.bM : p.nfft;
   using C = typename O::C;
   if (R == 2) {
     C a = v[0], b = v[1];
@@ -81,8 +89,8 @@ __device__ __forceinline__ void dft_reg(typename O::C *v, int sign, const KParam
       e[k] = v[2 * k];
       o[k] = v[2 * k + 1];
     }
-    dft_reg<O, 4>(e, sign, p);
-    dft_reg<O, 4>(o, sign, p);
+    dft_reg<O, 4, B>(e, sign, p);
+    dft_reg<O, 4, B>(o, sign, p);
     // o[k] *= W8^k (forward), conj for backward
     C o1 = O::rsqrt2(sign < 0 ? O::add(o[1], O::mulmi(o[1])) : O::add(o[1], O::muli(o[1])));
     C o2 = sign < 0 ? O::mulmi(o[2]) : O::muli(o[2]);
@@ -96,18 +104,18 @@ __device__ __forceinline__ void dft_reg(typename O::C *v, int sign, const KParam
     v[3] = O::add(e[3], o3);
     v[7] = O::sub(e[3], o3);
   } else if (R == 3) {
-    dft3<O>(v, sign, twid<O>(p, p.nfft / 3, -1));
+    dft3<O>(v, sign, twid<O, B>(p, nf / 3, -1));
   } else if (R == 5) {
-    dft5<O>(v, sign, twid<O>(p, p.nfft / 5, -1), twid<O>(p, 2 * (p.nfft / 5), -1));
+    dft5<O>(v, sign, twid<O, B>(p, nf / 5, -1), twid<O, B>(p, 2 * (nf / 5), -1));
   } else {
     // other odd radix: direct sum with W_R^q from the table (index q * nfft/R)
     C out[R];
-    const int unit = p.nfft / R;
+    const int unit = nf / R;
 #pragma unroll
     for (int q = 0; q < R; q++) {
       C acc = v[0];
 #pragma unroll
-      for (int r = 1; r < R; r++) acc = O::add(acc, O::mul(v[r], twid<O>(p, ((r * q) % R) * unit, sign)));
+      for (int r = 1; r < R; r++) acc = O::add(acc, O::mul(v[r], twid<O, B>(p, ((r * q) % R) * unit, sign)));
       out[q] = acc;
     }
 #pragma unroll
@@ -115,7 +123,7 @@ __device__ __forceinline__ void dft_reg(typename O::C *v, int sign, const KParam
   }
 }
 
-template <class O, int R>
+template <class O, int R, bool B = false>
 __device__ __forceinline__ void bfly(const typename O::C *src, typename O::C *dst, int j, int T, int Ns,
                                      int sign, const KParams &p) {
   using C = typename O::C;
@@ -124,44 +132,46 @@ __device__ __forceinline__ void bfly(const typename O::C *src, typename O::C *ds
 #pragma unroll
   for (int r = 0; r < R; r++) v[r] = src[j + r * T];
   if (Ns > 1) {
-    int unit = k * (p.nfft / (Ns * R));
+    int unit = k * ((B ? p.bM : p.nfft) / (Ns * R));
 #pragma unroll
-    for (int r = 1; r < R; r++) v[r] = O::mul(v[r], twid<O>(p, r * unit, sign));
+    for (int r = 1; r < R; r++) v[r] = O::mul(v[r], twid<O, B>(p, r * unit, sign));
   }
-  dft_reg<O, R>(v, sign, p);
+  dft_reg<O, R, B>(v, sign, p);
   int base = (j - k) * R + k;
 #pragma unroll
   for (int r = 0; r < R; r++) dst[base + r * Ns] = O::norm(v[r]);
 }
 
-template <class O>
+template <class O, bool B = false>
 __device__ void bfly_generic(const typename O::C *src, typename O::C *dst, int j, int T, int Ns, int R,
                              int sign, const KParams &p) {
   using C = typename O::C;
+  const int nf = B ? p.bM : p.nfft;
   int k = j % Ns;
-  int unit = k * (p.nfft / (Ns * R));
-  int runit = p.nfft / R;
+  int unit = k * (nf / (Ns * R));
+  int runit = nf / R;
   int base = (j - k) * R + k;
   for (int q = 0; q < R; q++) {
     C acc = O::zero();
     for (int r = 0; r < R; r++) {
       C x = src[j + r * T];
       int m = r * unit + ((r * q) % R) * runit;  // twiddle * W_R^{rq}
-      m %= p.nfft;
-      acc = O::add(acc, O::mul(x, twid<O>(p, m, sign)));
+      m %= nf;
+      acc = O::add(acc, O::mul(x, twid<O, B>(p, m, sign)));
     }
     dst[base + q * Ns] = O::norm(acc);
   }
 }
 
 // Runs the radix passes over `nlines` lines; returns the buffer index holding the result.
-template <class O>
+template <class O, bool B = false>
 __device__ int fft_passes(const KParams &p, typename O::C *b0, typename O::C *b1, int nlines, int sign) {
   using C = typename O::C;
   int Ns = 1, cur = 0;
-  for (int s = 0; s < p.nrad; s++) {
-    const int R = p.rad[s];
-    const int T = p.nfft / R;
+  const int nrad = B ? p.bnrad : p.nrad;
+  for (int s = 0; s < nrad; s++) {
+    const int R = B ? p.brad[s] : p.rad[s];
+    const int T = (B ? p.bM : p.nfft) / R;
     const C *src = cur ? b1 : b0;
     C *dst = cur ? b0 : b1;
     const int total = nlines * T;
@@ -170,13 +180,13 @@ __device__ int fft_passes(const KParams &p, typename O::C *b0, typename O::C *b1
       const C *sl = src + (size_t)lt * p.ls;
       C *dl = dst + (size_t)lt * p.ls;
       switch (R) {
-        case 2: bfly<O, 2>(sl, dl, j, T, Ns, sign, p); break;
-        case 3: bfly<O, 3>(sl, dl, j, T, Ns, sign, p); break;
-        case 4: bfly<O, 4>(sl, dl, j, T, Ns, sign, p); break;
-        case 5: bfly<O, 5>(sl, dl, j, T, Ns, sign, p); break;
-        case 7: bfly<O, 7>(sl, dl, j, T, Ns, sign, p); break;
-        case 8: bfly<O, 8>(sl, dl, j, T, Ns, sign, p); break;
-        default: bfly_generic<O>(sl, dl, j, T, Ns, R, sign, p); break;
+        case 2: bfly<O, 2, B>(sl, dl, j, T, Ns, sign, p); break;
+        case 3: bfly<O, 3, B>(sl, dl, j, T, Ns, sign, p); break;
+        case 4: bfly<O, 4, B>(sl, dl, j, T, Ns, sign, p); break;
+        case 5: bfly<O, 5, B>(sl, dl, j, T, Ns, sign, p); break;
+        case 7: bfly<O, 7, B>(sl, dl, j, T, Ns, sign, p); break;
+        case 8: bfly<O, 8, B>(sl, dl, j, T, Ns, sign, p); break;
+        default: bfly_generic<O, B>(sl, dl, j, T, Ns, R, sign, p); break;
       }
     }
     __syncthreads();
@@ -224,6 +234,56 @@ struct GenericFFT {
   template <class O>
   __device__ static int run(const KParams &p, typename O::C *b0, typename O::C *b1, int nflines, int sign) {
     return fft_passes<O>(p, b0, b1, nflines, sign);
+  }
+};
+
+// BluesteinFFT: the DFT of a length n with a large prime factor as a circular convolution of
+// length bM (a power of two >= 2n-1), computed with two bM-point radix FFTs (Bluestein, 1970):
+//   W_m = exp(s i pi m^2 / n)  (s = sign),  a_j = x_j W_j,  b_m = conj(W_m) for |m| < n,
+//   X_k = W_k (a (*) b)_k,  k < n.
+// The bM-point transforms of b for both signs are precomputed on the host (long double).
+struct BluesteinFFT {
+  static constexpr int PADSH = 0;
+  static constexpr bool FIXED = false;
+  template <class O>
+  __device__ static int run(const KParams &p, typename O::C *b0, typename O::C *b1, int nlines, int sign) {
+    using C = typename O::C;
+    using T = typename O::T;
+    const int n = p.nfft, M = p.bM;
+    const T *tab = reinterpret_cast<const T *>(p.baux);
+    const T *chirp = tab + M;
+    const T *kern = tab + M + n + (sign < 0 ? 0 : M);
+    int total = nlines * M;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      const int lt = idx / M, k = idx - lt * M;
+      C v = O::zero();
+      if (k < n) {
+        const C w = O::tw(chirp, k);
+        v = O::mul(b0[(size_t)lt * p.ls + k], sign < 0 ? w : O::conj(w));
+      }
+      b1[(size_t)lt * p.ls + k] = O::norm(v);
+    }
+    __syncthreads();
+    int cur = fft_passes<O, true>(p, b1, b0, nlines, -1);
+    C *A = cur ? b0 : b1, *other = cur ? b1 : b0;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      const int lt = idx / M, k = idx - lt * M;
+      C *a = A + (size_t)lt * p.ls + k;
+      *a = O::norm(O::mul(*a, O::tw(kern, k)));
+    }
+    __syncthreads();
+    cur = fft_passes<O, true>(p, A, other, nlines, 1);
+    C *c = cur ? other : A;
+    const float inv = 1.0f / (float)M;  // exact: M is a power of two
+    total = nlines * n;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      const int lt = idx / n, k = idx - lt * n;
+      C *y = c + (size_t)lt * p.ls + k;
+      const C w = O::tw(chirp, k);
+      *y = O::norm(O::scalef(O::mul(*y, sign < 0 ? w : O::conj(w)), inv));
+    }
+    __syncthreads();
+    return c == b0 ? 0 : 1;
   }
 };
 
@@ -496,11 +556,10 @@ __global__ void k_deriv(const R *in, R *out, long long n, int sd0, int sd1, int 
 // double pairs (fmt 0), float pairs (fmt 1) or float-float pairs (fmt 2).
 size_t table_bytes(int N, int fmt) { return (size_t)N * (fmt == 1 ? 8 : 16); }
 
-// entry i of a table: W_M^m in format fmt
-static void put_twiddle(unsigned char *host, size_t i, long long m, long long M, int fmt) {
-  const long double TWO_PI = 6.283185307179586476925286766559005768L;
-  const long double a = TWO_PI * (long double)(m % M) / (long double)M;
-  const long double c = cosl(a), s = -sinl(a);
+static const long double TWO_PI_L = 6.283185307179586476925286766559005768L;
+
+// entry i of a table: the complex value c + i s in format fmt
+static void put_value(unsigned char *host, size_t i, long double c, long double s, int fmt) {
   if (fmt == 0) {
     double v[2] = {(double)c, (double)s};
     memcpy(&host[i * 16], v, 16);
@@ -511,6 +570,88 @@ static void put_twiddle(unsigned char *host, size_t i, long long m, long long M,
     float ch = (float)c, sh = (float)s;
     float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
     memcpy(&host[i * 16], v, 16);
+  }
+}
+
+// entry i of a table: W_M^m = exp(-2 pi i m / M) in format fmt
+static void put_twiddle(unsigned char *host, size_t i, long long m, long long M, int fmt) {
+  const long double a = TWO_PI_L * (long double)(m % M) / (long double)M;
+  put_value(host, i, cosl(a), -sinl(a), fmt);
+}
+
+// Bluestein: convolution length (power of two >= 2n - 1)
+static int blue_len(int n) {
+  int M = 1;
+  while (M < 2 * n - 1) M <<= 1;
+  return M;
+}
+
+static int largest_prime_factor(int n) {
+  int m = n, lp = 1;
+  for (int f = 2; (long long)f * f <= m; f++)
+    while (m % f == 0) {
+      lp = f;
+      m /= f;
+    }
+  return m > 1 ? std::max(lp, m) : lp;
+}
+
+size_t blue_table_bytes(int n, int fmt) { return (size_t)(3 * blue_len(n) + n) * (fmt == 1 ? 8 : 16); }
+
+// In-place forward DFT (exp(-2 pi i jk/M)) of a power-of-two length, in long double.
+static void ld_fft(std::vector<long double> &re, std::vector<long double> &im) {
+  const size_t n = re.size();
+  for (size_t i = 1, j = 0; i < n; i++) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(re[i], re[j]);
+      std::swap(im[i], im[j]);
+    }
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    for (size_t j = 0; j < len / 2; j++) {
+      const long double a = -TWO_PI_L * (long double)j / (long double)len, wr = cosl(a), wi = sinl(a);
+      for (size_t i = 0; i < n; i += len) {
+        const size_t u = i + j, v = i + j + len / 2;
+        const long double xr = re[v] * wr - im[v] * wi, xi = re[v] * wi + im[v] * wr;
+        re[v] = re[u] - xr;
+        im[v] = im[u] - xi;
+        re[u] += xr;
+        im[u] += xi;
+      }
+    }
+  }
+}
+
+// [W_M^k, k < M][W_m = exp(-i pi m^2 / n), m < n][FFT_M of b_m = conj(W_m)][FFT_M of b_m = W_m],
+// b placed circularly (b_{M-m} = b_m, 0 < m < n).
+void fill_blue_table(int n, int fmt, void *dst) {
+  unsigned char *host = static_cast<unsigned char *>(dst);
+  const int M = blue_len(n);
+  for (int k = 0; k < M; k++) put_twiddle(host, k, k, M, fmt);
+  std::vector<long double> wr(n), wi(n);
+  for (int m = 0; m < n; m++) {
+    const long long q = ((long long)m * m) % (2LL * n);  // exp(-i pi m^2 / n) = W_{2n}^{m^2}
+    const long double a = TWO_PI_L * (long double)q / (long double)(2 * n);
+    wr[m] = cosl(a);
+    wi[m] = -sinl(a);
+    put_value(host, (size_t)M + m, wr[m], wi[m], fmt);
+  }
+  for (int sgn = 0; sgn < 2; sgn++) {  // 0: b = conj(W) (forward), 1: b = W (backward)
+    std::vector<long double> br(M, 0.0L), bi(M, 0.0L);
+    for (int m = 0; m < n; m++) {
+      const long double im = sgn == 0 ? -wi[m] : wi[m];
+      br[m] = wr[m];
+      bi[m] = im;
+      if (m > 0) {
+        br[M - m] = wr[m];
+        bi[M - m] = im;
+      }
+    }
+    ld_fft(br, bi);
+    for (int k = 0; k < M; k++) put_value(host, (size_t)M + n + (size_t)sgn * M + k, br[k], bi[k], fmt);
   }
 }
 
@@ -547,15 +688,17 @@ struct DeviceTables {
   ~DeviceTables() {
     for (auto &kv : tabs) cudaFree(kv.second);
   }
-  // pass = 1: the specialised kernels' per-pass twiddle rows of FFT length N
+  // pass = 1: the specialised kernels' per-pass twiddle rows of FFT length N; pass = 2: the
+  // Bluestein engine's tables for length N
   const void *get(int N, int fmt, int *err, int pass = 0) {
     std::lock_guard<std::mutex> g(mu);
     auto key = std::make_pair(N, fmt + 8 * pass);
     auto it = tabs.find(key);
     if (it != tabs.end()) return it->second;
-    size_t bytes = pass ? pass_table_bytes(N, fmt) : table_bytes(N, fmt);
+    size_t bytes = pass == 2 ? blue_table_bytes(N, fmt) : (pass ? pass_table_bytes(N, fmt) : table_bytes(N, fmt));
     std::vector<unsigned char> host(bytes);
-    if (pass) fill_pass_table(N, fmt, host.data());
+    if (pass == 2) fill_blue_table(N, fmt, host.data());
+    else if (pass) fill_pass_table(N, fmt, host.data());
     else fill_table(N, fmt, host.data());
     void *d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) {
@@ -634,8 +777,9 @@ static int launch_fixed(const KParams &p, size_t smem, int grid, int threads, cu
 }
 
 template <class O>
-static int launch_any(const KParams &p, bool fixed, size_t smem, int grid, int threads, cudaStream_t st) {
+static int launch_any(const KParams &p, bool fixed, bool blue, size_t smem, int grid, int threads, cudaStream_t st) {
   if (fixed) return launch_fixed<O>(p, smem, grid, threads, st);
+  if (blue) return launch_k<O, BluesteinFFT>(p, smem, grid, threads, st);
   return launch_k<O, GenericFFT>(p, smem, grid, threads, st);
 }
 
@@ -741,6 +885,13 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   if (d.engine == ENG_FAST && !fast_ok) return E_UNSUPPORTED;
   if (d.engine == ENG_FIXED && !fixed_engine_len(p.nfft)) return E_UNSUPPORTED;
   const bool use_fast = fast_ok && (d.engine == ENG_FAST || (d.engine == ENG_AUTO && !generic_only));
+  // Bluestein for lengths with a prime factor above 16 (radix passes would spend O(p^2) work per
+  // butterfly), when its tables come from the cache and its convolution fits in shared memory
+  const int bM = blue_len(p.nfft);
+  const bool use_blue = !use_fast && !tw_given && !tabs_out && !fast_prep && !generic_only &&
+                        (d.engine == ENG_AUTO || d.engine == ENG_BLUESTEIN) && largest_prime_factor(p.nfft) > 16 &&
+                        bM <= (d.prec == 4 ? 4096 : 2048);
+  if (d.engine == ENG_BLUESTEIN && !use_blue) return E_UNSUPPORTED;
 
   const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? 2 : 0);
   if (tabs_out) {  // caller supplies the tables: report what is needed, launch nothing
@@ -763,6 +914,12 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     } else if (d.kind == K_R2R && p.r2r_np > 0) {
       p.aux = tabs->get(8 * p.r2r_np, fmt, &err);
       if (!p.aux) return err;
+    }
+    if (use_blue) {
+      p.bM = bM;
+      p.bnrad = factorize(bM, p.brad, 12);
+      p.baux = tabs->get(p.nfft, fmt, &err, 2);
+      if (!p.baux || p.bnrad < 0) return err ? err : E_UNSUPPORTED;
     }
   }
   if (d.deriv && d.dt2 == 2) {
@@ -829,8 +986,9 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   if (fast_prep) return E_UNSUPPORTED;
 
   const size_t csz = (d.prec == 4) ? 8 : 16;
-  const bool fixed = fixed_engine_len(p.nfft) && (d.engine == ENG_FIXED || (d.engine == ENG_AUTO && !generic_only));
+  const bool fixed = !use_blue && fixed_engine_len(p.nfft) && (d.engine == ENG_FIXED || (d.engine == ENG_AUTO && !generic_only));
   int slots = p.nfft;
+  if (use_blue) slots = std::max(slots, bM);
   if (p.nin > slots) slots = p.nin;
   if (p.nout > slots) slots = p.nout;
   if (d.kind == K_C2R) slots = std::max(slots, p.nfft + 1);
@@ -867,9 +1025,9 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   if (grid > 0x7fffffffLL) return E_TOO_LARGE;
   size_t smem = per_line * TB;
   int rc;
-  if (d.prec == 4) rc = launch_any<Native<float>>(p, fixed, smem, (int)grid, threads, stream);
-  else if (arith == AR_DF) rc = launch_any<DF>(p, fixed, smem, (int)grid, threads, stream);
-  else rc = launch_any<Native<double>>(p, fixed, smem, (int)grid, threads, stream);
+  if (d.prec == 4) rc = launch_any<Native<float>>(p, fixed, use_blue, smem, (int)grid, threads, stream);
+  else if (arith == AR_DF) rc = launch_any<DF>(p, fixed, use_blue, smem, (int)grid, threads, stream);
+  else rc = launch_any<Native<double>>(p, fixed, use_blue, smem, (int)grid, threads, stream);
   if (rc == E_OK && kernels_launched) (*kernels_launched)++;
   return rc;
 }
