@@ -158,17 +158,6 @@ __host__ __device__ constexpr int fast_ls() {
   return best;
 }
 
-// 1: values are normalised before every shared-memory store between passes (float-float: one
-// Fast2Sum per component); 0: stored as computed (the next pass's TwoSum adds accept them)
-#ifndef FAST_STORE_NORM
-#define FAST_STORE_NORM 1
-#endif
-
-// 1: twiddles of the Stockham passes from the per-pass tables below; 0: from the length-N table
-#ifndef FAST_PASS_TABLES
-#define FAST_PASS_TABLES 1
-#endif
-
 // Per-pass twiddle tables.  Pass I >= 1 of the radix plan (radix R, Ns = product of the earlier
 // radices) multiplies by W_{Ns R}^{r k}, r = 1 .. R-1, for its k = jj mod Ns.  They are stored per
 // pass as R-1 rows of Ns entries, row r-1 holding W_{Ns R}^{r k} at entry k: the threads of a warp
@@ -223,7 +212,6 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       for (int r = 0; r < R; r++)
         v[b * R + r] = line[(M % (1 << PS) == 0) ? pj + r * (M + (M >> PS)) : pad<PS>(jj + r * M)];
       if constexpr (Ns > 1) {
-#if FAST_PASS_TABLES
         const typename O::T *pt = ptab + fast_pass_offset(N, I) + jj % Ns;
         if constexpr (O::TW_POWERS) {
           // two table twiddles per butterfly, the others as products of at most two of them
@@ -244,12 +232,6 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
 #pragma unroll
           for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(pt, (r - 1) * Ns, sign));
         }
-#else
-        const int k = jj % Ns;
-#pragma unroll
-        for (int r = 1; r < R; r++)
-          v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(tab, r * k * (N / (Ns * R)) * TWSTEP, sign));
-#endif
       }
       if constexpr (R == 3) dft3<O>(&v[b * R], sign, w1);
       else if constexpr (R == 5) dft5<O>(&v[b * R], sign, w1, w2);
@@ -273,7 +255,7 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
 #pragma unroll
       for (int r = 0; r < R; r++) {
         const int slot = NS_AL ? pb + r * (Ns + (Ns >> PS)) : (FIRST_AL ? pb + r : pad<PS>(base + r * Ns));
-        line[slot] = FAST_STORE_NORM ? O::norm(v[b * R + r]) : v[b * R + r];
+        line[slot] = O::norm(v[b * R + r]);  // (unnormalised stores measured 1.7% faster, 2x the error)
       }
     }
   }
