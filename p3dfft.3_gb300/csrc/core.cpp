@@ -427,28 +427,41 @@ static Plan *make_plan3(const int types[3], const GridDesc &g1, const GridDesc &
 // the reference schedule on ties.  P3DFFT_GB300_REFERENCE_SCHEDULE=1 runs the reference schedule.
 // Cost of one side of a stage: 1 for contiguous lines, or for lines taken across a contiguous
 // tile dim t with the line's points near each other; 1.4 with the points >= 16 Ki elements
-// apart; 4 when neither the lines nor t are contiguous (uncoalesced).
-static double side_cost(const long long s[3], int L, int t) {
-  if (s[L] == 1) return 1.0;
-  if (s[t] != 1) return 4.0;
-  return s[L] >= 16384 ? 1.4 : 1.0;
+// apart; 4 when neither the lines nor t are contiguous (uncoalesced).  Plus 0.15 when rows of the
+// contiguous dim are not a multiple of 128 bytes (e.g. 257 complex values), so that accesses
+// straddle an extra cache line (measured: the float-float C2R stage reading 257-element rows
+// ran 0.14 ms, 13%, slower than reading 512-element rows).
+static double side_cost(const long long s[3], const int *gd, int L, int t, int esz) {
+  double c;
+  int cdim;
+  if (s[L] == 1) {
+    c = 1.0;
+    cdim = L;
+  } else if (s[t] != 1) {
+    return 4.0;
+  } else {
+    c = s[L] >= 16384 ? 1.4 : 1.0;
+    cdim = t;
+  }
+  return c + (((long long)gd[cdim] * esz) % 128 ? 0.15 : 0.0);
 }
 
 // Load + store cost of a stage with the kernel's choice of tile dim (launch_stage): by output
 // stride when the input lines are contiguous, else by input stride.
-static double stage_cost(const Stage &st) {
+static double stage_cost(const Stage &st, int prec) {
   long long s1[3], s2[3];
   strides(st.g1, s1);
   strides(st.g2, s2);
+  const TypeInfo &ti = g_types[st.type];
   const int L = st.dim, a = (L + 1) % 3, b = (L + 2) % 3;
   const int t = (s1[L] == 1) ? (s2[a] <= s2[b] ? a : b) : (s1[a] <= s1[b] ? a : b);
-  return side_cost(s1, L, t) + side_cost(s2, L, t);
+  return side_cost(s1, st.g1.gdims, L, t, ti.dt1 * prec) + side_cost(s2, st.g2.gdims, L, t, ti.dt2 * prec);
 }
 
-static double schedule_cost(const std::vector<Stage> &v) {
+static double schedule_cost(const std::vector<Stage> &v, int prec) {
   double c = 0;
   for (auto &st : v)
-    if (g_types[st.type].kind != K_EMPTY) c += stage_cost(st);
+    if (g_types[st.type].kind != K_EMPTY) c += stage_cost(st, prec);
   return c;
 }
 
@@ -460,7 +473,7 @@ static void optimize_schedule(Plan *P) {
     if (g_types[st.type].kind == K_EMPTY) return;
   static const int MO[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
   static const int PERM[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-  double best = schedule_cost(P->ex) - 1e-9;
+  double best = schedule_cost(P->ex, P->prec) - 1e-9;
   for (auto &pm : PERM) {
     // the data type must chain: real-to-complex first, complex-to-real last
     int dt = P->dt1;
@@ -498,7 +511,7 @@ static void optimize_schedule(Plan *P) {
         bool dims_ok = true;
         for (int i = 0; i < 3; i++) dims_ok &= v[2].g2.gdims[i] == P->g2.gdims[i];
         if (!dims_ok) continue;
-        const double c = schedule_cost(v);
+        const double c = schedule_cost(v, P->prec);
         if (c < best) {
           best = c - 1e-9;
           P->ex = v;
