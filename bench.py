@@ -243,6 +243,24 @@ def load_traffic(kernel_key):
     return None
 
 
+def load_instr(kernel_key):
+    """Warp instructions per complex FFT point of a kernel, from an `INSTR <kernel> <count>` line
+    of a committed ncu summary under profiles/ (None when no summary covers it)."""
+    pdir = os.path.join(ROOT, "profiles")
+    try:
+        for fn in sorted(os.listdir(pdir)):
+            if not fn.endswith((".md", ".txt")):
+                continue
+            with open(os.path.join(pdir, fn)) as f:
+                for line in f:
+                    p = line.split()
+                    if len(p) == 3 and p[0] == "INSTR" and p[1] == kernel_key:
+                        return float(p[2])
+    except OSError:
+        pass
+    return None
+
+
 def kernel_id(stage, arith, n_dims):
     """Name of the kernel instantiation that runs a stage (matches the ncu kernel names)."""
     kind = {5: 1, 7: 2}.get(stage["type"], 0)  # R2C_D, C2R_D, else C2C
@@ -297,7 +315,8 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
 
     mixed = [(gd, prec, buffers(gd, prec, 4000 + i)) for i, (gd, prec) in enumerate(jobs)]
     plain = [(gd, 8, buffers(gd, 8, 4000 + i)) for i, (gd, _) in enumerate(jobs)]
-    for gd, prec in set(jobs) | {(gd, 8) for gd, _ in jobs}:
+    single = [(gd, 4, buffers(gd, 4, 4000 + i)) for i, (gd, _) in enumerate(jobs)]
+    for gd, prec in set(jobs) | {(gd, p) for gd, _ in jobs for p in (4, 8)}:
         plan_pair(gd, prec)
 
     def make_batch(items, graph=True, grouped=True):
@@ -335,6 +354,14 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
     ms_mixed, k_mixed = time_batch(b_mixed)
     b_f64 = make_batch(plain)
     ms_b64, _ = time_batch(b_f64)
+    b_f32 = make_batch(single)
+    ms_b32, _ = time_batch(b_f32)
+    # each FP32 job's result against the same job in FP64 (both unnormalised round trips)
+    err32 = 0.0
+    for (gd, _, (_, _, y32)), (_, _, (_, _, y64)) in zip(single, plain):
+        a = y32.download(np.empty(gd[0] * gd[1] * gd[2], np.float32)).astype(np.float64)
+        r = y64.download(np.empty(gd[0] * gd[1] * gd[2], np.float64))
+        err32 = max(err32, float(np.linalg.norm(a - r) / np.linalg.norm(r)))
     b_nog = make_batch(mixed, graph=False)
     ms_nog, _ = time_batch(b_nog)
     b_br = make_batch(mixed, grouped=False)
@@ -376,6 +403,11 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
                                        "mode": f"{nbranches} concurrent branch streams, one launch per stage"},
         "batch_graph_all_fp64": {"ms": ms_b64, "round_trips_per_s": n / (ms_b64 * 1e-3),
                                  "GB_per_s": alg_plain / (ms_b64 * 1e-3) / 1e9},
+        "batch_graph_all_fp32": {"ms": ms_b32, "round_trips_per_s": n / (ms_b32 * 1e-3),
+                                 "GB_per_s": alg_plain / 2 / (ms_b32 * 1e-3) / 1e9,
+                                 "speedup_vs_sequential_fp64": ms_seq / ms_b32,
+                                 "speedup_vs_batch_fp64": ms_b64 / ms_b32,
+                                 "max_rel_l2_vs_fp64": err32},
         "batch_streams_no_graph_mixed": {"ms": ms_nog, "round_trips_per_s": n / (ms_nog * 1e-3)},
         "sequential_plain_fp64": {"ms": ms_seq, "round_trips_per_s": n / (ms_seq * 1e-3),
                                   "GB_per_s": alg_plain / (ms_seq * 1e-3) / 1e9},
@@ -384,7 +416,7 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
         "autotune": {"seconds": t_tune, "engines": "1 specialised, 2 register, 3 generic; [engine, alt tile dim, ms]",
                      "choices": tuning},
     }
-    for bt in (b_mixed, b_f64, b_nog, b_br):
+    for bt in (b_mixed, b_f64, b_f32, b_nog, b_br):
         del bt
     return out
 
@@ -432,6 +464,42 @@ def serve_job_bytes(gd, kind, prec):
     if kind == "r2c":
         return round_trip_bytes(gd, prec)
     return 12 * 2 * prec * n
+
+
+def mixed_types_workload(p3d, L, steps, arith):
+    """384x256x257 with x R2C, y C2C, z DCT-I (complex), forward and backward, FP64 and FP32:
+    per-stage device time (CUDA events between stages) and 3-pass GB/s of the round trip."""
+    import ctypes
+    gd, gd2 = (384, 256, 257), (193, 256, 257)
+    out = {"grid": list(gd), "types_forward": "R2C,CFFT_FORWARD,DCT1_COMPLEX",
+           "types_backward": "C2R,CFFT_BACKWARD,DCT1_COMPLEX"}
+    for prec in (8, 4):
+        sfx = "D" if prec == 8 else "S"
+        ft = [p3d.TYPE_IDS[f"R2CFFT_{sfx}"], p3d.TYPE_IDS[f"CFFT_FORWARD_{sfx}"], p3d.TYPE_IDS[f"DCT1_COMPLEX_{sfx}"]]
+        bt = [p3d.TYPE_IDS[f"C2RFFT_{sfx}"], p3d.TYPE_IDS[f"CFFT_BACKWARD_{sfx}"], p3d.TYPE_IDS[f"DCT1_COMPLEX_{sfx}"]]
+        f = p3d.Transform3D(ft, gd, MO1, gd2, MO2, -1, 0)
+        b = p3d.Transform3D(bt, gd2, MO2, gd, MO1, 0, -1)
+        s_r = prec * gd[0] * gd[1] * gd[2]
+        s_c = 2 * prec * gd2[0] * gd2[1] * gd2[2]
+        d_x, d_s, d_y = p3d.DeviceArray(s_r), p3d.DeviceArray(s_c), p3d.DeviceArray(s_r)
+        x = np.random.default_rng(384).uniform(-1.0, 1.0, gd[0] * gd[1] * gd[2])
+        d_x.upload(x.astype(np.float64 if prec == 8 else np.float32))
+        ms_f = (ctypes.c_double * 8)()
+        ms_b = (ctypes.c_double * 8)()
+        nf = L.p3dfft_gb300_profile_stages(f.handle, ctypes.c_void_p(d_x.ptr), ctypes.c_void_p(d_s.ptr), -1,
+                                          max(5, steps), ms_f, 8)
+        nb = L.p3dfft_gb300_profile_stages(b.handle, ctypes.c_void_p(d_s.ptr), ctypes.c_void_p(d_y.ptr), -1,
+                                          max(5, steps), ms_b, 8)
+        stages = []
+        for plan, msv, n in ((f, ms_f, nf), (b, ms_b, nb)):
+            for i, st in enumerate(plan.stages(executed=True)[:n]):
+                stages.append({"dim": st["dim"], "type": st["type"], "ms": round(msv[i], 4)})
+        ms = sum(st["ms"] for st in stages)
+        alg = 2 * s_r + 10 * s_c
+        key = ("fp64_float_float" if arith else "fp64_native") if prec == 8 else "fp32"
+        out[key] = {"ms_per_round_trip": ms, "GB_per_s": alg / (ms * 1e-3) / 1e9, "stages": stages}
+        del d_x, d_s, d_y, f, b
+    return out
 
 
 def serve_workload(p3d, n_jobs=10000, seed=5, fractions=(0.5, 0.75, 0.9), nslots=16, budget=120 << 30):
@@ -643,14 +711,17 @@ def main():
             dt1 = 1 if st["type"] in (5,) else 2
             dt2 = 1 if st["type"] in (7,) else 2
             bytes_ = 8 * (dt1 * int(np.prod(st["gdims1"])) + dt2 * int(np.prod(st["gdims2"])))
+            # complex FFT points of the stage (an even-length R2C / C2R runs a half-length FFT)
+            pts = int(np.prod(st["gdims1"] if dt2 == 2 else st["gdims2"])) // (2 if st["type"] in (5, 7) else 1)
             stages.append({"dim": st["dim"], "type": st["type"], "ms": msv[i], "bytes": bytes_,
-                           "kernel": kernel_id(st, arith, GD)})
+                           "points": pts, "kernel": kernel_id(st, arith, GD)})
     # dominant kernel = the instantiation with the largest total time per step
     per_kernel = {}
     for s in stages:
-        agg = per_kernel.setdefault(s["kernel"], {"ms": 0.0, "bytes": 0, "launches": 0})
+        agg = per_kernel.setdefault(s["kernel"], {"ms": 0.0, "bytes": 0, "points": 0, "launches": 0})
         agg["ms"] += s["ms"]
         agg["bytes"] += s["bytes"]
+        agg["points"] += s["points"]
         agg["launches"] += 1
     kernel_key = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
     dk = per_kernel[kernel_key]
@@ -663,6 +734,18 @@ def main():
                 "ms_per_launch": dk["ms"] / dk["launches"], "step_share": dk["ms"] / sum(s["ms"] for s in stages),
                 "whole_step_frac": value / world / peak,
                 "stages_ms": [round(s["ms"], 4) for s in stages]}
+    # float-float kernels are bound by FP32-pipe instruction issue: warp instructions per launch
+    # (ncu count per point x the launch's points) over the live duration, against 4 warp
+    # instructions per SM per clock at the median SM clock sampled during the timed region
+    ipp = load_instr(kernel_key) if arith else None
+    n_sm = L.p3dfft_gb300_sm_count()
+    if ipp and n_sm and clocks.get("sm_mhz"):
+        inst = ipp * dk["points"] / dk["launches"]
+        ach = inst / (roofline["ms_per_launch"] * 1e-3)
+        pk = 4.0 * n_sm * clocks["sm_mhz"] * 1e6
+        roofline["issue"] = {"bound": "fp32-pipe instruction issue", "achieved": ach, "peak": pk,
+                             "unit": "warp-inst/s", "frac": ach / pk, "warp_inst_per_launch": inst,
+                             "warp_inst_per_point": ipp, "sms": n_sm, "sm_mhz": clocks["sm_mhz"]}
 
     # ---- e2e: pinned host buffers through the public API ----
     hin = p3d.PinnedArray(p3d.storage_shape(GD, MO1), np.float64)
@@ -726,6 +809,7 @@ def main():
                      "round_trips_per_s": 1e3 / ms32, "speedup_vs_fp64_transforms_per_s": ms_step / ms32,
                      "rel_l2_vs_fp64": float(np.linalg.norm(y32 - y) / np.linalg.norm(y))}
     del d_in32, d_spec32, d_out32, f32, b32
+    forms["mixed_types_384x256x257"] = mixed_types_workload(p3d, L, max(5, args.steps // 5), arith)
     if not args.no_batch:
         del d_in, d_spec, d_out  # free HBM for the batch buffers
         forms["batched_uneven"] = batch_workload(p3d, L, max(3, min(args.steps, 10)), 3)

@@ -182,6 +182,8 @@ void p3dfft_gb300_host_free_pinned(void *p);
 int p3dfft_gb300_memcpy_h2d(void *dst, const void *src, long long bytes);
 int p3dfft_gb300_memcpy_d2h(void *dst, const void *src, long long bytes);
 int p3dfft_gb300_synchronize(void);
+/* streaming multiprocessors of the library's device (0 when no device is usable) */
+int p3dfft_gb300_sm_count(void);
 /* library version string */
 const char *p3dfft_gb300_version(void);
 

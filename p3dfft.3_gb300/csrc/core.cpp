@@ -1566,6 +1566,13 @@ int p3dfft_gb300_memcpy_d2h(void *dst, const void *src, long long bytes) {
 }
 int p3dfft_gb300_synchronize(void) { return cudaStreamSynchronize(g_stream) == cudaSuccess ? E_OK : E_CUDA; }
 
+int p3dfft_gb300_sm_count(void) {
+  int dev = 0, n = 0;
+  if (!ensure_device() || cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  return n;
+}
+
 // ==========================================================================================
 // Reference C ABI (Cwrap.h, build/wrap.C:85-571)
 

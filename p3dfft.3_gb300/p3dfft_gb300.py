@@ -78,7 +78,7 @@ def lib():
         "p3dfft_gb300_device_alloc": ([ctypes.c_longlong], vp), "p3dfft_gb300_device_free": ([vp], None),
         "p3dfft_gb300_memcpy_h2d": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
         "p3dfft_gb300_memcpy_d2h": ([vp, vp, ctypes.c_longlong], ctypes.c_int),
-        "p3dfft_gb300_synchronize": ([], ctypes.c_int), "p3dfft_gb300_version": ([], ctypes.c_char_p),
+        "p3dfft_gb300_synchronize": ([], ctypes.c_int), "p3dfft_gb300_sm_count": ([], ctypes.c_int), "p3dfft_gb300_version": ([], ctypes.c_char_p),
         "p3dfft_gb300_host_alloc_pinned": ([ctypes.c_longlong], vp), "p3dfft_gb300_host_free_pinned": ([vp], None),
         "p3dfft_gb300_exec3d_noalloc": ([ctypes.c_int, vp, vp, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_noalloc_max_field_bytes": ([], ctypes.c_longlong),
