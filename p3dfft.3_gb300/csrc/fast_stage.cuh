@@ -15,6 +15,9 @@
 //   - Stockham passes of radix 8/4/2 then 5/3 in registers, one padded shared-memory scatter
 //     per pass; in a pass of radix R each thread does ceil(N/R / T) butterflies
 //   - R2C / C2R half-length packing and the fused i*k derivative are done on the way in / out
+//   - DCT-I / DST-I (FFTW REDFT00 / RODFT00) are the FFT of the line's even / odd extension,
+//     built on the way in; real lines are transformed two at a time as the real and imaginary
+//     parts of one complex line (both transforms are real-linear)
 #pragma once
 #include <cuda_runtime.h>
 
@@ -23,7 +26,7 @@
 
 namespace p3d {
 
-enum FastKind { FK_C2C = 0, FK_R2C = 1, FK_C2R = 2 };
+enum FastKind { FK_C2C = 0, FK_R2C = 1, FK_C2R = 2, FK_R2R1 = 3 };
 
 struct FParams {
   const void *in;
@@ -36,6 +39,9 @@ struct FParams {
   int sign;                          // C2C: -1 forward, +1 backward
   int deriv, dg, dmid;               // fused derivative (compute_deriv_loc wavenumbers)
   int load_Lmajor, store_Lmajor;
+  // FK_R2R1: r2r_odd 0 DCT-I (N = 2(n-1)), 1 DST-I (N = 2(n+1)); pair 1 for real lines, taken
+  // two at a time (lines 2g and 2g+1 of nreal form FFT line g), 0 for complex lines
+  int r2r_odd, pair, nreal;
 };
 
 // resident 256-thread CTAs per SM the register allocation is sized for (FP64 and float-float;
@@ -53,6 +59,13 @@ struct FParams {
   X(75) X(80) X(81) X(90) X(96) X(100) X(108) X(120) X(125) X(128) X(135) X(144) X(150) X(160) X(162)    \
   X(180) X(192) X(200) X(216) X(225) X(240) X(243) X(250) X(256) X(270) X(288) X(300) X(320) X(324)      \
   X(360) X(375) X(384) X(400) X(405) X(432) X(450) X(480) X(486) X(500) X(512) X(1024) X(2048)
+
+// The even lengths (FFT lengths of DCT-I / DST-I extensions).
+#define P3D_FAST_EVEN_LENGTHS(X)                                                                         \
+  X(16) X(18) X(20) X(24) X(30) X(32) X(36) X(40) X(48) X(50) X(54) X(60) X(64) X(72) X(80) X(90) X(96)   \
+  X(100) X(108) X(120) X(128) X(144) X(150) X(160) X(162) X(180) X(192) X(200) X(216) X(240) X(250)     \
+  X(256) X(270) X(288) X(300) X(320) X(324) X(360) X(384) X(400) X(432) X(450) X(480) X(486) X(500)     \
+  X(512) X(1024) X(2048)
 
 // Radix plan: radix-8 passes, the leftover power of two (4 or 2), then 5s, then 3s.
 struct RadixList {
@@ -317,7 +330,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   using G = typename O::G;
   using RAW = typename O::RAW;
   using SH = FastShape<N>;
-  constexpr int TWSTEP = (KIND == FK_C2C) ? 1 : 2;  // FFT twiddle W_N^m = tab[m * TWSTEP]
+  constexpr int TWSTEP = (KIND == FK_C2C || KIND == FK_R2R1) ? 1 : 2;  // FFT twiddle W_N^m = tab[m * TWSTEP]
   constexpr int LS = fast_ls<N, (int)sizeof(C)>(), TB = SH::TB, TT = SH::T, V = SH::V;
   constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -353,33 +366,59 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     const int g0 = tile * TB;
     const int gl = g0 + l;
     const bool act = valid && gl < p.nlines;
-    const int lt = gl % p.dt, lo = gl / p.dt;
-    const long long ibase = (long long)lt * p.it + (long long)lo * p.io;
+    // element offset of line g's first point; paired real lines: lines 2g and 2g+1 (the last
+    // line of an odd count is paired with itself and its second result is not stored)
+    auto line_base = [&](int g, long long st, long long so) -> long long {
+      return (long long)(g % p.dt) * st + (long long)(g / p.dt) * so;
+    };
+    long long ibase, ibase2 = 0;
+    if (KIND == FK_R2R1 && p.pair) {
+      ibase = line_base(2 * gl, p.it, p.io);
+      ibase2 = line_base(min(2 * gl + 1, p.nreal - 1), p.it, p.io);
+    } else {
+      ibase = line_base(gl, p.it, p.io);
+    }
+    // raw value of FFT input point j of this thread's line
+    const G *src = gin + ((KIND == FK_R2C || (KIND == FK_R2R1 && p.pair)) ? ibase : 2 * ibase);
+    auto load_raw = [&](int j) -> RAW {
+      if constexpr (KIND == FK_R2C) {  // packed z[j] = x[2j] + i x[2j+1]
+        if (p.iL == 1) return O::ldraw(src + 2 * j);
+        return O::ldraw2(src + (long long)(2 * j) * p.iL, src + (long long)(2 * j + 1) * p.iL);
+      } else if constexpr (KIND == FK_R2R1) {
+        // even extension x[0..n-1], x[n-2..1]; odd extension 0, x[0..n-1], 0, -x[n-1..0]
+        int m = j;
+        bool neg = false;
+        if (!p.r2r_odd) {
+          if (j > N / 2) m = N - j;
+        } else {
+          if (j == 0 || j == N / 2) return RAW{};
+          if (j < N / 2) m = j - 1;
+          else {
+            m = N - j - 1;
+            neg = true;
+          }
+        }
+        RAW r = p.pair ? O::ldraw2(src + (long long)m * p.iL, gin + ibase2 + (long long)m * p.iL)
+                       : O::ldraw(src + 2 * (long long)m * p.iL);
+        return neg ? O::rneg(r) : r;
+      } else {
+        return O::ldraw(src + 2 * (long long)j * p.iL);
+      }
+    };
 
     C *lb = buf + (size_t)l * LS;
-    const int fsign = KIND == FK_C2C ? p.sign : (KIND == FK_R2C ? -1 : 1);
+    const int fsign = KIND == FK_C2C ? p.sign : ((KIND == FK_R2C || KIND == FK_R2R1) ? -1 : 1);
     constexpr RadixList RL = fast_radices(N);
     // Native arithmetic, no C2R packing, and a first radix equal to the points per thread: the
     // values a thread loads are exactly the inputs of its first butterfly, so the first pass runs
     // on them in registers and the tile's first trip through shared memory is skipped.
-    constexpr bool FUSE1 = !O::SCALED && KIND != FK_C2R && RL.r[0] == V;
+    constexpr bool FUSE1 = !O::SCALED && KIND != FK_C2R && KIND != FK_R2R1 && RL.r[0] == V;
     if constexpr (FUSE1) {
       constexpr int R0 = RL.r[0];
       C x[V];
       if (act) {
-        const G *src = gin + (KIND == FK_R2C ? ibase : 2 * ibase);
 #pragma unroll
-        for (int e = 0; e < V; e++) {
-          const int j = j0 + e * TT;
-          RAW r;
-          if (KIND == FK_R2C) {
-            if (p.iL == 1) r = O::ldraw(src + 2 * j);
-            else r = O::ldraw2(src + (long long)(2 * j) * p.iL, src + (long long)(2 * j + 1) * p.iL);
-          } else {
-            r = O::ldraw(src + 2 * (long long)j * p.iL);
-          }
-          x[e] = O::from_raw(r, 0);
-        }
+        for (int e = 0; e < V; e++) x[e] = O::from_raw(load_raw(j0 + e * TT), 0);
         if constexpr (R0 == 3) dft3<O>(x, fsign, O::tw(tab, (N / 3) * TWSTEP));
         else if constexpr (R0 == 5) dft5<O>(x, fsign, O::tw(tab, (N / 5) * TWSTEP), O::tw(tab, 2 * (N / 5) * TWSTEP));
         else dft_p2<O, R0>(x, fsign);
@@ -399,18 +438,30 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     RAW *lr = reinterpret_cast<RAW *>(lb);
     int emax = 0;
     const int pj0 = pad<PS>(j0);
-    if (act) {
-      const G *src = gin + (KIND == FK_R2C ? ibase : 2 * ibase);
+    if (act && KIND == FK_R2R1) {
+      // extensions: each input element is read once and written to slots j and N - j
+      const int pn0 = pad<PS>(N - j0);
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int j = j0 + e * TT;
+        if (j > N / 2) return;
+        const RAW r = load_raw(j);
+        const bool mirror = j > 0 && j < N / 2;
+        const RAW rm = (mirror && p.r2r_odd) ? O::rneg(r) : r;
         const int sj = fk_slot<PS, TT>(j0, pj0, e);
-        RAW r;
-        if (KIND == FK_R2C) {  // packed z[j] = x[2j] + i x[2j+1]
-          if (p.iL == 1) r = O::ldraw(src + 2 * j);
-          else r = O::ldraw2(src + (long long)(2 * j) * p.iL, src + (long long)(2 * j + 1) * p.iL);
+        const int sm = mirror ? fk_slot_rev<PS, TT, N>(j0, pn0, e) : sj;
+        if (O::SCALED) {
+          emax = max(emax, O::rexp(r));
+          lr[sj] = r;
+          lr[sm] = rm;
         } else {
-          r = O::ldraw(src + 2 * (long long)j * p.iL);
+          lb[sj] = O::from_raw(r, 0);
+          lb[sm] = O::from_raw(rm, 0);
         }
+      });
+    } else if (act) {
+      fk_for<V, O::IO_UNROLL>([&](int e) {
+        const int sj = fk_slot<PS, TT>(j0, pj0, e);
+        const RAW r = load_raw(j0 + e * TT);
         if (O::SCALED) {
           emax = max(emax, O::rexp(r));
           lr[sj] = r;
@@ -491,7 +542,15 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     const bool sact = valid && gs < p.nlines;
     if (sact) {
       const C *Y = buf + (size_t)ls * LS;
-      const long long obase = (long long)(gs % p.dt) * p.ot + (long long)(gs / p.dt) * p.oo;
+      long long obase, obase2 = 0;
+      bool second = false;  // paired real lines: the second line exists
+      if (KIND == FK_R2R1 && p.pair) {
+        obase = line_base(2 * gs, p.ot, p.oo);
+        second = 2 * gs + 1 < p.nreal;
+        obase2 = second ? line_base(2 * gs + 1, p.ot, p.oo) : 0;
+      } else {
+        obase = line_base(gs, p.ot, p.oo);
+      }
       const int pjs = pad<PS>(js), pns = pad<PS>(N - js);
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int k = js + e * TT;
@@ -508,6 +567,25 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
             C z0 = Y[pad<PS>(0)];
             C xn = O::mk(O::norm(O::sub(O::mk(z0.x, O::rzero()), O::mk(z0.y, O::rzero()))).x, O::rzero());
             O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc_out));
+          }
+        } else if (KIND == FK_R2R1) {
+          // DCT-I: Y[k], k <= N/2; DST-I: i Y[k+1], k < N/2 - 1
+          int ko = k;
+          C y = Y[sk];
+          if (!p.r2r_odd) {
+            if (k > N / 2) return;
+          } else {
+            if (k == 0 || k >= N / 2) return;
+            ko = k - 1;
+            y = O::muli(y);
+          }
+          const RAW r = O::to_raw(y, sc_out);
+          if (!p.pair) {
+            O::straw(gout + 2 * (obase + (long long)ko * p.oL), r);
+          } else if (second) {
+            O::straw2(gout + obase + (long long)ko * p.oL, gout + obase2 + (long long)ko * p.oL, r);
+          } else {
+            O::strawx(gout + obase + (long long)ko * p.oL, r);
           }
         } else {  // C2R: reals 2k, 2k+1 = z[k]
           RAW r = O::to_raw(Y[sk], sc_out);
@@ -582,17 +660,28 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
     int rc = E_OK;
 #define P3D_FAST_CASE(L) \
   if (fk_configure<O, KIND, L>() != E_OK) rc = E_CUDA;
-    P3D_FAST_LENGTHS(P3D_FAST_CASE)
+    if constexpr (KIND == FK_R2R1) {
+      P3D_FAST_EVEN_LENGTHS(P3D_FAST_CASE)
+    } else {
+      P3D_FAST_LENGTHS(P3D_FAST_CASE)
+    }
 #undef P3D_FAST_CASE
     return rc;
   }
-  switch (n) {
 #define P3D_FAST_CASE(L) \
   case L: return fk_launch<O, KIND, L>(p, g, ctas, st);
-    P3D_FAST_LENGTHS(P3D_FAST_CASE)
-#undef P3D_FAST_CASE
-    default: return E_UNSUPPORTED;
+  if constexpr (KIND == FK_R2R1) {
+    switch (n) {
+      P3D_FAST_EVEN_LENGTHS(P3D_FAST_CASE)
+      default: return E_UNSUPPORTED;
+    }
+  } else {
+    switch (n) {
+      P3D_FAST_LENGTHS(P3D_FAST_CASE)
+      default: return E_UNSUPPORTED;
+    }
   }
+#undef P3D_FAST_CASE
 }
 
 // One (arithmetic, kind) pair per translation unit (fast_inst.cu), so they compile in parallel.
@@ -604,12 +693,15 @@ int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStr
 P3D_FAST_DECL(DF, FK_C2C)
 P3D_FAST_DECL(DF, FK_R2C)
 P3D_FAST_DECL(DF, FK_C2R)
+P3D_FAST_DECL(DF, FK_R2R1)
 P3D_FAST_DECL(Native<double>, FK_C2C)
 P3D_FAST_DECL(Native<double>, FK_R2C)
 P3D_FAST_DECL(Native<double>, FK_C2R)
+P3D_FAST_DECL(Native<double>, FK_R2R1)
 P3D_FAST_DECL(Native<float>, FK_C2C)
 P3D_FAST_DECL(Native<float>, FK_R2C)
 P3D_FAST_DECL(Native<float>, FK_C2R)
+P3D_FAST_DECL(Native<float>, FK_R2R1)
 #undef P3D_FAST_DECL
 
 template <class O>
@@ -618,6 +710,7 @@ inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaS
     case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, g, ctas, st);
     case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, g, ctas, st);
     case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, g, ctas, st);
+    case FK_R2R1: return fast_launch_kind<O, FK_R2R1>(a.n, a.p, g, ctas, st);
     default: return E_UNSUPPORTED;
   }
 }
@@ -626,7 +719,7 @@ inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaS
 inline int fast_preload(int prec, int arith) {
   FastArgs a{};
   int rc = E_OK;
-  for (int k = FK_C2C; k <= FK_C2R; k++) {
+  for (int k = FK_C2C; k <= FK_R2R1; k++) {
     a.kind = k;
     a.n = 0;
     int r;
@@ -647,7 +740,8 @@ inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, 
   return fast_launch_arith<Native<double>>(a, g, ctas, st);
 }
 
-inline bool fast_supported(int n) {
+inline bool fast_supported(int n, int kind = FK_C2C) {
+  if (kind == FK_R2R1 && n % 2) return false;
   switch (n) {
 #define P3D_FAST_CASE(L) case L:
     P3D_FAST_LENGTHS(P3D_FAST_CASE)

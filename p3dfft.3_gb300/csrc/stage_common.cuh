@@ -120,6 +120,12 @@ struct Native {
     *p0 = r.x;
     *p1 = r.y;
   }
+  static __device__ __forceinline__ void strawx(G *p, RAW r) { *p = r.x; }  // real part only
+  static __device__ __forceinline__ RAW rneg(RAW r) {
+    r.x = -r.x;
+    r.y = -r.y;
+    return r;
+  }
 };
 
 // float-float arithmetic for FP64 data (see df_arith.cuh)
@@ -197,6 +203,12 @@ struct DF {
   static __device__ __forceinline__ void straw2(G *p0, G *p1, RAW r) {
     *reinterpret_cast<long long *>(p0) = r.x;
     *reinterpret_cast<long long *>(p1) = r.y;
+  }
+  static __device__ __forceinline__ void strawx(G *p, RAW r) { *reinterpret_cast<long long *>(p) = r.x; }
+  static __device__ __forceinline__ RAW rneg(RAW r) {  // flip both sign bits
+    r.x ^= (long long)0x8000000000000000ull;
+    r.y ^= (long long)0x8000000000000000ull;
+    return r;
   }
   static __device__ __forceinline__ C tws(const T *t, int k) { return t[k]; }
   static __device__ __forceinline__ C tw(const T *t, int k) {

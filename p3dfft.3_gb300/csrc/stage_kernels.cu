@@ -879,9 +879,11 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   const uintptr_t align_need = (d.prec == 8) ? 16 : 8;
   const bool aligned = (((uintptr_t)in | (uintptr_t)out) % align_need) == 0;
   const bool even = (p.nlog % 2) == 0;
-  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even);
+  // DCT-I / DST-I run as the FFT of the extended line (no fused derivative on that path)
+  const bool r2r1 = d.kind == K_R2R && (d.r2r == REDFT00 || d.r2r == RODFT00) && !(d.deriv && d.dt2 == 2);
+  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even) || r2r1;
   const bool generic_only = getenv("P3DFFT_GB300_GENERIC_ONLY") != nullptr;
-  const bool fast_ok = fast_kind && fast_supported(p.nfft) && aligned;
+  const bool fast_ok = fast_kind && fast_supported(p.nfft, r2r1 ? FK_R2R1 : FK_C2C) && aligned;
   if (d.engine == ENG_FAST && !fast_ok) return E_UNSUPPORTED;
   if (d.engine == ENG_FIXED && !fixed_engine_len(p.nfft)) return E_UNSUPPORTED;
   const bool use_fast = fast_ok && (d.engine == ENG_FAST || (d.engine == ENG_AUTO && !generic_only));
@@ -949,7 +951,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
 
   if (use_fast) {
     FastArgs fa;
-    fa.kind = (d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C);
+    fa.kind = r2r1 ? FK_R2R1 : ((d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C));
     fa.n = p.nfft;
     FParams &q = fa.p;
     q.in = in;
@@ -964,8 +966,12 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.oo = p.oo;
     q.dt = p.dt;
     const int TB = fast_tile_lines(p.nfft);
-    const long long nl = (long long)p.dt * p.dother;
-    if (nl + TB > 0x7fffffffLL) return E_TOO_LARGE;
+    const long long nreal = (long long)p.dt * p.dother;
+    q.r2r_odd = (r2r1 && d.r2r == RODFT00) ? 1 : 0;
+    q.pair = (r2r1 && !p.in_complex) ? 1 : 0;  // real lines, two per FFT line
+    const long long nl = q.pair ? (nreal + 1) / 2 : nreal;
+    if (2 * nreal + TB > 0x7fffffffLL) return E_TOO_LARGE;
+    q.nreal = (int)nreal;
     q.nlines = (int)nl;
     q.ntotal = (int)((nl + TB - 1) / TB);
     q.sign = p.sign;
@@ -1075,7 +1081,7 @@ static std::vector<long long> fast_key(const StageLaunch &st, const FastArgs &fa
   const FParams &q = fa.p;
   return {st.d.prec, st.d.prec == 8 ? st.arith : 0, fa.kind, fa.n, (long long)(uintptr_t)q.tw,
           (long long)(uintptr_t)q.ptw, q.iL, q.it, q.io, q.oL, q.ot, q.oo, q.dt, q.nlines, q.ntotal, q.sign,
-          q.deriv, q.dg, q.dmid, q.load_Lmajor, q.store_Lmajor};
+          q.deriv, q.dg, q.dmid, q.load_Lmajor, q.store_Lmajor, q.r2r_odd, q.pair, q.nreal};
 }
 
 LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err) {
