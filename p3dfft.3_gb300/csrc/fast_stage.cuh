@@ -489,11 +489,13 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
 #pragma unroll
       for (int w = 0; w < SH::BLOCK / 32; w++) emax = max(emax, red[w]);
       sc = 1043 - emax;
-      if (act && KIND != FK_C2R) {
+      // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
+      if (act) {
         fk_for<V, O::IO_UNROLL>([&](int e) {
           const int j = fk_slot<PS, TT>(j0, pj0, e);
           lb[j] = O::from_raw(lr[j], sc);
         });
+        if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
       }
     }
     if (KIND == FK_C2R) {
@@ -506,14 +508,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         for (int e = 0; e < V; e++) {
           const int k = j0 + e * TT;
           const int sa = fk_slot<PS, TT>(j0, pj0, e), sb = fk_slot_rev<PS, TT, N>(j0, pn0, e);
-          C a, b;
-          if (O::SCALED) {
-            a = O::from_raw(lr[sa], sc);
-            b = O::from_raw(lr[sb], sc);
-          } else {
-            a = lb[sa];
-            b = lb[sb];
-          }
+          C a = lb[sa], b = lb[sb];
           if (k == 0) {
             a.y = O::rzero();
             b.y = O::rzero();
