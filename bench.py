@@ -266,7 +266,7 @@ def kernel_id(stage, arith, n_dims):
     kind = {5: 1, 7: 2}.get(stage["type"], 0)  # R2C_D, C2R_D, else C2C
     n = stage["gdims1"][stage["dim"]] if kind != 2 else stage["gdims2"][stage["dim"]]
     nfft = n // 2 if kind else n
-    return f"k_fast<{'DF' if arith else 'Native<double>'},{kind},{nfft}>"
+    return f"k_fast<{'DFP' if arith else 'Native<double>'},{kind},{nfft}>"
 
 
 # ------------------------------------------------------------------------------------------

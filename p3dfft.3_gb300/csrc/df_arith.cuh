@@ -225,4 +225,73 @@ __device__ __forceinline__ long long ff_to_double_bits(ff v) {
   return (long long)(sign | ((unsigned long long)(eh + 1023) << 52) | ((unsigned long long)S & 0xfffffffffffffull));
 }
 
+// ------------------------------------------------------------------------------------------
+// Packed float-float complex values for the FP32x2 instructions of sm_100 and later
+// (add/sub/mul/fma .f32x2: two FP32 operations per instruction issue).  A complex value keeps
+// its real and imaginary parts side by side, hi = (re.hi, im.hi) and lo = (re.lo, im.lo), so the
+// componentwise operations of an FFT (sums, differences, real scalings) issue once for both parts.
+// The arithmetic of each lane is that of the scalar float-float operations above.
+struct __align__(16) pcf {
+  float2 hi, lo;
+};
+// A twiddle w = wx + i wy in product form: xh = (wx.hi, wx.hi), yh = (-wy.hi, wy.hi), and the same
+// for the lo parts, so that a * w = a (wx, wx) + swap(a) (-wy, wy) lane by lane.
+struct __align__(16) pcw {
+  float2 xh, yh, xl, yl;
+};
+
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  unsigned long long ua = *reinterpret_cast<const unsigned long long *>(&a);
+  unsigned long long ub = *reinterpret_cast<const unsigned long long *>(&b);
+  unsigned long long ud;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(ud) : "l"(ua), "l"(ub));
+  return *reinterpret_cast<const float2 *>(&ud);
+}
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2swap(float2 a) { return make_float2(a.y, a.x); }
+__device__ __forceinline__ float2 f2dup(float a) { return make_float2(a, a); }
+
+// unnormalised sum / difference (TwoSum on the hi parts, as ff_add_nn)
+__device__ __forceinline__ pcf pcf_add_nn(pcf a, pcf b) {
+  const float2 s = f2add(a.hi, b.hi);
+  const float2 bb = f2sub(s, a.hi);
+  const float2 e = f2add(f2sub(a.hi, f2sub(s, bb)), f2sub(b.hi, bb));
+  return pcf{s, f2add(e, f2add(a.lo, b.lo))};
+}
+__device__ __forceinline__ pcf pcf_sub_nn(pcf a, pcf b) {
+  const float2 s = f2sub(a.hi, b.hi);
+  const float2 bb = f2sub(s, a.hi);
+  const float2 e = f2sub(f2sub(a.hi, f2sub(s, bb)), f2add(b.hi, bb));
+  return pcf{s, f2add(e, f2sub(a.lo, b.lo))};
+}
+__device__ __forceinline__ pcf pcf_norm(pcf a) {
+  const float2 h = f2add(a.hi, a.lo);
+  return pcf{h, f2sub(a.lo, f2sub(h, a.hi))};
+}
+// a * w, unnormalised (the terms of cff_mul_nn, lane by lane)
+__device__ __forceinline__ pcf pcf_mul_nn(pcf a, const pcw &w) {
+  const float2 as = f2swap(a.hi), als = f2swap(a.lo);
+  const float2 p = f2mul(a.hi, w.xh), q = f2mul(as, w.yh);
+  const float2 e1 = f2fma(a.hi, w.xh, f2neg(p)), e2 = f2fma(as, w.yh, f2neg(q));
+  const float2 s = f2add(p, q), bb = f2sub(s, p);
+  const float2 e3 = f2add(f2sub(p, f2sub(s, bb)), f2sub(q, bb));
+  float2 lo = f2add(f2add(e1, e2), e3);
+  lo = f2fma(a.hi, w.xl, lo);
+  lo = f2fma(a.lo, w.xh, lo);
+  lo = f2fma(as, w.yl, lo);
+  lo = f2fma(als, w.yh, lo);
+  return pcf{s, lo};
+}
+// a * (c.hi + c.lo) for a real float-float c, unnormalised
+__device__ __forceinline__ pcf pcf_rmul_nn(pcf a, float2 ch, float2 cl) {
+  const float2 p = f2mul(a.hi, ch);
+  float2 e = f2fma(a.hi, ch, f2neg(p));
+  e = f2fma(a.hi, cl, e);
+  e = f2fma(a.lo, ch, e);
+  return pcf{p, e};
+}
+
 }  // namespace p3d

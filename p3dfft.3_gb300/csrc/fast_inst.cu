@@ -9,7 +9,7 @@
 
 namespace p3d {
 #if P3D_FAST_ARITH == 0
-using FastArith = DF;
+using FastArith = DFP;
 #elif P3D_FAST_ARITH == 1
 using FastArith = Native<double>;
 #else

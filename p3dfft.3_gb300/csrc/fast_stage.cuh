@@ -192,8 +192,8 @@ __host__ __device__ constexpr int fast_pass_entries(int N) { return fast_pass_of
 // resident across the CTAs of an SM); a shared-memory copy per CTA was measured to cost more
 // registers and L2 traffic than it saves.
 template <class O>
-__device__ __forceinline__ typename O::C fk_tw(const typename O::T *tab, int m, int sign) {
-  typename O::C w = O::tw(tab, m);
+__device__ __forceinline__ typename O::W fk_tw(const typename O::T *tab, int m, int sign) {
+  const typename O::W w = O::tw(tab, m);
   return sign < 0 ? w : O::conj(w);
 }
 
@@ -211,7 +211,7 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
   constexpr int NB = (M + T - 1) / T;  // butterflies per thread
   constexpr bool GUARD = (M % T) != 0;
   C v[NB * R];
-  C w1, w2;  // W_R^1, W_R^2 for the odd radices
+  typename O::W w1, w2;  // W_R^1, W_R^2 for the odd radices
   if constexpr (R == 3 || R == 5) w1 = O::tw(tab, (N / R) * TWSTEP);
   if constexpr (R == 5) w2 = O::tw(tab, 2 * (N / R) * TWSTEP);
   if (active) {
@@ -510,13 +510,13 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           const int sa = fk_slot<PS, TT>(j0, pj0, e), sb = fk_slot_rev<PS, TT, N>(j0, pn0, e);
           C a = lb[sa], b = lb[sb];
           if (k == 0) {
-            a.y = O::rzero();
-            b.y = O::rzero();
+            a = O::mk(O::re(a), O::rzero());
+            b = O::mk(O::re(b), O::rzero());
           }
           C bc = O::conj(b);
           C s = O::add(a, bc), d = O::sub(a, bc);
-          C w = O::conj(O::tw(tab, k));
-          z[e] = O::norm(O::add(s, O::muli(O::mul(w, d))));
+          const typename O::W w = O::conj(O::tw(tab, k));
+          z[e] = O::norm(O::add(s, O::muli(O::mul(d, w))));
         }
       }
       __syncthreads();
@@ -556,11 +556,11 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           // X[k] = 1/2 [(Z_k + conj Z_{N-k}) - i W_2N^k (Z_k - conj Z_{N-k})]
           C a = Y[sk], b = O::conj(Y[k == 0 ? 0 : fk_slot_rev<PS, TT, N>(js, pns, e)]);
           C s = O::add(a, b), d = O::sub(a, b);
-          C x = O::half(O::sub(s, O::muli(O::mul(O::tw(tab, k), d))));
+          C x = O::half(O::sub(s, O::muli(O::mul(d, O::tw(tab, k)))));
           O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
           if (k == 0) {  // X[N] = Re Z_0 - Im Z_0
             C z0 = Y[pad<PS>(0)];
-            C xn = O::mk(O::norm(O::sub(O::mk(z0.x, O::rzero()), O::mk(z0.y, O::rzero()))).x, O::rzero());
+            C xn = O::mk(O::re(O::norm(O::sub(O::mk(O::re(z0), O::rzero()), O::mk(O::im(z0), O::rzero())))), O::rzero());
             O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc_out));
           }
         } else if (KIND == FK_R2R1) {
@@ -685,10 +685,10 @@ int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStr
 #define P3D_FAST_DECL(O, K) \
   template <>               \
   int fast_launch_kind<O, K>(int, const FParams &, const FGroup *, int, cudaStream_t);
-P3D_FAST_DECL(DF, FK_C2C)
-P3D_FAST_DECL(DF, FK_R2C)
-P3D_FAST_DECL(DF, FK_C2R)
-P3D_FAST_DECL(DF, FK_R2R1)
+P3D_FAST_DECL(DFP, FK_C2C)
+P3D_FAST_DECL(DFP, FK_R2C)
+P3D_FAST_DECL(DFP, FK_C2R)
+P3D_FAST_DECL(DFP, FK_R2R1)
 P3D_FAST_DECL(Native<double>, FK_C2C)
 P3D_FAST_DECL(Native<double>, FK_R2C)
 P3D_FAST_DECL(Native<double>, FK_C2R)
@@ -719,7 +719,7 @@ inline int fast_preload(int prec, int arith) {
     a.n = 0;
     int r;
     if (prec == 4) r = fast_launch_arith<Native<float>>(a, nullptr, 0, 0);
-    else if (arith == AR_DF) r = fast_launch_arith<DF>(a, nullptr, 0, 0);
+    else if (arith == AR_DF) r = fast_launch_arith<DFP>(a, nullptr, 0, 0);
     else r = fast_launch_arith<Native<double>>(a, nullptr, 0, 0);
     if (r != E_OK) rc = r;
   }
@@ -731,7 +731,7 @@ inline int fast_preload(int prec, int arith) {
 inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, const FGroup *g = nullptr,
                        int ctas = 0) {
   if (prec == 4) return fast_launch_arith<Native<float>>(a, g, ctas, st);
-  if (arith == AR_DF) return fast_launch_arith<DF>(a, g, ctas, st);
+  if (arith == AR_DF) return fast_launch_arith<DFP>(a, g, ctas, st);
   return fast_launch_arith<Native<double>>(a, g, ctas, st);
 }
 

@@ -12,13 +12,13 @@
 namespace p3d {
 
 // Loads / stores per thread that the specialised kernels keep in flight together (loop unroll
-// of their global-memory I/O): all of them for the native types; fewer for float-float, whose
-// raw values are wide and whose kernels are bound by instruction issue rather than latency.
+// of their global-memory I/O).  All of a thread's points for every arithmetic: with the packed
+// FP32x2 float-float arithmetic those kernels are latency- rather than issue-bound as well.
 #ifndef FAST_IO_UNROLL_NATIVE
 #define FAST_IO_UNROLL_NATIVE 8
 #endif
 #ifndef FAST_IO_UNROLL_DF
-#define FAST_IO_UNROLL_DF 4
+#define FAST_IO_UNROLL_DF 8
 #endif
 #ifndef FAST_TW_POWERS_FP32
 #define FAST_TW_POWERS_FP32 1
@@ -93,6 +93,12 @@ struct Native {
   }
   static __device__ __forceinline__ C norm(C a) { return a; }
   static __device__ __forceinline__ C tws(const T *t, int k) { return t[k]; }
+  // twiddles in registers are plain complex values; real and imaginary parts
+  using W = C;
+  static __device__ __forceinline__ S re(C a) { return a.x; }
+  static __device__ __forceinline__ S im(C a) { return a.y; }
+  static __device__ __forceinline__ S wre(C w) { return w.x; }
+  static __device__ __forceinline__ S wim(C w) { return w.y; }
   // register-level I/O of the specialised kernels (no tile scaling for native arithmetic)
   static constexpr bool SCALED = false;
   static constexpr int IO_UNROLL = FAST_IO_UNROLL_NATIVE;
@@ -218,6 +224,95 @@ struct DF {
     c.y = ff{v.z, v.w};
     return c;
   }
+  using W = C;
+  static __device__ __forceinline__ S re(C a) { return a.x; }
+  static __device__ __forceinline__ S im(C a) { return a.y; }
+  static __device__ __forceinline__ S wre(C w) { return w.x; }
+  static __device__ __forceinline__ S wim(C w) { return w.y; }
+};
+
+// Float-float for FP64 data with packed FP32x2 arithmetic (the specialised kernels): the same
+// operations as DF, the real and imaginary parts issued together (df_arith.cuh, pcf).  Twiddle
+// tables hold pcw entries (table format 3).
+struct DFP {
+  using G = double;
+  using S = ff;
+  using C = pcf;
+  using T = pcw;
+  using W = pcw;
+  static __device__ __forceinline__ C mk(S a, S b) { return C{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+  static __device__ __forceinline__ S re(C a) { return ff{a.hi.x, a.lo.x}; }
+  static __device__ __forceinline__ S im(C a) { return ff{a.hi.y, a.lo.y}; }
+  static __device__ __forceinline__ C add(C a, C b) { return pcf_add_nn(a, b); }
+  static __device__ __forceinline__ C sub(C a, C b) { return pcf_sub_nn(a, b); }
+  static __device__ __forceinline__ C norm(C a) { return pcf_norm(a); }
+  static __device__ __forceinline__ C mul(C a, const W &w) { return pcf_mul_nn(a, w); }
+  static __device__ __forceinline__ C muli(C a) {
+    return C{make_float2(-a.hi.y, a.hi.x), make_float2(-a.lo.y, a.lo.x)};
+  }
+  static __device__ __forceinline__ C mulmi(C a) {
+    return C{make_float2(a.hi.y, -a.hi.x), make_float2(a.lo.y, -a.lo.x)};
+  }
+  static __device__ __forceinline__ C conj(C a) { return C{make_float2(a.hi.x, -a.hi.y), make_float2(a.lo.x, -a.lo.y)}; }
+  static __device__ __forceinline__ W conj(const W &w) { return W{w.xh, f2neg(w.yh), w.xl, f2neg(w.yl)}; }
+  static __device__ __forceinline__ C half(C a) { return C{f2mul(a.hi, f2dup(0.5f)), f2mul(a.lo, f2dup(0.5f))}; }
+  static __device__ __forceinline__ C neg(C a) { return C{f2neg(a.hi), f2neg(a.lo)}; }
+  static __device__ __forceinline__ C rsqrt2(C a) {
+    return pcf_rmul_nn(a, f2dup(FF_RSQRT2_HI), f2dup(FF_RSQRT2_LO));
+  }
+  static __device__ __forceinline__ C rmul(C a, S c) { return pcf_rmul_nn(a, f2dup(c.hi), f2dup(c.lo)); }
+  static __device__ __forceinline__ C iscale(C a, int k) {  // a * (i k), normalised like ff_mul_int
+    const float2 kk = make_float2(-(float)k, (float)k);
+    const float2 as = f2swap(a.hi);
+    const float2 p = f2mul(as, kk);
+    float2 e = f2fma(as, kk, f2neg(p));
+    e = f2fma(f2swap(a.lo), kk, e);
+    return pcf_norm(C{p, e});
+  }
+  static __device__ __forceinline__ S rzero() { return ff{0.f, 0.f}; }
+  static __device__ __forceinline__ C zero() { return C{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
+  static __device__ __forceinline__ S negs(S a) { return ff_neg(a); }
+  // twiddle re / im parts (the radix-3 and radix-5 butterflies' cos / sin constants)
+  static __device__ __forceinline__ S wre(const W &w) { return ff{w.xh.x, w.xl.x}; }
+  static __device__ __forceinline__ S wim(const W &w) { return ff{w.yh.y, w.yl.y}; }
+  static __device__ __forceinline__ W tw(const T *t, int k) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(t + k));
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(t + k) + 1);
+    return W{make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y), make_float2(b.z, b.w)};
+  }
+  static constexpr bool SCALED = true;
+  static constexpr int IO_UNROLL = FAST_IO_UNROLL_DF;
+  static constexpr bool TW_POWERS = false;
+  using RAW = longlong2;
+  static __device__ __forceinline__ RAW ldraw(const G *p) { return __ldg(reinterpret_cast<const longlong2 *>(p)); }
+  static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
+    RAW r;
+    r.x = __ldg(reinterpret_cast<const long long *>(p0));
+    r.y = __ldg(reinterpret_cast<const long long *>(p1));
+    return r;
+  }
+  static __device__ __forceinline__ int rexp(RAW r) { return max(dbl_biased_exp(r.x), dbl_biased_exp(r.y)); }
+  static __device__ __forceinline__ C from_raw(RAW r, int sc) {
+    return mk(ff_from_bits_scaled(r.x, sc), ff_from_bits_scaled(r.y, sc));
+  }
+  static __device__ __forceinline__ RAW to_raw(C v, int sc) {
+    const C n = pcf_norm(v);
+    RAW r;
+    r.x = ff_to_bits_scaled(ff{n.hi.x, n.lo.x}, sc);
+    r.y = ff_to_bits_scaled(ff{n.hi.y, n.lo.y}, sc);
+    return r;
+  }
+  static __device__ __forceinline__ void straw(G *p, RAW r) { *reinterpret_cast<longlong2 *>(p) = r; }
+  static __device__ __forceinline__ void straw2(G *p0, G *p1, RAW r) {
+    *reinterpret_cast<long long *>(p0) = r.x;
+    *reinterpret_cast<long long *>(p1) = r.y;
+  }
+  static __device__ __forceinline__ void strawx(G *p, RAW r) { *reinterpret_cast<long long *>(p) = r.x; }
+  static __device__ __forceinline__ RAW rneg(RAW r) {
+    r.x ^= (long long)0x8000000000000000ull;
+    r.y ^= (long long)0x8000000000000000ull;
+    return r;
+  }
 };
 
 
@@ -272,11 +367,11 @@ __device__ __forceinline__ void dft_p2(typename O::C *v, int sign) {
 // carry the table's precision.  Pairing x_j with x_{R-j} leaves one real multiply per constant:
 //   y_q = x0 + sum_j cos(2pi jq/R) (x_j + x_{R-j}) + sign*i sum_j sin(2pi jq/R) (x_j - x_{R-j}).
 template <class O>
-__device__ __forceinline__ void dft3(typename O::C *v, int sign, typename O::C w1) {
+__device__ __forceinline__ void dft3(typename O::C *v, int sign, const typename O::W &w1) {
   using C = typename O::C;
   const C a = O::add(v[1], v[2]), b = O::sub(v[1], v[2]);
   const C m = O::sub(v[0], O::half(a));  // x0 + cos(2pi/3) a, cos(2pi/3) = -1/2
-  C t = O::rmul(b, O::negs(w1.y));        // sin(2pi/3) b
+  C t = O::rmul(b, O::negs(O::wim(w1)));  // sin(2pi/3) b
   t = sign < 0 ? O::mulmi(t) : O::muli(t);
   v[0] = O::add(v[0], a);
   v[1] = O::add(m, t);
@@ -284,10 +379,10 @@ __device__ __forceinline__ void dft3(typename O::C *v, int sign, typename O::C w
 }
 
 template <class O>
-__device__ __forceinline__ void dft5(typename O::C *v, int sign, typename O::C w1, typename O::C w2) {
+__device__ __forceinline__ void dft5(typename O::C *v, int sign, const typename O::W &w1, const typename O::W &w2) {
   using C = typename O::C;
   using S = typename O::S;
-  const S c1 = w1.x, s1 = O::negs(w1.y), c2 = w2.x, s2 = O::negs(w2.y);
+  const S c1 = O::wre(w1), s1 = O::negs(O::wim(w1)), c2 = O::wre(w2), s2 = O::negs(O::wim(w2));
   const C a1 = O::add(v[1], v[4]), b1 = O::sub(v[1], v[4]);
   const C a2 = O::add(v[2], v[3]), b2 = O::sub(v[2], v[3]);
   const C m1 = O::add(v[0], O::add(O::rmul(a1, c1), O::rmul(a2, c2)));

@@ -554,7 +554,11 @@ __global__ void k_deriv(const R *in, R *out, long long n, int sd0, int sd1, int 
 // ------------------------------------------------------------------------------------------
 // Host side: twiddle tables W_N^k = exp(-2 pi i k / N), generated in long double and stored as
 // double pairs (fmt 0), float pairs (fmt 1) or float-float pairs (fmt 2).
-size_t table_bytes(int N, int fmt) { return (size_t)N * (fmt == 1 ? 8 : 16); }
+// bytes per table entry: format 0 double, 1 float, 2 float-float, 3 packed float-float in
+// product form (pcw: (c, c), (-s, s) for the hi parts, then the lo parts)
+static size_t entry_bytes(int fmt) { return fmt == 1 ? 8 : (fmt == 3 ? 32 : 16); }
+
+size_t table_bytes(int N, int fmt) { return (size_t)N * entry_bytes(fmt); }
 
 static const long double TWO_PI_L = 6.283185307179586476925286766559005768L;
 
@@ -566,10 +570,15 @@ static void put_value(unsigned char *host, size_t i, long double c, long double 
   } else if (fmt == 1) {
     float v[2] = {(float)c, (float)s};
     memcpy(&host[i * 8], v, 8);
-  } else {
+  } else if (fmt == 2) {
     float ch = (float)c, sh = (float)s;
     float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
     memcpy(&host[i * 16], v, 16);
+  } else {
+    const float ch = (float)c, sh = (float)s;
+    const float cl = (float)(c - (long double)ch), sl = (float)(s - (long double)sh);
+    float v[8] = {ch, ch, -sh, sh, cl, cl, -sl, sl};
+    memcpy(&host[i * 32], v, 32);
   }
 }
 
@@ -596,7 +605,7 @@ static int largest_prime_factor(int n) {
   return m > 1 ? std::max(lp, m) : lp;
 }
 
-size_t blue_table_bytes(int n, int fmt) { return (size_t)(3 * blue_len(n) + n) * (fmt == 1 ? 8 : 16); }
+size_t blue_table_bytes(int n, int fmt) { return (size_t)(3 * blue_len(n) + n) * entry_bytes(fmt); }
 
 // In-place forward DFT (exp(-2 pi i jk/M)) of a power-of-two length, in long double.
 static void ld_fft(std::vector<long double> &re, std::vector<long double> &im) {
@@ -661,7 +670,7 @@ void fill_table(int N, int fmt, void *dst) {
 }
 
 size_t pass_table_bytes(int N, int fmt) {
-  return (size_t)std::max(1, fast_pass_entries(N)) * (fmt == 1 ? 8 : 16);
+  return (size_t)std::max(1, fast_pass_entries(N)) * entry_bytes(fmt);
 }
 
 // Pass I >= 1: entry (r-1) Ns + k holds W_{Ns R}^{r k}, r = 1 .. R-1, k < Ns.
@@ -683,7 +692,7 @@ void fill_pass_table(int N, int fmt, void *dst) {
 // Kept resident per device; the map owns device allocations made on first use of each length.
 struct DeviceTables {
   std::mutex mu;
-  // key: (N, format) format 0 = double, 1 = float, 2 = float-float
+  // key: (N, format + 8 pass) format 0 = double, 1 = float, 2 = float-float, 3 = packed float-float
   std::map<std::pair<int, int>, void *> tabs;
   ~DeviceTables() {
     for (auto &kv : tabs) cudaFree(kv.second);
@@ -895,7 +904,8 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
                         bM <= (d.prec == 4 ? 4096 : 2048);
   if (d.engine == ENG_BLUESTEIN && !use_blue) return E_UNSUPPORTED;
 
-  const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? 2 : 0);
+  // float-float tables: packed product form for the specialised kernels
+  const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? (use_fast ? 3 : 2) : 0);
   if (tabs_out) {  // caller supplies the tables: report what is needed, launch nothing
     tabs_out->fmt = fmt;
     tabs_out->tabN = tabN;
