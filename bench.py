@@ -243,9 +243,10 @@ def load_traffic(kernel_key):
     return None
 
 
-def load_instr(kernel_key):
-    """Warp instructions per complex FFT point of a kernel, from an `INSTR <kernel> <count>` line
-    of a committed ncu summary under profiles/ (None when no summary covers it)."""
+def load_instr(kernel_key, tag="INSTR"):
+    """Per-point count of a kernel from a `<tag> <kernel> <count>` line of a committed ncu summary
+    under profiles/ (None when no summary covers it): INSTR = warp instructions, FP32OPS = FP32
+    operations per complex FFT point."""
     pdir = os.path.join(ROOT, "profiles")
     try:
         for fn in sorted(os.listdir(pdir)):
@@ -254,7 +255,7 @@ def load_instr(kernel_key):
             with open(os.path.join(pdir, fn)) as f:
                 for line in f:
                     p = line.split()
-                    if len(p) == 3 and p[0] == "INSTR" and p[1] == kernel_key:
+                    if len(p) == 3 and p[0] == tag and p[1] == kernel_key:
                         return float(p[2])
     except OSError:
         pass
@@ -734,18 +735,24 @@ def main():
                 "ms_per_launch": dk["ms"] / dk["launches"], "step_share": dk["ms"] / sum(s["ms"] for s in stages),
                 "whole_step_frac": value / world / peak,
                 "stages_ms": [round(s["ms"], 4) for s in stages]}
-    # float-float kernels are bound by FP32-pipe instruction issue: warp instructions per launch
-    # (ncu count per point x the launch's points) over the live duration, against 4 warp
-    # instructions per SM per clock at the median SM clock sampled during the timed region
-    ipp = load_instr(kernel_key) if arith else None
+    # float-float kernels are compute-side bound: instruction issue (warp instructions per launch,
+    # ncu count per point x the launch's points, over the live duration, against 4 per SM per
+    # clock) and the FMA pipe (FP32 operations against 128 per SM per clock), both at the median
+    # SM clock sampled during the timed region
     n_sm = L.p3dfft_gb300_sm_count()
-    if ipp and n_sm and clocks.get("sm_mhz"):
-        inst = ipp * dk["points"] / dk["launches"]
-        ach = inst / (roofline["ms_per_launch"] * 1e-3)
-        pk = 4.0 * n_sm * clocks["sm_mhz"] * 1e6
-        roofline["issue"] = {"bound": "fp32-pipe instruction issue", "achieved": ach, "peak": pk,
-                             "unit": "warp-inst/s", "frac": ach / pk, "warp_inst_per_launch": inst,
-                             "warp_inst_per_point": ipp, "sms": n_sm, "sm_mhz": clocks["sm_mhz"]}
+    ipp = load_instr(kernel_key) if arith else None
+    fpp = load_instr(kernel_key, "FP32OPS") if arith else None
+    if n_sm and clocks.get("sm_mhz"):
+        clk = clocks["sm_mhz"] * 1e6
+        per_s = dk["points"] / dk["launches"] / (roofline["ms_per_launch"] * 1e-3)
+        if ipp:
+            ach, pk = ipp * per_s, 4.0 * n_sm * clk
+            roofline["issue"] = {"bound": "instruction issue", "achieved": ach, "peak": pk, "unit": "warp-inst/s",
+                                 "frac": ach / pk, "warp_inst_per_point": ipp, "sms": n_sm, "sm_mhz": clocks["sm_mhz"]}
+        if fpp:
+            ach, pk = fpp * per_s, 128.0 * n_sm * clk
+            roofline["fp32_pipe"] = {"bound": "FMA pipe (FP32 operations)", "achieved": ach, "peak": pk,
+                                     "unit": "FP32 op/s", "frac": ach / pk, "fp32_ops_per_point": fpp}
 
     # ---- e2e: pinned host buffers through the public API ----
     hin = p3d.PinnedArray(p3d.storage_shape(GD, MO1), np.float64)
