@@ -200,7 +200,10 @@ __device__ __forceinline__ typename O::W fk_tw(const typename O::T *tab, int m, 
 // Stockham pass I (radix R = plan[I], Ns = product of the earlier radices): butterfly jj reads
 // x[jj + r N/R], multiplies by W_{Ns R}^{r k} (k = jj mod Ns), applies DFT-R and writes slot
 // (jj - k) R + k + r Ns.  Values stay in registers across the barrier; one scatter per pass.
-template <class O, int N, int TWSTEP, int Ns, int I>
+// C2RPRE (first pass of a C2R stage): each value read is the half-length packing
+// Z[k] = (X[k] + conj X[N-k]) + i conj(W_2N^k) (X[k] - conj X[N-k]) of the spectrum in the line
+// (slots 0..N; imaginary parts of X[0], X[N] ignored), formed as it is read.
+template <class O, int N, int TWSTEP, int Ns, int I, bool C2RPRE = false>
 __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T *tab, const typename O::T *ptab,
                                         int j, bool active, int sign) {
   using C = typename O::C;
@@ -222,8 +225,22 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       // padded slots: pad(jj + r M) = pad(jj) + r (M + M/2^PS) when M is a multiple of 2^PS
       const int pj = pad<PS>(jj);
 #pragma unroll
-      for (int r = 0; r < R; r++)
-        v[b * R + r] = line[(M % (1 << PS) == 0) ? pj + r * (M + (M >> PS)) : pad<PS>(jj + r * M)];
+      for (int r = 0; r < R; r++) {
+        const int slot = (M % (1 << PS) == 0) ? pj + r * (M + (M >> PS)) : pad<PS>(jj + r * M);
+        if constexpr (C2RPRE) {
+          const int k = jj + r * M;
+          C xa = line[slot], xb = line[pad<PS>(N - k)];
+          if (k == 0) {
+            xa = O::mk(O::re(xa), O::rzero());
+            xb = O::mk(O::re(xb), O::rzero());
+          }
+          const C xbc = O::conj(xb);
+          const C s = O::add(xa, xbc), d = O::sub(xa, xbc);
+          v[b * R + r] = O::norm(O::add(s, O::muli(O::mul(d, O::conj(O::tw(tab, k))))));
+        } else {
+          v[b * R + r] = line[slot];
+        }
+      }
       if constexpr (Ns > 1) {
         const typename O::T *pt = ptab + fast_pass_offset(N, I) + jj % Ns;
         if constexpr (O::TW_POWERS) {
@@ -498,37 +515,10 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
       }
     }
-    if (KIND == FK_C2R) {
-      // Z'[k] = (X[k] + conj X[N-k]) + i conj(W_2N^k) (X[k] - conj X[N-k]); imag of X[0], X[N] ignored
-      __syncthreads();
-      C z[V];
-      if (act) {
-#pragma unroll
-        const int pn0 = pad<PS>(N - j0);
-        for (int e = 0; e < V; e++) {
-          const int k = j0 + e * TT;
-          const int sa = fk_slot<PS, TT>(j0, pj0, e), sb = fk_slot_rev<PS, TT, N>(j0, pn0, e);
-          C a = lb[sa], b = lb[sb];
-          if (k == 0) {
-            a = O::mk(O::re(a), O::rzero());
-            b = O::mk(O::re(b), O::rzero());
-          }
-          C bc = O::conj(b);
-          C s = O::add(a, bc), d = O::sub(a, bc);
-          const typename O::W w = O::conj(O::tw(tab, k));
-          z[e] = O::norm(O::add(s, O::muli(O::mul(d, w))));
-        }
-      }
-      __syncthreads();
-      if (act) {
-#pragma unroll
-        for (int e = 0; e < V; e++) lb[fk_slot<PS, TT>(j0, pj0, e)] = z[e];
-      }
-    }
     __syncthreads();
 
-    // ---------------- FFT ----------------
-    fk_pass<O, N, TWSTEP, 1, 0>(lb, tab, ptab, j0, act, fsign);
+    // ---------------- FFT (C2R: the half-length packing is formed as the first pass reads) ----
+    fk_pass<O, N, TWSTEP, 1, 0, KIND == FK_C2R>(lb, tab, ptab, j0, act, fsign);
     sc_out = sc;
     }
 
