@@ -537,6 +537,27 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         obase = line_base(gs, p.ot, p.oo);
       }
       const int pjs = pad<PS>(js), pns = pad<PS>(N - js);
+      if constexpr (KIND == FK_R2C && V % 2 == 0) {
+        // X[k] = 1/2 (s - i t), X[N-k] = 1/2 conj(s + i t), with s = Z_k + conj Z_{N-k} and
+        // t = W_2N^k (Z_k - conj Z_{N-k}): each thread unpacks the pairs (k, N-k), k < N/2,
+        // k = 0 giving X[0] and X[N]; X[N/2] (its own partner) by the thread with js = 0
+        auto put = [&](int k, C x) {
+          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
+        };
+        fk_for<V / 2, O::IO_UNROLL>([&](int e) {
+          const int k = js + e * TT;
+          const C a = Y[fk_slot<PS, TT>(js, pjs, e)];
+          const C b = O::conj(Y[k == 0 ? pad<PS>(0) : fk_slot_rev<PS, TT, N>(js, pns, e)]);
+          const C sv = O::add(a, b);
+          const C it = O::muli(O::mul(O::sub(a, b), O::tw(tab, k)));
+          put(k, O::half(O::sub(sv, it)));
+          put(N - k, O::half(O::conj(O::add(sv, it))));
+        });
+        if (js == 0) {
+          const C a = Y[pad<PS>(N / 2)], b = O::conj(a);
+          put(N / 2, O::half(O::sub(O::add(a, b), O::muli(O::mul(O::sub(a, b), O::tw(tab, N / 2))))));
+        }
+      } else
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int k = js + e * TT;
         const int sk = fk_slot<PS, TT>(js, pjs, e);
