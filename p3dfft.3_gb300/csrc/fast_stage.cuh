@@ -197,6 +197,21 @@ __device__ __forceinline__ typename O::W fk_tw(const typename O::T *tab, int m, 
   return sign < 0 ? w : O::conj(w);
 }
 
+// Barrier between the phases of a tile.  sid = 0: the whole CTA; otherwise only the threads of
+// one line, which then exchange data with no other line: a named barrier of the line's T threads
+// (sid = 1 + line, T a multiple of 32 above one warp) or the warp (lines of T <= 32 threads that
+// divide a warp).
+template <int T>
+__device__ __forceinline__ void fk_sync(int sid) {
+  if (sid == 0) {
+    __syncthreads();
+  } else if constexpr (T % 32 == 0 && T > 32) {
+    asm volatile("bar.sync %0, %1;" ::"r"(sid), "n"(T) : "memory");
+  } else {
+    __syncwarp();
+  }
+}
+
 // Stockham pass I (radix R = plan[I], Ns = product of the earlier radices): butterfly jj reads
 // x[jj + r N/R], multiplies by W_{Ns R}^{r k} (k = jj mod Ns), applies DFT-R and writes slot
 // (jj - k) R + k + r Ns.  Values stay in registers across the barrier; one scatter per pass.
@@ -205,7 +220,7 @@ __device__ __forceinline__ typename O::W fk_tw(const typename O::T *tab, int m, 
 // (slots 0..N; imaginary parts of X[0], X[N] ignored), formed as it is read.
 template <class O, int N, int TWSTEP, int Ns, int I, bool C2RPRE = false>
 __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T *tab, const typename O::T *ptab,
-                                        int j, bool active, int sign) {
+                                        int j, bool active, int sign, int sid) {
   using C = typename O::C;
   constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   constexpr RadixList RL = fast_radices(N);
@@ -268,7 +283,7 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       else dft_p2<O, R>(&v[b * R], sign);
     }
   }
-  __syncthreads();
+  fk_sync<T>(sid);
   if (active) {
 #pragma unroll
     for (int b = 0; b < NB; b++) {
@@ -289,8 +304,8 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       }
     }
   }
-  __syncthreads();
-  if constexpr (I + 1 < RL.n) fk_pass<O, N, TWSTEP, Ns * R, I + 1>(line, tab, ptab, j, active, sign);
+  fk_sync<T>(sid);
+  if constexpr (I + 1 < RL.n) fk_pass<O, N, TWSTEP, Ns * R, I + 1>(line, tab, ptab, j, active, sign, sid);
 }
 
 // f(e) for e = 0 .. V-1, U iterations unrolled per step of the outer loop
@@ -358,6 +373,11 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   // threads past TB*T (BLOCK rounded up to whole warps) hold no line
   const bool valid = SH::BLOCK == SH::USED || (int)threadIdx.x < SH::USED;
 
+  // The float-float FFT passes of a tile synchronise per line when each line's threads are whole
+  // warps or share one warp and the load gives each line to consecutive threads (then the passes
+  // of different lines run independently: -2.6% on the 512^3 round trip); otherwise, around the
+  // block-wide steps, and for the FP32 kernels (measured 9% slower per line), per CTA.
+  constexpr bool LSYNC = O::SCALED && SH::BLOCK == SH::USED && ((TT % 32 == 0 && TB <= 15) || (32 % TT == 0));
   // this thread's line and first point: the same V points j0 + e*TT for load, FFT and store
   int l, j0;
   if (p.load_Lmajor) {
@@ -377,6 +397,9 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   }
   const G *gin = reinterpret_cast<const G *>(in);
   G *gout = reinterpret_cast<G *>(out);
+  // (giving the FFT phase the line-contiguous mapping also after a t-major load, with the
+  // conversion after the block-wide barrier, measured 1% slower on those stages)
+  const int sid = (LSYNC && p.load_Lmajor) ? (TT > 32 ? 1 + l : -1) : 0;
 
   // One tile per CTA: a persistent loop over tiles was measured to keep ~80 more registers live.
   {
@@ -444,8 +467,8 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         for (int r = 0; r < R0; r++)
           lb[((R0 & (R0 - 1)) == 0 && R0 <= (1 << PS)) ? pb + r : pad<PS>(j0 * R0 + r)] = O::norm(x[r]);
       }
-      __syncthreads();
-      if constexpr (RL.n > 1) fk_pass<O, N, TWSTEP, R0, 1>(lb, tab, ptab, j0, act, fsign);
+      fk_sync<TT>(sid);
+      if constexpr (RL.n > 1) fk_pass<O, N, TWSTEP, R0, 1>(lb, tab, ptab, j0, act, fsign, sid);
     }
     int sc_out = 0;  // the tile's power-of-two scale (float-float)
     if constexpr (!FUSE1) {
@@ -515,12 +538,14 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
       }
     }
-    __syncthreads();
+    fk_sync<TT>(sid);
 
     // ---------------- FFT (C2R: the half-length packing is formed as the first pass reads) ----
-    fk_pass<O, N, TWSTEP, 1, 0, KIND == FK_C2R>(lb, tab, ptab, j0, act, fsign);
+    fk_pass<O, N, TWSTEP, 1, 0, KIND == FK_C2R>(lb, tab, ptab, j0, act, fsign, sid);
     sc_out = sc;
     }
+    // a store that gives each thread points of other lines than the load waits for all of them
+    if (sid != 0 && !p.store_Lmajor) __syncthreads();
 
     // ---------------- post-processing + store ----------------
     const int gs = g0 + ls;
@@ -600,7 +625,6 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         }
       });
     }
-    __syncthreads();
   }
 }
 
