@@ -133,6 +133,7 @@ __device__ __forceinline__ ff ff_from_double_bits(long long bits) {
   const int E = (int)((b >> 52) & 0x7ff);
   const int e = E - 1023;
   if (e < -100) return ff{__int_as_float(sign), 0.f};
+  if (E == 0x7ff && (b & 0xfffffffffffffull)) return ff{__int_as_float(sign | 0x7fc00000u), 0.f};  // NaN
   if (e > 127) return ff{__int_as_float(sign | 0x7f800000u), 0.f};
   const unsigned long long m = b & 0xfffffffffffffull;
   const unsigned int hib = sign | ((unsigned int)(e + 127) << 23) | (unsigned int)(m >> 29);
@@ -166,12 +167,33 @@ __device__ __forceinline__ ff ff_from_bits_scaled(long long bits, int sc) {
   return ff{hi, __uint_as_float(__float_as_uint(lo) ^ sign)};
 }
 
-// normalised float-float times 2^-sc -> IEEE double bits (round to nearest on the lo part)
+// Non-finite inputs of a tile (exponent field 0x7ff): the tile's scale is taken from its finite
+// values and these convert to the float infinity or NaN of the same sign.
+__device__ __forceinline__ int dbl_biased_exp_finite(long long bits) {
+  const int e = dbl_biased_exp(bits);
+  return e == 0x7ff ? 0 : e;
+}
+__device__ __forceinline__ ff ff_from_bits_scaled_nf(long long bits, int sc) {
+  const unsigned long long b = (unsigned long long)bits;
+  if (((b >> 52) & 0x7ff) == 0x7ff) {
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned nan = (b & 0xfffffffffffffull) ? 0x00400000u : 0u;
+    return ff{__uint_as_float(sign | 0x7f800000u | nan), 0.f};
+  }
+  return ff_from_bits_scaled(bits, sc);
+}
+
+// normalised float-float times 2^-sc -> IEEE double bits (round to nearest on the lo part);
+// a float infinity or NaN in hi gives the double infinity or NaN
 __device__ __forceinline__ long long ff_to_bits_scaled(ff v, int sc) {
   const unsigned uh = __float_as_uint(v.hi);
   const unsigned Ef = (uh >> 23) & 0xff;
   const unsigned sign = uh & 0x80000000u;
-  if (Ef == 0) return 0;
+  if (Ef - 1u >= 254u) {  // zero, or infinity / NaN (one unsigned comparison for both)
+    if (Ef == 0) return 0;
+    return (long long)(((unsigned long long)sign << 32) | 0x7ff0000000000000ull |
+                       ((uh & 0x7fffffu) ? 0x0008000000000000ull : 0ull));
+  }
   const int E = (int)Ef + 896 - sc;
   if (E <= 0) return (long long)((unsigned long long)sign << 32);
   const unsigned H = sign | ((unsigned)E << 20) | ((uh & 0x7fffffu) >> 3);

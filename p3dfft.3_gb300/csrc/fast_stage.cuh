@@ -537,8 +537,31 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
 #pragma unroll
       for (int w = 0; w < SH::BLOCK / 32; w++) emax = max(emax, red[w]);
       sc = 1043 - emax;
-      // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
-      if (act) {
+      if (emax == 0x7ff) {
+        // the tile holds an infinity or NaN (rare, block-uniform): scale from the finite values,
+        // keep the non-finite ones, so that they reach only their own line's outputs
+        int em = 0;
+        if (act) {
+          fk_for<V, 1>([&](int e) { em = max(em, O::rexp_finite(lr[fk_slot<PS, TT>(j0, pj0, e)])); });
+          if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_finite(lr[pad<PS>(N)]));
+        }
+        em = __reduce_max_sync(0xffffffffu, em);
+        __syncthreads();  // every warp has read red[]
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = em;
+        __syncthreads();
+        em = 0;
+#pragma unroll
+        for (int w = 0; w < SH::BLOCK / 32; w++) em = max(em, red[w]);
+        sc = 1043 - em;
+        if (act) {
+          fk_for<V, 1>([&](int e) {
+            const int j = fk_slot<PS, TT>(j0, pj0, e);
+            lb[j] = O::from_raw_nf(lr[j], sc);
+          });
+          if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw_nf(lr[pad<PS>(N)], sc);
+        }
+      } else if (act) {
+        // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
         fk_for<V, O::IO_UNROLL>([&](int e) {
           const int j = fk_slot<PS, TT>(j0, pj0, e);
           lb[j] = O::from_raw(lr[j], sc);

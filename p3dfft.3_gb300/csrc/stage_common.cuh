@@ -295,6 +295,13 @@ struct DFP {
   static __device__ __forceinline__ C from_raw(RAW r, int sc) {
     return mk(ff_from_bits_scaled(r.x, sc), ff_from_bits_scaled(r.y, sc));
   }
+  // tiles holding infinities or NaNs: the scale from the finite values, non-finite values kept
+  static __device__ __forceinline__ int rexp_finite(RAW r) {
+    return max(dbl_biased_exp_finite(r.x), dbl_biased_exp_finite(r.y));
+  }
+  static __device__ __forceinline__ C from_raw_nf(RAW r, int sc) {
+    return mk(ff_from_bits_scaled_nf(r.x, sc), ff_from_bits_scaled_nf(r.y, sc));
+  }
   static __device__ __forceinline__ RAW to_raw(C v, int sc) {
     const C n = pcf_norm(v);
     RAW r;

@@ -1,0 +1,47 @@
+"""GPU: infinities and NaNs in the input stay in their own line, as in the reference's FFTW path
+(each 1D transform of a stage is independent).  The float-float kernels scale each tile of lines
+by a power of two taken from its largest exponent; a tile that holds a non-finite value takes
+its scale from the finite values, so the other lines of the tile are transformed exactly as
+without it, and the non-finite value reaches every output of its own line."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+N = 512
+
+
+def _field(dtype, seed=9):
+    rng = np.random.default_rng(seed)
+    shape = (3, 8, N)  # storage order (z, y, x) for memory order (0,1,2): 24 lines along x
+    x = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+    return x.astype(dtype)
+
+
+@pytest.mark.parametrize("form", ["D_ff", "D_native", "S"])
+def test_nonfinite_values_stay_in_their_line(gpu, oracle, form):
+    p3d = gpu
+    p3d.set_fp64_arith(0 if form == "D_native" else 1)
+    tid = p3d.CFFT_FORWARD_S if form == "S" else p3d.CFFT_FORWARD_D
+    cdt = np.complex64 if form == "S" else np.complex128
+    g = (N, 8, 3)
+    x = _field(cdt)
+    bad = {(0, 5): (7, np.nan), (1, 2): (100, np.inf), (2, 6): (0, -np.inf)}
+    xb = x.copy()
+    for (z, y), (i, v) in bad.items():
+        xb[z, y, i] = v + 0j
+    tp = p3d.TransPlan(tid, g, (0, 1, 2), g, (0, 1, 2), 0)
+    out = np.empty_like(xb)
+    tp.exec(np.ascontiguousarray(xb), out)
+    ref = oracle.exec_stage(p3d.CFFT_FORWARD_D, 0, g, (0, 1, 2), g, (0, 1, 2), x.astype(np.complex128))
+    tol = 5e-6 if form == "S" else 1e-12
+    for z in range(3):
+        for y in range(8):
+            line = out[z, y]
+            if (z, y) in bad:
+                assert not np.isfinite(line).any(), (z, y)
+            else:
+                assert np.isfinite(line).all(), (z, y)
+                assert rel_l2(line, ref[z, y]) < tol, (z, y, rel_l2(line, ref[z, y]))
