@@ -148,9 +148,9 @@ __device__ __forceinline__ ff ff_from_double_bits(long long bits) {
   return ff{__int_as_float(hib), lo};
 }
 
-// Tile-scaled conversions of the specialised stage kernels.  A tile is multiplied by 2^sc
-// (an integer added to every exponent field) so that its largest value is near 2^20; values
-// more than 2^94 below the tile maximum are flushed to zero.  Only integer and FP32 pipe
+// Scaled conversions of the specialised stage kernels.  Each line of a tile is multiplied by
+// 2^sc (an integer added to every exponent field) so that its largest value is near 2^20; values
+// more than 2^94 below the line's maximum are flushed to zero.  Only integer and FP32 pipe
 // instructions are used.
 __device__ __forceinline__ int dbl_biased_exp(long long bits) { return (int)(((unsigned long long)bits >> 52) & 0x7ff); }
 

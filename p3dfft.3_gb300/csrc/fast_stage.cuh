@@ -375,7 +375,10 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf = reinterpret_cast<C *>(smem_raw);
-  __shared__ int red[32];
+  __shared__ int red[32], red2[32];
+  // float-float tiles whose lines differ widely in magnitude: each line's largest biased
+  // exponent (finite values), so that every line gets its own power-of-two scale
+  __shared__ int lfin[TB];
   const T *tab = reinterpret_cast<const T *>(p.tw);
   const T *ptab = reinterpret_cast<const T *>(p.ptw);
   // threads past TB*T (BLOCK rounded up to whole warps) hold no line
@@ -478,11 +481,11 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
       fk_sync<TT>(sid);
       if constexpr (RL.n > 1) fk_pass<O, N, TWSTEP, R0, 1>(lb, tab, ptab, j0, act, fsign, sid);
     }
-    int sc_out = 0;  // the tile's power-of-two scale (float-float)
+    int sc_out = 0;  // the stored line's power-of-two scale (float-float)
     if constexpr (!FUSE1) {
     // ---------------- load the tile into shared memory ----------------
-    // Raw input values go straight to their slot (slot N holds X[N] for C2R).  Float-float tiles
-    // are converted in place once the block-wide largest exponent is known.
+    // Raw input values go straight to their slot (slot N holds X[N] for C2R).  Float-float lines
+    // are converted in place once their largest exponent is known.
     RAW *lr = reinterpret_cast<RAW *>(lb);
     int emax = 0;
     const int pj0 = pad<PS>(j0);
@@ -528,31 +531,43 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
       }
     }
     int sc = 0;
+    bool perline = false;  // lines scaled one by one (wide spread of magnitudes, or non-finite input)
     if constexpr (O::SCALED) {
-      // block-wide max exponent -> scale 2^sc bringing the tile maximum near 2^20
-      emax = __reduce_max_sync(0xffffffffu, emax);
-      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = emax;
+      // The tile's largest exponent and the smallest of its threads' largest nonzero ones: when
+      // they are within 2^40 (the usual case) one scale 2^sc brings the tile maximum near 2^20 and
+      // keeps every line's precision (values are flushed only 2^94 below the tile maximum, so at
+      // least 2^54 below their own line's).  Otherwise (rare, block-uniform) each line takes its own
+      // scale from its finite values and keeps non-finite values, so that a line far smaller than
+      // its neighbours keeps its precision and an infinity or NaN reaches only its own line.
+      int emin = (act && emax > 0) ? emax : 0x7ff;
+      const int wmax = __reduce_max_sync(0xffffffffu, emax), wmin = __reduce_min_sync(0xffffffffu, emin);
+      if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = wmax;
+        red2[threadIdx.x >> 5] = wmin;
+      }
       __syncthreads();
-      emax = 0;
+      int tmax = 0, tmin = 0x7ff;
 #pragma unroll
-      for (int w = 0; w < SH::BLOCK / 32; w++) emax = max(emax, red[w]);
-      sc = 1043 - emax;
-      if (emax == 0x7ff) {
-        // the tile holds an infinity or NaN (rare, block-uniform): scale from the finite values,
-        // keep the non-finite ones, so that they reach only their own line's outputs
+      for (int w = 0; w < SH::BLOCK / 32; w++) {
+        tmax = max(tmax, red[w]);
+        tmin = min(tmin, red2[w]);
+      }
+      perline = tmax == 0x7ff || tmax - tmin > 40;
+      if (perline) {
+        if ((int)threadIdx.x < TB) lfin[threadIdx.x] = 0;
+        __syncthreads();
         int em = 0;
         if (act) {
           fk_for<V, 1>([&](int e) { em = max(em, O::rexp_finite(lr[fk_slot<PS, TT>(j0, pj0, e)])); });
           if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_finite(lr[pad<PS>(N)]));
         }
-        em = __reduce_max_sync(0xffffffffu, em);
-        __syncthreads();  // every warp has read red[]
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = em;
+        {
+          const unsigned grp = __match_any_sync(0xffffffffu, l);
+          const int lm = __reduce_max_sync(grp, em);
+          if (act && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&lfin[l], lm);
+        }
         __syncthreads();
-        em = 0;
-#pragma unroll
-        for (int w = 0; w < SH::BLOCK / 32; w++) em = max(em, red[w]);
-        sc = 1043 - em;
+        sc = 1043 - lfin[l];
         if (act) {
           fk_for<V, 1>([&](int e) {
             const int j = fk_slot<PS, TT>(j0, pj0, e);
@@ -560,20 +575,24 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           });
           if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw_nf(lr[pad<PS>(N)], sc);
         }
-      } else if (act) {
-        // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
-        fk_for<V, O::IO_UNROLL>([&](int e) {
-          const int j = fk_slot<PS, TT>(j0, pj0, e);
-          lb[j] = O::from_raw(lr[j], sc);
-        });
-        if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
+      } else {
+        sc = 1043 - tmax;
+        if (act) {
+          // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
+          fk_for<V, O::IO_UNROLL>([&](int e) {
+            const int j = fk_slot<PS, TT>(j0, pj0, e);
+            lb[j] = O::from_raw(lr[j], sc);
+          });
+          if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
+        }
       }
     }
     fk_sync<TT>(sid);
 
     // ---------------- FFT (C2R: the half-length packing is formed as the first pass reads) ----
     fk_pass<O, N, TWSTEP, 1, 0, KIND == FK_C2R>(lb, tab, ptab, j0, act, fsign, sid);
-    sc_out = sc;
+    // the scale of the line this thread stores (the store may map threads to other lines)
+    if constexpr (O::SCALED) sc_out = perline ? 1043 - lfin[ls] : sc;
     }
     // a store that gives each thread points of other lines than the load waits for all of them
     if (sid != 0 && !p.store_Lmajor) __syncthreads();

@@ -45,3 +45,24 @@ def test_nonfinite_values_stay_in_their_line(gpu, oracle, form):
             else:
                 assert np.isfinite(line).all(), (z, y)
                 assert rel_l2(line, ref[z, y]) < tol, (z, y, rel_l2(line, ref[z, y]))
+
+
+@pytest.mark.parametrize("form", ["D_ff", "D_native"])
+def test_lines_of_a_tile_keep_their_own_precision(gpu, oracle, form):
+    """Lines 1e300 apart in magnitude inside one tile: each line's result is accurate relative to
+    its own norm (the float-float kernels scale every line by its own power of two)."""
+    p3d = gpu
+    p3d.set_fp64_arith(0 if form == "D_native" else 1)
+    g = (N, 8, 3)
+    x = _field(np.complex128, seed=10)
+    mags = np.array([1e150, 1e-150, 1.0, 1e-300 * 1e10])  # repeated over the lines
+    scale = np.resize(mags, 24).reshape(3, 8, 1)
+    x = x * scale
+    for tid, kind in ((p3d.CFFT_FORWARD_D, "C2C"), (p3d.CFFT_BACKWARD_D, "C2C")):
+        tp = p3d.TransPlan(tid, g, (0, 1, 2), g, (0, 1, 2), 0)
+        out = np.empty_like(x)
+        tp.exec(np.ascontiguousarray(x), out)
+        ref = oracle.exec_stage(tid, 0, g, (0, 1, 2), g, (0, 1, 2), x)
+        for z in range(3):
+            for y in range(8):
+                assert rel_l2(out[z, y], ref[z, y]) < 1e-12, (kind, z, y, scale[z, y, 0])
