@@ -29,7 +29,7 @@ CFLAGS += os.environ.get("P3DFFT_GB300_NVCC_FLAGS", "").split()  # extra tuning 
 
 SOURCES = ["stage_kernels.cu", "core.cpp", "batch.cpp", "serve.cpp", "noalloc.cu"]
 # fast_inst.cu once per (arithmetic, kind): 0 float-float / 1 FP64 / 2 FP32 x C2C / R2C / C2R
-FAST_UNITS = [(a, k) for a in range(3) for k in range(4)]
+FAST_UNITS = [(a, k) for a in range(3) for k in range(5)]
 HEADERS = ["kernels.h", "runtime.h", "df_arith.cuh", "stage_common.cuh", "fast_stage.cuh"]
 
 

@@ -4,7 +4,7 @@
 #include "fast_stage.cuh"
 
 #if !defined(P3D_FAST_ARITH) || !defined(P3D_FAST_KIND)
-#error "compile with -DP3D_FAST_ARITH=<0|1|2> -DP3D_FAST_KIND=<0|1|2|3>"
+#error "compile with -DP3D_FAST_ARITH=<0|1|2> -DP3D_FAST_KIND=<0|1|2|3|4>"
 #endif
 
 namespace p3d {

@@ -18,6 +18,9 @@
 //   - DCT-I / DST-I (FFTW REDFT00 / RODFT00) are the FFT of the line's even / odd extension,
 //     built on the way in; real lines are transformed two at a time as the real and imaginary
 //     parts of one complex line (both transforms are real-linear)
+//   - DCT / DST II-IV (FFTW REDFT10/01/11, RODFT10/01/11) are one FFT of length 2n of the
+//     pre-twiddled, zero-padded real line and a post-twiddle on the way out; a complex line is
+//     two real lines (its real and imaginary parts)
 #pragma once
 #include <cuda_runtime.h>
 
@@ -26,7 +29,7 @@
 
 namespace p3d {
 
-enum FastKind { FK_C2C = 0, FK_R2C = 1, FK_C2R = 2, FK_R2R1 = 3 };
+enum FastKind { FK_C2C = 0, FK_R2C = 1, FK_C2R = 2, FK_R2R1 = 3, FK_R2RG = 4 };
 
 struct FParams {
   const void *in;
@@ -42,6 +45,11 @@ struct FParams {
   // FK_R2R1: r2r_odd 0 DCT-I (N = 2(n-1)), 1 DST-I (N = 2(n+1)); pair 1 for real lines, taken
   // two at a time (lines 2g and 2g+1 of nreal form FFT line g), 0 for complex lines
   int r2r_odd, pair, nreal;
+  // FK_R2RG: y_k = 2 Re or -2 Im of W_{8n}^{a2 (2k + b2)} U_k, U = FFT_{2n}(x_j W_{8n}^{2 b2 j},
+  // j < n, x_0 / x_{n-1} halved when half0 / half1), aux = the W_{8n} table; cplx: FFT line g is
+  // part g & 1 of complex line g >> 1
+  const void *aux;
+  int rg_n, rg_a2, rg_b2, rg_sin, rg_half0, rg_half1, rg_cplx;
 };
 
 // resident 256-thread CTAs per SM the register allocation is sized for (FP64 and float-float;
@@ -370,7 +378,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   using G = typename O::G;
   using RAW = typename O::RAW;
   using SH = FastShape<N>;
-  constexpr int TWSTEP = (KIND == FK_C2C || KIND == FK_R2R1) ? 1 : 2;  // FFT twiddle W_N^m = tab[m * TWSTEP]
+  constexpr int TWSTEP = (KIND == FK_C2C || KIND == FK_R2R1 || KIND == FK_R2RG) ? 1 : 2;  // W_N^m = tab[m * TWSTEP]
   constexpr int LS = fast_ls<N, (int)sizeof(C)>(), TB = SH::TB, TT = SH::T, V = SH::V;
   constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -426,11 +434,21 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     if (KIND == FK_R2R1 && p.pair) {
       ibase = line_base(2 * gl, p.it, p.io);
       ibase2 = line_base(min(2 * gl + 1, p.nreal - 1), p.it, p.io);
+    } else if (KIND == FK_R2RG && p.rg_cplx) {
+      ibase = 2 * line_base(gl >> 1, p.it, p.io) + (gl & 1);  // in reals: one part of a complex line
     } else {
       ibase = line_base(gl, p.it, p.io);
     }
     // raw value of FFT input point j of this thread's line
-    const G *src = gin + ((KIND == FK_R2C || (KIND == FK_R2R1 && p.pair)) ? ibase : 2 * ibase);
+    const G *src = gin + ((KIND == FK_R2C || (KIND == FK_R2R1 && p.pair) || KIND == FK_R2RG) ? ibase : 2 * ibase);
+    const long long rstride = (KIND == FK_R2RG && p.rg_cplx) ? 2 * p.iL : p.iL;  // FK_R2RG, in reals
+    const T *raux = reinterpret_cast<const T *>(p.aux);
+    // FK_R2RG: the pre-twiddled, zero-padded input point j
+    auto rg_pre = [&](C x, int j) -> C {
+      if (j >= p.rg_n) return O::zero();
+      if ((p.rg_half0 && j == 0) || (p.rg_half1 && j == p.rg_n - 1)) x = O::half(x);
+      return O::mul(x, O::tw(raux, 2 * p.rg_b2 * j));
+    };
     auto load_raw = [&](int j) -> RAW {
       if constexpr (KIND == FK_R2C) {  // packed z[j] = x[2j] + i x[2j+1]
         if (p.iL == 1) return O::ldraw(src + 2 * j);
@@ -452,18 +470,20 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         RAW r = p.pair ? O::ldraw2(src + (long long)m * p.iL, gin + ibase2 + (long long)m * p.iL)
                        : O::ldraw(src + 2 * (long long)m * p.iL);
         return neg ? O::rneg(r) : r;
+      } else if constexpr (KIND == FK_R2RG) {
+        return j < p.rg_n ? O::ldraw1(src + (long long)j * rstride) : RAW{};
       } else {
         return O::ldraw(src + 2 * (long long)j * p.iL);
       }
     };
 
     C *lb = buf + (size_t)l * LS;
-    const int fsign = KIND == FK_C2C ? p.sign : ((KIND == FK_R2C || KIND == FK_R2R1) ? -1 : 1);
+    const int fsign = KIND == FK_C2C ? p.sign : ((KIND == FK_R2C || KIND == FK_R2R1 || KIND == FK_R2RG) ? -1 : 1);
     constexpr RadixList RL = fast_radices(N);
     // Native arithmetic, no C2R packing, and a first radix equal to the points per thread: the
     // values a thread loads are exactly the inputs of its first butterfly, so the first pass runs
     // on them in registers and the tile's first trip through shared memory is skipped.
-    constexpr bool FUSE1 = !O::SCALED && KIND != FK_C2R && KIND != FK_R2R1 && RL.r[0] == V;
+    constexpr bool FUSE1 = !O::SCALED && KIND != FK_C2R && KIND != FK_R2R1 && KIND != FK_R2RG && RL.r[0] == V;
     if constexpr (FUSE1) {
       constexpr int R0 = RL.r[0];
       C x[V];
@@ -516,6 +536,8 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         if (O::SCALED) {
           emax = max(emax, O::rexp(r));
           lr[sj] = r;
+        } else if (KIND == FK_R2RG) {
+          lb[sj] = rg_pre(O::from_raw(r, 0), j0 + e * TT);
         } else {
           lb[sj] = O::from_raw(r, 0);
         }
@@ -571,7 +593,8 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         if (act) {
           fk_for<V, 1>([&](int e) {
             const int j = fk_slot<PS, TT>(j0, pj0, e);
-            lb[j] = O::from_raw_nf(lr[j], sc);
+            const C x = O::from_raw_nf(lr[j], sc);
+            lb[j] = KIND == FK_R2RG ? rg_pre(x, j0 + e * TT) : x;
           });
           if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw_nf(lr[pad<PS>(N)], sc);
         }
@@ -581,7 +604,8 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
           fk_for<V, O::IO_UNROLL>([&](int e) {
             const int j = fk_slot<PS, TT>(j0, pj0, e);
-            lb[j] = O::from_raw(lr[j], sc);
+            const C x = O::from_raw(lr[j], sc);
+            lb[j] = KIND == FK_R2RG ? rg_pre(x, j0 + e * TT) : x;
           });
           if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
         }
@@ -608,9 +632,12 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         obase = line_base(2 * gs, p.ot, p.oo);
         second = 2 * gs + 1 < p.nreal;
         obase2 = second ? line_base(2 * gs + 1, p.ot, p.oo) : 0;
+      } else if (KIND == FK_R2RG && p.rg_cplx) {
+        obase = 2 * line_base(gs >> 1, p.ot, p.oo) + (gs & 1);  // in reals
       } else {
         obase = line_base(gs, p.ot, p.oo);
       }
+      const long long ostride = (KIND == FK_R2RG && p.rg_cplx) ? 2 * p.oL : p.oL;  // FK_R2RG, in reals
       const int pjs = pad<PS>(js), pns = pad<PS>(N - js);
       if constexpr (KIND == FK_R2C && V % 2 == 0) {
         // X[k] = 1/2 (s - i t), X[N-k] = 1/2 conj(s + i t), with s = Z_k + conj Z_{N-k} and
@@ -668,6 +695,13 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           } else {
             O::strawx(gout + obase + (long long)ko * p.oL, r);
           }
+        } else if (KIND == FK_R2RG) {
+          // y_k = S+ + S- (cosine kinds) or -i (S+ - S-) (sine kinds), S- = W^{a2 (2k+b2)} U_k, S+ = conj S-
+          if (k >= p.rg_n) return;
+          const C sm = O::mul(Y[sk], O::tw(raux, p.rg_a2 * (2 * k + p.rg_b2)));
+          const C sp = O::conj(sm);
+          const C v = p.rg_sin ? O::mulmi(O::sub(sp, sm)) : O::add(sp, sm);
+          O::strawx(gout + obase + (long long)k * ostride, O::to_raw(v, sc_out));
         } else {  // C2R: reals 2k, 2k+1 = z[k]
           RAW r = O::to_raw(Y[sk], sc_out);
           if (p.oL == 1) O::straw(gout + obase + 2 * k, r);
@@ -740,7 +774,7 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
     int rc = E_OK;
 #define P3D_FAST_CASE(L) \
   if (fk_configure<O, KIND, L>() != E_OK) rc = E_CUDA;
-    if constexpr (KIND == FK_R2R1) {
+    if constexpr (KIND == FK_R2R1 || KIND == FK_R2RG) {
       P3D_FAST_EVEN_LENGTHS(P3D_FAST_CASE)
     } else {
       P3D_FAST_LENGTHS(P3D_FAST_CASE)
@@ -750,7 +784,7 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
   }
 #define P3D_FAST_CASE(L) \
   case L: return fk_launch<O, KIND, L>(p, g, ctas, st);
-  if constexpr (KIND == FK_R2R1) {
+  if constexpr (KIND == FK_R2R1 || KIND == FK_R2RG) {
     switch (n) {
       P3D_FAST_EVEN_LENGTHS(P3D_FAST_CASE)
       default: return E_UNSUPPORTED;
@@ -774,14 +808,17 @@ P3D_FAST_DECL(DFP, FK_C2C)
 P3D_FAST_DECL(DFP, FK_R2C)
 P3D_FAST_DECL(DFP, FK_C2R)
 P3D_FAST_DECL(DFP, FK_R2R1)
+P3D_FAST_DECL(DFP, FK_R2RG)
 P3D_FAST_DECL(Native<double>, FK_C2C)
 P3D_FAST_DECL(Native<double>, FK_R2C)
 P3D_FAST_DECL(Native<double>, FK_C2R)
 P3D_FAST_DECL(Native<double>, FK_R2R1)
+P3D_FAST_DECL(Native<double>, FK_R2RG)
 P3D_FAST_DECL(Native<float>, FK_C2C)
 P3D_FAST_DECL(Native<float>, FK_R2C)
 P3D_FAST_DECL(Native<float>, FK_C2R)
 P3D_FAST_DECL(Native<float>, FK_R2R1)
+P3D_FAST_DECL(Native<float>, FK_R2RG)
 #undef P3D_FAST_DECL
 
 template <class O>
@@ -791,6 +828,7 @@ inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaS
     case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, g, ctas, st);
     case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, g, ctas, st);
     case FK_R2R1: return fast_launch_kind<O, FK_R2R1>(a.n, a.p, g, ctas, st);
+    case FK_R2RG: return fast_launch_kind<O, FK_R2RG>(a.n, a.p, g, ctas, st);
     default: return E_UNSUPPORTED;
   }
 }
@@ -799,7 +837,7 @@ inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaS
 inline int fast_preload(int prec, int arith) {
   FastArgs a{};
   int rc = E_OK;
-  for (int k = FK_C2C; k <= FK_R2R1; k++) {
+  for (int k = FK_C2C; k <= FK_R2RG; k++) {
     a.kind = k;
     a.n = 0;
     int r;
@@ -821,7 +859,7 @@ inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, 
 }
 
 inline bool fast_supported(int n, int kind = FK_C2C) {
-  if (kind == FK_R2R1 && n % 2) return false;
+  if ((kind == FK_R2R1 || kind == FK_R2RG) && n % 2) return false;
   switch (n) {
 #define P3D_FAST_CASE(L) case L:
     P3D_FAST_LENGTHS(P3D_FAST_CASE)

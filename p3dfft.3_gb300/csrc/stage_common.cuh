@@ -113,6 +113,12 @@ struct Native {
     r.y = __ldg(p1);
     return r;
   }
+  static __device__ __forceinline__ RAW ldraw1(const G *p) {  // one real, imaginary part 0
+    RAW r;
+    r.x = __ldg(p);
+    r.y = R(0);
+    return r;
+  }
   static __device__ __forceinline__ int rexp(RAW) { return 0; }
   static __device__ __forceinline__ C from_raw(RAW r, int) { return mk(r.x, r.y); }
   static __device__ __forceinline__ RAW to_raw(C v, int) {
@@ -289,6 +295,12 @@ struct DFP {
     RAW r;
     r.x = __ldg(reinterpret_cast<const long long *>(p0));
     r.y = __ldg(reinterpret_cast<const long long *>(p1));
+    return r;
+  }
+  static __device__ __forceinline__ RAW ldraw1(const G *p) {  // one real, imaginary part 0
+    RAW r;
+    r.x = __ldg(reinterpret_cast<const long long *>(p));
+    r.y = 0;
     return r;
   }
   static __device__ __forceinline__ int rexp(RAW r) { return max(dbl_biased_exp(r.x), dbl_biased_exp(r.y)); }

@@ -890,9 +890,13 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   const bool even = (p.nlog % 2) == 0;
   // DCT-I / DST-I run as the FFT of the extended line (no fused derivative on that path)
   const bool r2r1 = d.kind == K_R2R && (d.r2r == REDFT00 || d.r2r == RODFT00) && !(d.deriv && d.dt2 == 2);
-  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even) || r2r1;
+  // DCT / DST II-IV: FFT of the pre-twiddled, zero-padded line; it reads a third table (W_8n), so
+  // it is not used where the caller supplies the tables or groups the launch
+  const bool r2rg = d.kind == K_R2R && p.r2r_np > 0 && !(d.deriv && d.dt2 == 2) && !tw_given && !tabs_out && !fast_prep;
+  const int fkind = r2r1 ? FK_R2R1 : (r2rg ? FK_R2RG : FK_C2C);
+  const bool fast_kind = d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || ((d.kind == K_R2C || d.kind == K_C2R) && even) || r2r1 || r2rg;
   const bool generic_only = getenv("P3DFFT_GB300_GENERIC_ONLY") != nullptr;
-  const bool fast_ok = fast_kind && fast_supported(p.nfft, r2r1 ? FK_R2R1 : FK_C2C) && aligned;
+  const bool fast_ok = fast_kind && fast_supported(p.nfft, fkind) && aligned;
   if (d.engine == ENG_FAST && !fast_ok) return E_UNSUPPORTED;
   if (d.engine == ENG_FIXED && !fixed_engine_len(p.nfft)) return E_UNSUPPORTED;
   const bool use_fast = fast_ok && (d.engine == ENG_FAST || (d.engine == ENG_AUTO && !generic_only));
@@ -961,7 +965,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
 
   if (use_fast) {
     FastArgs fa;
-    fa.kind = r2r1 ? FK_R2R1 : ((d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C));
+    fa.kind = (r2r1 || r2rg) ? fkind : ((d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C));
     fa.n = p.nfft;
     FParams &q = fa.p;
     q.in = in;
@@ -979,7 +983,20 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     const long long nreal = (long long)p.dt * p.dother;
     q.r2r_odd = (r2r1 && d.r2r == RODFT00) ? 1 : 0;
     q.pair = (r2r1 && !p.in_complex) ? 1 : 0;  // real lines, two per FFT line
-    const long long nl = q.pair ? (nreal + 1) / 2 : nreal;
+    q.aux = nullptr;
+    q.rg_n = q.rg_a2 = q.rg_b2 = q.rg_sin = q.rg_half0 = q.rg_half1 = q.rg_cplx = 0;
+    if (r2rg) {
+      q.aux = tabs->get(8 * p.r2r_np, fmt, &err);
+      if (!q.aux) return err;
+      q.rg_n = p.r2r_np;
+      q.rg_a2 = p.r2r_a2;
+      q.rg_b2 = p.r2r_b2;
+      q.rg_sin = p.r2r_sin;
+      q.rg_half0 = p.r2r_halffirst;
+      q.rg_half1 = p.r2r_halflast;
+      q.rg_cplx = p.in_complex ? 1 : 0;  // each part of a complex line is one FFT line
+    }
+    const long long nl = q.pair ? (nreal + 1) / 2 : (q.rg_cplx ? 2 * nreal : nreal);
     if (2 * nreal + TB > 0x7fffffffLL) return E_TOO_LARGE;
     q.nreal = (int)nreal;
     q.nlines = (int)nl;
@@ -1091,7 +1108,8 @@ static std::vector<long long> fast_key(const StageLaunch &st, const FastArgs &fa
   const FParams &q = fa.p;
   return {st.d.prec, st.d.prec == 8 ? st.arith : 0, fa.kind, fa.n, (long long)(uintptr_t)q.tw,
           (long long)(uintptr_t)q.ptw, q.iL, q.it, q.io, q.oL, q.ot, q.oo, q.dt, q.nlines, q.ntotal, q.sign,
-          q.deriv, q.dg, q.dmid, q.load_Lmajor, q.store_Lmajor, q.r2r_odd, q.pair, q.nreal};
+          q.deriv, q.dg, q.dmid, q.load_Lmajor, q.store_Lmajor, q.r2r_odd, q.pair, q.nreal,
+          (long long)(uintptr_t)q.aux, q.rg_n, q.rg_a2, q.rg_b2, q.rg_sin, q.rg_half0, q.rg_half1, q.rg_cplx};
 }
 
 LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err) {

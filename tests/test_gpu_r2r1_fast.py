@@ -1,10 +1,13 @@
-"""GPU: DCT-I / DST-I (FFTW REDFT00 / RODFT00, and the DCT4 IDs the reference registers with the
-DCT-I planners, build/init.C:640-676) on the specialised kernels, which transform the line's even
-/ odd extension with one FFT of length 2(n-1) / 2(n+1).  Real lines go two at a time as the real
-and imaginary parts of one complex line, so line counts are chosen odd as well as even (the last
-line of an odd count is paired with itself).  Each case runs with the specialised engine forced
-and with the generic engine, and both are compared with the CPU oracle's stage: 1e-12 relative
-L2 for FP64 (float-float and native), 5e-6 for FP32."""
+"""GPU: the DCT / DST kinds on the specialised kernels.
+
+DCT-I / DST-I (FFTW REDFT00 / RODFT00, and the DCT4 IDs the reference registers with the DCT-I
+planners, build/init.C:640-676) transform the line's even / odd extension with one FFT of length
+2(n-1) / 2(n+1); real lines go two at a time as the real and imaginary parts of one complex line,
+so line counts are chosen odd as well as even (the last line of an odd count is paired with
+itself).  DCT / DST II-IV transform the pre-twiddled, zero-padded line with one FFT of length 2n.
+Each case runs with the specialised engine forced and with the generic engine, and both are
+compared with the CPU oracle's stage: 1e-12 relative L2 for FP64 (float-float and native), 5e-6
+for FP32."""
 import itertools
 
 import numpy as np
@@ -91,3 +94,27 @@ def test_config3_dct_stage_on_specialised_kernel(gpu):
             f.set_engine(s, eng if st[s]["type"] == p3d.DCT1_COMPLEX_D else ENG_FAST)
         out[eng] = f.exec(x)
     assert rel_l2(out[ENG_FAST], out[ENG_GENERIC]) < 1e-13
+
+
+# DCT / DST II-IV on the specialised kernels (one FFT of length 2n of the pre-twiddled,
+# zero-padded line): n with 2n among the specialised lengths
+CASES_G = [(f, n) for f in ("DCT2", "DCT3", "DST2", "DST3", "DST4") for n in (8, 12, 25, 50, 256)]
+
+
+@pytest.mark.parametrize("family,n", CASES_G)
+@pytest.mark.parametrize("data", ["REAL", "COMPLEX"])
+@pytest.mark.parametrize("form", ["D_ff", "D_native", "S"])
+def test_dct_dst_2_3_4_specialised_vs_oracle(gpu, oracle, family, n, data, form):
+    p3d = gpu
+    p3d.set_fp64_arith(0 if form == "D_native" else 1)
+    name = f"{family}_{data}_{form[0]}"
+    worst = {ENG_FAST: 0.0, ENG_GENERIC: 0.0}
+    for k, (mo1, mo2) in enumerate(ORDERS):
+        dim = k % 3
+        others = (5, 7) if k % 2 == 0 else (6, 4)
+        for eng in (ENG_FAST, ENG_GENERIC):
+            e, prec = _run(p3d, oracle, name, n, dim, mo1, mo2, others, eng, seed=2000 * n + k)
+            worst[eng] = max(worst[eng], e)
+    tol = 1e-12 if prec == 8 else 5e-6
+    assert worst[ENG_FAST] < tol, worst
+    assert worst[ENG_GENERIC] < tol, worst
