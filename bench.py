@@ -191,7 +191,7 @@ def run_reference(args, rank, world):
         nbytes += step()
     dt = time.perf_counter() - t0
     value = nbytes / dt / 1e9
-    sample = (f"{frac:.4f} of the lines of each of the 6 stages of the {N}^3 round trip per step "
+    sample = (f"{frac:.4f} of the lines of each of the 6 stages of the {GD[0]}x{GD[1]}x{GD[2]} round trip per step "
               f"(oracle C port, OpenMP {cores} threads)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
@@ -221,7 +221,7 @@ def cpu_baseline_sample():
             t_tot += time.perf_counter() - t0
             b_tot += (b_in + b_out) * m / nlines
     return {"value": b_tot / t_tot / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
-            "sample": f"1/8 of the lines of each of the 6 stages of the {N}^3 FP64 round trip "
+            "sample": f"1/8 of the lines of each of the 6 stages of the {GD[0]}x{GD[1]}x{GD[2]} FP64 round trip "
                       f"(CPU oracle port, OpenMP {cores} threads, {t_tot:.2f} s)"}
 
 
