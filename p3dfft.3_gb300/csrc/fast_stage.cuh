@@ -416,7 +416,8 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   }
   const G *gin = reinterpret_cast<const G *>(in);
   G *gout = reinterpret_cast<G *>(out);
-  // (giving the FFT phase the line-contiguous mapping also after a t-major load, with the
+  // barrier of this thread's FFT passes (fk_sync): per line only after a line-contiguous load
+  // (remapping the FFT phase of a tile-dim-contiguous load to lines, with the float-float
   // conversion after the block-wide barrier, measured 1% slower on those stages)
   const int sid = (LSYNC && p.load_Lmajor) ? (TT > 32 ? 1 + l : -1) : 0;
 
