@@ -140,7 +140,8 @@ struct Native {
   }
 };
 
-// float-float arithmetic for FP64 data (see df_arith.cuh)
+// float-float arithmetic for FP64 data (see df_arith.cuh), scalar form: the generic engines
+// (k_stage); the specialised kernels use the packed form DFP below
 struct DF {
   using G = double;
   using S = ff;
@@ -188,39 +189,6 @@ struct DF {
     w.x = ff_to_double_bits(ff_norm(v.x));
     w.y = ff_to_double_bits(ff_norm(v.y));
     *reinterpret_cast<longlong2 *>(p) = w;
-  }
-  // register-level I/O of the specialised kernels: raw IEEE bits, tile scaled by 2^sc
-  static constexpr bool SCALED = true;
-  static constexpr int IO_UNROLL = FAST_IO_UNROLL_DF;
-  static constexpr bool TW_POWERS = false;
-  using RAW = longlong2;
-  static __device__ __forceinline__ RAW ldraw(const G *p) { return __ldg(reinterpret_cast<const longlong2 *>(p)); }
-  static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
-    RAW r;
-    r.x = __ldg(reinterpret_cast<const long long *>(p0));
-    r.y = __ldg(reinterpret_cast<const long long *>(p1));
-    return r;
-  }
-  static __device__ __forceinline__ int rexp(RAW r) { return max(dbl_biased_exp(r.x), dbl_biased_exp(r.y)); }
-  static __device__ __forceinline__ C from_raw(RAW r, int sc) {
-    return mk(ff_from_bits_scaled(r.x, sc), ff_from_bits_scaled(r.y, sc));
-  }
-  static __device__ __forceinline__ RAW to_raw(C v, int sc) {
-    RAW r;
-    r.x = ff_to_bits_scaled(ff_norm(v.x), sc);
-    r.y = ff_to_bits_scaled(ff_norm(v.y), sc);
-    return r;
-  }
-  static __device__ __forceinline__ void straw(G *p, RAW r) { *reinterpret_cast<longlong2 *>(p) = r; }
-  static __device__ __forceinline__ void straw2(G *p0, G *p1, RAW r) {
-    *reinterpret_cast<long long *>(p0) = r.x;
-    *reinterpret_cast<long long *>(p1) = r.y;
-  }
-  static __device__ __forceinline__ void strawx(G *p, RAW r) { *reinterpret_cast<long long *>(p) = r.x; }
-  static __device__ __forceinline__ RAW rneg(RAW r) {  // flip both sign bits
-    r.x ^= (long long)0x8000000000000000ull;
-    r.y ^= (long long)0x8000000000000000ull;
-    return r;
   }
   static __device__ __forceinline__ C tws(const T *t, int k) { return t[k]; }
   static __device__ __forceinline__ C tw(const T *t, int k) {
