@@ -129,11 +129,30 @@ struct FastShape {
   static constexpr int MINB = fast_max_values(N) > 8 ? 3 : FAST_MIN_BLOCKS;
 };
 
-// Padding of a line in shared memory: one slot after every 2^PS data slots, PS = 3 for 16-byte
-// complex elements and 4 for 8-byte ones, i.e. one slot per 128 bytes of line data.
+// Layout of a line in shared memory.  Padding: one slot after every 2^PS data slots, PS = 3 for
+// 16-byte complex elements and 4 for 8-byte ones, i.e. one slot per 128 bytes of line data.
+// Swizzle (PS = FK_SWZ, 8-byte elements with FAST_SWIZZLE8): slot i ^ ((i >> 3) & 15), a
+// permutation within each aligned block of 16 slots that a wavefront model of the Stockham
+// passes finds conflict-free where the padding leaves 1/6 extra wavefronts.  Measured: correct,
+// but the FP32 512^3 round trip 15% slower (1.43 vs 1.24 ms), the slots of a thread's points
+// being computed one by one instead of by constant steps; so the padding is the default.
+#ifndef FAST_SWIZZLE8
+#define FAST_SWIZZLE8 0
+#endif
+constexpr int FK_SWZ = 15;
 template <int ESZ>
 __host__ __device__ constexpr int fast_pad_shift() {
-  return ESZ >= 16 ? 3 : 4;
+  return ESZ >= 16 ? 3 : (FAST_SWIZZLE8 ? FK_SWZ : 4);
+}
+template <int PS>
+__host__ __device__ __forceinline__ constexpr int fk_pos(int i) {
+  if constexpr (PS == FK_SWZ) return i ^ ((i >> 3) & 15);
+  else return PS ? i + (i >> PS) : i;
+}
+// additive padding (slots of evenly spaced points advance by constant steps)
+template <int PS>
+__host__ __device__ constexpr bool fk_additive() {
+  return PS != FK_SWZ;
 }
 
 // Bank-conflict cost of a shared-memory line stride LS (complex slots of ESZ bytes): a warp's
@@ -152,7 +171,7 @@ __host__ __device__ constexpr int fast_ls_cost(int LS, int ESZ) {
       for (int t = g0; t < g0 + U && t < SH::USED; t++) {
         const int l = map ? t % SH::TB : t / SH::T;
         const int j = map ? t / SH::TB : t % SH::T;
-        const int slot = l * LS + j + (j >> (ESZ >= 16 ? 3 : 4));
+        const int slot = l * LS + (ESZ >= 16 ? fk_pos<3>(j) : fk_pos<fast_pad_shift<8>()>(j));
         const int c = ++cnt[slot % U];
         worst = c > worst ? c : worst;
       }
@@ -162,11 +181,15 @@ __host__ __device__ constexpr int fast_ls_cost(int LS, int ESZ) {
   return cost;
 }
 
-// Padded line stride: more than the padded slot of N (which C2R uses), the cheapest under
+// Line stride: more than the largest slot of points 0..N (N is used by C2R), the cheapest under
 // fast_ls_cost among the next 128/ESZ candidates.
 template <int N, int ESZ>
 __host__ __device__ constexpr int fast_ls() {
-  const int base = N + (N >> fast_pad_shift<ESZ>()) + 1;
+  int base = 0;
+  for (int i = 0; i <= N; i++) {
+    const int sl = fk_pos<fast_pad_shift<ESZ>()>(i);
+    base = sl + 1 > base ? sl + 1 : base;
+  }
   const int U = 128 / ESZ;
   int best = base, best_cost = 1 << 30;
   for (int ls = base; ls < base + U; ls++) {
@@ -254,13 +277,13 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       const int jj = j + b * T;
       if (GUARD && jj >= M) break;
       // padded slots: pad(jj + r M) = pad(jj) + r (M + M/2^PS) when M is a multiple of 2^PS
-      const int pj = pad<PS>(jj);
+      const int pj = fk_pos<PS>(jj);
 #pragma unroll
       for (int r = 0; r < R; r++) {
-        const int slot = (M % (1 << PS) == 0) ? pj + r * (M + (M >> PS)) : pad<PS>(jj + r * M);
+        const int slot = (fk_additive<PS>() && M % (1 << PS) == 0) ? pj + r * (M + (M >> PS)) : fk_pos<PS>(jj + r * M);
         if constexpr (C2RPRE) {
           const int k = jj + r * M;
-          C xa = line[slot], xb = line[pad<PS>(N - k)];
+          C xa = line[slot], xb = line[fk_pos<PS>(N - k)];
           if (k == 0) {
             xa = O::mk(O::re(xa), O::rzero());
             xb = O::mk(O::re(xb), O::rzero());
@@ -310,12 +333,12 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
       // pad(base + r Ns) = pad(base) + r (Ns + Ns/2^PS) for Ns a multiple of 2^PS, and
       // pad(base) + r in the first pass when R is a power of two up to 2^PS (base = jj R then
       // stays in one padding block)
-      constexpr bool NS_AL = Ns % (1 << PS) == 0;
-      constexpr bool FIRST_AL = Ns == 1 && (R & (R - 1)) == 0 && R <= (1 << PS);
-      const int pb = pad<PS>(base);
+      constexpr bool NS_AL = fk_additive<PS>() && Ns % (1 << PS) == 0;
+      constexpr bool FIRST_AL = fk_additive<PS>() && Ns == 1 && (R & (R - 1)) == 0 && R <= (1 << PS);
+      const int pb = fk_pos<PS>(base);
 #pragma unroll
       for (int r = 0; r < R; r++) {
-        const int slot = NS_AL ? pb + r * (Ns + (Ns >> PS)) : (FIRST_AL ? pb + r : pad<PS>(base + r * Ns));
+        const int slot = NS_AL ? pb + r * (Ns + (Ns >> PS)) : (FIRST_AL ? pb + r : fk_pos<PS>(base + r * Ns));
         line[slot] = FAST_PASS_NORM ? O::norm(v[b * R + r]) : v[b * R + r];
       }
     }
@@ -336,17 +359,17 @@ __device__ __forceinline__ void fk_for(F &&f) {
   }
 }
 
-// Padded slot of point j0 + e*TT given pj0 = pad(j0): constant steps when TT is a multiple of 2^PS.
+// Slot of point j0 + e*TT given pj0 = slot(j0): constant steps when TT is a multiple of 2^PS.
 template <int PS, int TT>
 __device__ __forceinline__ int fk_slot(int j0, int pj0, int e) {
-  if constexpr (TT % (1 << PS) == 0) return pj0 + e * (TT + (TT >> PS));
-  else return pad<PS>(j0 + e * TT);
+  if constexpr (fk_additive<PS>() && TT % (1 << PS) == 0) return pj0 + e * (TT + (TT >> PS));
+  else return fk_pos<PS>(j0 + e * TT);
 }
-// Padded slot of point N - (j0 + e*TT) given pn = pad(N - j0), for 0 < j0 + e*TT <= N.
+// Slot of point N - (j0 + e*TT) given pn = slot(N - j0), for 0 < j0 + e*TT <= N.
 template <int PS, int TT, int N>
 __device__ __forceinline__ int fk_slot_rev(int j0, int pn, int e) {
-  if constexpr (TT % (1 << PS) == 0 && N % (1 << PS) == 0) return pn - e * (TT + (TT >> PS));
-  else return pad<PS>(N - j0 - e * TT);
+  if constexpr (fk_additive<PS>() && TT % (1 << PS) == 0 && N % (1 << PS) == 0) return pn - e * (TT + (TT >> PS));
+  else return fk_pos<PS>(N - j0 - e * TT);
 }
 
 template <class O>
@@ -494,10 +517,10 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         if constexpr (R0 == 3) dft3<O>(x, fsign, O::tw(tab, (N / 3) * TWSTEP));
         else if constexpr (R0 == 5) dft5<O>(x, fsign, O::tw(tab, (N / 5) * TWSTEP), O::tw(tab, 2 * (N / 5) * TWSTEP));
         else dft_p2<O, R0>(x, fsign);
-        const int pb = pad<PS>(j0 * R0);
+        const int pb = fk_pos<PS>(j0 * R0);
 #pragma unroll
         for (int r = 0; r < R0; r++)
-          lb[((R0 & (R0 - 1)) == 0 && R0 <= (1 << PS)) ? pb + r : pad<PS>(j0 * R0 + r)] = O::norm(x[r]);
+          lb[(fk_additive<PS>() && (R0 & (R0 - 1)) == 0 && R0 <= (1 << PS)) ? pb + r : fk_pos<PS>(j0 * R0 + r)] = O::norm(x[r]);
       }
       fk_sync<TT>(sid);
       if constexpr (RL.n > 1) fk_pass<O, N, TWSTEP, R0, 1>(lb, tab, ptab, j0, act, fsign, sid);
@@ -509,10 +532,10 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     // are converted in place once their largest exponent is known.
     RAW *lr = reinterpret_cast<RAW *>(lb);
     int emax = 0;
-    const int pj0 = pad<PS>(j0);
+    const int pj0 = fk_pos<PS>(j0);
     if (act && KIND == FK_R2R1) {
       // extensions: each input element is read once and written to slots j and N - j
-      const int pn0 = pad<PS>(N - j0);
+      const int pn0 = fk_pos<PS>(N - j0);
       fk_for<V, O::IO_UNROLL>([&](int e) {
         const int j = j0 + e * TT;
         if (j > N / 2) return;
@@ -547,9 +570,9 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         RAW r = O::ldraw(src + 2 * (long long)N * p.iL);
         if (O::SCALED) {
           emax = max(emax, O::rexp(r));
-          lr[pad<PS>(N)] = r;
+          lr[fk_pos<PS>(N)] = r;
         } else {
-          lb[pad<PS>(N)] = O::from_raw(r, 0);
+          lb[fk_pos<PS>(N)] = O::from_raw(r, 0);
         }
       }
     }
@@ -582,7 +605,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         int em = 0;
         if (act) {
           fk_for<V, 1>([&](int e) { em = max(em, O::rexp_finite(lr[fk_slot<PS, TT>(j0, pj0, e)])); });
-          if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_finite(lr[pad<PS>(N)]));
+          if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_finite(lr[fk_pos<PS>(N)]));
         }
         {
           const unsigned grp = __match_any_sync(0xffffffffu, l);
@@ -597,7 +620,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
             const C x = O::from_raw_nf(lr[j], sc);
             lb[j] = KIND == FK_R2RG ? rg_pre(x, j0 + e * TT) : x;
           });
-          if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw_nf(lr[pad<PS>(N)], sc);
+          if (KIND == FK_C2R && j0 == 0) lb[fk_pos<PS>(N)] = O::from_raw_nf(lr[fk_pos<PS>(N)], sc);
         }
       } else {
         sc = 1043 - tmax;
@@ -608,7 +631,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
             const C x = O::from_raw(lr[j], sc);
             lb[j] = KIND == FK_R2RG ? rg_pre(x, j0 + e * TT) : x;
           });
-          if (KIND == FK_C2R && j0 == 0) lb[pad<PS>(N)] = O::from_raw(lr[pad<PS>(N)], sc);
+          if (KIND == FK_C2R && j0 == 0) lb[fk_pos<PS>(N)] = O::from_raw(lr[fk_pos<PS>(N)], sc);
         }
       }
     }
@@ -639,7 +662,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         obase = line_base(gs, p.ot, p.oo);
       }
       const long long ostride = (KIND == FK_R2RG && p.rg_cplx) ? 2 * p.oL : p.oL;  // FK_R2RG, in reals
-      const int pjs = pad<PS>(js), pns = pad<PS>(N - js);
+      const int pjs = fk_pos<PS>(js), pns = fk_pos<PS>(N - js);
       if constexpr (KIND == FK_R2C && V % 2 == 0) {
         // X[k] = 1/2 (s - i t), X[N-k] = 1/2 conj(s + i t), with s = Z_k + conj Z_{N-k} and
         // t = W_2N^k (Z_k - conj Z_{N-k}): each thread unpacks the pairs (k, N-k), k < N/2,
@@ -650,14 +673,14 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         fk_for<V / 2, O::IO_UNROLL>([&](int e) {
           const int k = js + e * TT;
           const C a = Y[fk_slot<PS, TT>(js, pjs, e)];
-          const C b = O::conj(Y[k == 0 ? pad<PS>(0) : fk_slot_rev<PS, TT, N>(js, pns, e)]);
+          const C b = O::conj(Y[k == 0 ? fk_pos<PS>(0) : fk_slot_rev<PS, TT, N>(js, pns, e)]);
           const C sv = O::add(a, b);
           const C it = O::muli(O::mul(O::sub(a, b), O::tw(tab, k)));
           put(k, O::half(O::sub(sv, it)));
           put(N - k, O::half(O::conj(O::add(sv, it))));
         });
         if (js == 0) {
-          const C a = Y[pad<PS>(N / 2)], b = O::conj(a);
+          const C a = Y[fk_pos<PS>(N / 2)], b = O::conj(a);
           put(N / 2, O::half(O::sub(O::add(a, b), O::muli(O::mul(O::sub(a, b), O::tw(tab, N / 2))))));
         }
       } else
@@ -673,7 +696,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           C x = O::half(O::sub(s, O::muli(O::mul(d, O::tw(tab, k)))));
           O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
           if (k == 0) {  // X[N] = Re Z_0 - Im Z_0
-            C z0 = Y[pad<PS>(0)];
+            C z0 = Y[fk_pos<PS>(0)];
             C xn = O::mk(O::re(O::norm(O::sub(O::mk(O::re(z0), O::rzero()), O::mk(O::im(z0), O::rzero())))), O::rzero());
             O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc_out));
           }
