@@ -1,8 +1,9 @@
-"""GPU: infinities and NaNs in the input stay in their own line, as in the reference's FFTW path
-(each 1D transform of a stage is independent).  The float-float kernels scale each tile of lines
-by a power of two taken from its largest exponent; a tile that holds a non-finite value takes
-its scale from the finite values, so the other lines of the tile are transformed exactly as
-without it, and the non-finite value reaches every output of its own line."""
+"""GPU: lines of a stage stay independent, as in the reference's FFTW path (each 1D transform
+is its own FFTW call).  The float-float kernels scale a tile of lines by a power of two taken
+from its largest exponent; a tile whose lines differ widely in magnitude, or that holds an
+infinity or NaN, scales each line by its own power of two taken from its finite values.  So an
+infinity or NaN reaches every output of its own line and no other, and a line far smaller than
+its tile neighbours keeps its relative accuracy."""
 import numpy as np
 import pytest
 
