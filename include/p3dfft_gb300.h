@@ -42,6 +42,16 @@ void p3dfft_gb300_set_host_direct(int on);
  * can be set with P3DFFT_GB300_FP64_ARITH=native. */
 void p3dfft_gb300_set_fp64_arith(int mode);
 int p3dfft_gb300_get_fp64_arith(void);
+/* 1 (default): reproduce two reference behaviours whose results are deterministic, so outputs
+ * equal the reference's: compute_deriv differentiates along storage axis imo[idir], the logical
+ * dim whose storage rank is idir (reference build/deriv.C:89-93; differs from the storage axis of
+ * dim idir only for the 3-cycle memory orders), and a 1D plan whose input and output orders both
+ * have the transform dim non-leading reads its input as stored in order swap0(mo1, dim) (reference
+ * build/templ.C:1015-1023, where find_m overwrites the plan's input order).  0: differentiate
+ * along logical dim idir and read 1D inputs in their declared order.  The initial value can be
+ * set with P3DFFT_GB300_REFERENCE_COMPAT=0. */
+void p3dfft_gb300_set_reference_compat(int on);
+int p3dfft_gb300_get_reference_compat(void);
 
 /* ---- planning / execution by explicit grid descriptions (1x1x1 processor grid) ----
  * A grid is (gdims[3], mem_order[3], dim_conj_sym).  Returns a handle >= 0, or -1 with the
@@ -100,7 +110,10 @@ void p3dfft_gb300_tune_cache_clear(void);
  * p3dfft_gb300_noalloc_max_field_bytes() (about 95 MiB, e.g. a 128^3 or 256x256x128 FP64
  * R2C round trip), larger transforms are rejected with P3DFFT_ERR_TOO_LARGE.  The first call on
  * a device resolves the array's device address (cudaGetSymbolAddress) and should come before
- * any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+ * any stream capture.  Each call stages the plan's twiddle tables through a static host array
+ * that the next call overwrites, so a call made while the library stream is being captured is
+ * refused with P3DFFT_ERR_UNSUPPORTED.  Calls share the arrays: calls that overlap on the GPU
+ * race.  Stages whose tuned engine needs the library's cached tables run the heuristic engine. */
 #define P3DFFT_GB300_NOALLOC_BYTES (192ull << 20)
 int p3dfft_gb300_exec3d_noalloc(int plan, const void *in, void *out, int idir);
 long long p3dfft_gb300_noalloc_max_field_bytes(void);

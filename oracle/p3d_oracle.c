@@ -338,6 +338,46 @@ void orc_dft_c2r(int n, const double *in, double *out)
   lineplan_free(&L);
 }
 
+/* Reusable line plans for callers that run many lines of one transform (the FFTW-API shim of
+ * oracle/refshim/fftw_shim.c, through which the reference's own driver runs on this arithmetic). */
+struct orc_line {
+  lineplan L;
+  int maxp;
+};
+
+orc_line *orc_line_new(int kind, int r2r, int n)
+{
+  orc_line *P;
+  if (n < 1 || kind < ORC_K_EMPTY || kind > ORC_K_R2R) return NULL;
+  if (kind == ORC_K_R2R && ((r2r == ORC_REDFT00 && n < 2) || r2r < ORC_REDFT00 || r2r > ORC_RODFT11)) return NULL;
+  P = (orc_line *)calloc(1, sizeof(*P));
+  lineplan_init(&P->L, kind, r2r, n);
+  P->maxp = (kind != ORC_K_EMPTY && kind != ORC_K_R2R) ? P->L.P.maxp : 1;
+  return P;
+}
+
+size_t orc_line_work_doubles(const orc_line *P) { return 6 * (size_t)P->L.n + 2 * (size_t)P->maxp + 72; }
+
+void orc_line_exec(const orc_line *P, const double *in, double *out, double *work)
+{
+  const lineplan *L = &P->L;
+  switch (L->kind) {
+    case ORC_K_EMPTY: memcpy(out, in, sizeof(double) * L->n); break;
+    case ORC_K_R2C: r2c_line(L, in, out, work); break;
+    case ORC_K_C2R: c2r_line(L, in, out, work); break;
+    case ORC_K_C2C_FWD: fft_exec(&L->P, -1, in, out, work); break;
+    case ORC_K_C2C_BWD: fft_exec(&L->P, +1, in, out, work); break;
+    case ORC_K_R2R: r2r_line(L, in, 1, out, 1); break;
+  }
+}
+
+void orc_line_free(orc_line *P)
+{
+  if (!P) return;
+  lineplan_free(&P->L);
+  free(P);
+}
+
 /* compute_deriv_loc, build/exec.C:228-287, on one complex line of length M (M = output length
  * of the stage's transform).  r2c lines use g = 2(M-1) (exec.C:240-243). */
 static void deriv_line(double *x, int M, int r2c)
@@ -624,21 +664,30 @@ int orc_exec3d(const orc_plan3d *p, const double *in, double *out, int idir, int
 }
 
 /* compute_deriv, build/deriv.C:85-184, on one task (GlobStart = 0).
- * QUIRK (not reproduced): deriv.C:91-92 locates the storage axis of idir with
- * `MemOrder[i] == idir` (the inverse permutation), which differs from MemOrder[idir] when the
- * memory order is a 3-cycle such as (1,2,0).  The oracle differentiates along the storage
- * axis MemOrder[idir] of logical dimension idir, as the function documents. */
-int orc_compute_deriv(const orc_grid *g, const double *in, double *out, int idir)
+ * ref_axis = 1 restates the reference literally: deriv.C:89-93 takes ldir with
+ * MemOrder[ldir] == idir and then uses ldir as the STORAGE axis (deriv.C:107-180), i.e. it
+ * differentiates along the storage axis holding the logical dim whose storage rank is idir, with
+ * the wavenumbers of logical dim idir (g, mid from Gdims[idir], deriv.C:95-102).  For the identity
+ * and transposition memory orders that is the storage axis of dim idir; for the 3-cycles (1,2,0)
+ * and (2,0,1) it is another axis (QUIRK).  ref_axis = 0 differentiates along logical dim idir. */
+int orc_compute_deriv_axis(const orc_grid *g, const double *in, double *out, int idir, int ref_axis)
 {
   long long s[3], n0, n1, i, j;
-  int a, b, gg, mid, M;
+  int a, b, gg, mid, M, ax = idir;
   if (idir < 0 || idir > 2) return -1;
   strides_of(g, s);
-  M = g->gdims[idir];
-  gg = (g->dcs == idir) ? (M - 1) * 2 : M;
+  if (ref_axis) {
+    int d, ldir = idir;
+    for (d = 0; d < 3; d++)
+      if (g->mo[d] == idir) ldir = d; /* deriv.C:89-93 */
+    for (d = 0; d < 3; d++)
+      if (g->mo[d] == ldir) ax = d;   /* the logical dim stored at storage rank ldir */
+  }
+  M = g->gdims[ax];
+  gg = (g->dcs == idir) ? (g->gdims[idir] - 1) * 2 : g->gdims[idir];
   mid = gg / 2;
-  a = (idir + 1) % 3;
-  b = (idir + 2) % 3;
+  a = (ax + 1) % 3;
+  b = (ax + 2) % 3;
   n0 = g->gdims[a];
   n1 = g->gdims[b];
   for (j = 0; j < n1; j++)
@@ -646,7 +695,7 @@ int orc_compute_deriv(const orc_grid *g, const double *in, double *out, int idir
       int k;
       long long base = i * s[a] + j * s[b];
       for (k = 0; k < M; k++) {
-        long long o = 2 * (base + (long long)k * s[idir]);
+        long long o = 2 * (base + (long long)k * s[ax]);
         double re = in[o], im = in[o + 1], kk;
         if (k < mid) kk = k;
         else if (k == mid) { out[o] = 0.0; out[o + 1] = 0.0; continue; }
@@ -656,4 +705,9 @@ int orc_compute_deriv(const orc_grid *g, const double *in, double *out, int idir
       }
     }
   return 0;
+}
+
+int orc_compute_deriv(const orc_grid *g, const double *in, double *out, int idir)
+{
+  return orc_compute_deriv_axis(g, in, out, idir, 0);
 }

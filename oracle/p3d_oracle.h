@@ -16,6 +16,7 @@
  */
 #ifndef P3D_ORACLE_H
 #define P3D_ORACLE_H
+#include <stddef.h>
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -60,6 +61,16 @@ void orc_r2r(int kind, int n, const double *in, double *out);
 /* O(n^2) long-double direct DFT for self-checks */
 void orc_dft_direct(int n, int sign, const double *in, double *out);
 
+/* Reusable plan for many lines of one transform: kind ORC_K_*, r2r kind for ORC_K_R2R, logical
+ * length n.  orc_line_exec runs one contiguous line (complex = interleaved pairs; in and out must
+ * not overlap) with `work` holding orc_line_work_doubles() doubles.  NULL for an invalid kind or
+ * length. */
+typedef struct orc_line orc_line;
+orc_line *orc_line_new(int kind, int r2r, int n);
+size_t orc_line_work_doubles(const orc_line *L);
+void orc_line_exec(const orc_line *L, const double *in, double *out, double *work);
+void orc_line_free(orc_line *L);
+
 /* ---- Planner (1x1x1 processor grid) ---- */
 typedef struct {
   int gdims[3];  /* global == local dims on one rank */
@@ -95,8 +106,11 @@ int orc_exec_stage(const orc_stage *s, const double *in, double *out, int deriv,
  * first batch dim fastest); line1 < 0 means all lines.  Used to time bounded samples. */
 int orc_exec_stage_lines(const orc_stage *s, const double *in, double *out, int deriv, int nthreads,
                          long long line0, long long line1);
-/* Standalone spectral derivative (build/deriv.C:85-184) on a complex field. */
+/* Standalone spectral derivative (build/deriv.C:85-184) on a complex field, along logical dim
+ * idir.  orc_compute_deriv_axis with ref_axis = 1 differentiates along the storage axis the
+ * reference uses (rank imo[idir], deriv.C:89-93), which differs for the 3-cycle memory orders. */
 int orc_compute_deriv(const orc_grid *g, const double *in, double *out, int idir);
+int orc_compute_deriv_axis(const orc_grid *g, const double *in, double *out, int idir, int ref_axis);
 
 /* helpers exposed for tests */
 void orc_swap0(int newmo[3], const int mo[3], int L);

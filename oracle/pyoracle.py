@@ -87,6 +87,7 @@ def lib():
         _lib.orc_exec_stage_lines.argtypes = [ctypes.POINTER(Stage), dp, dp, ctypes.c_int, ctypes.c_int,
                                               ctypes.c_longlong, ctypes.c_longlong]
         _lib.orc_compute_deriv.argtypes = [ctypes.POINTER(Grid), dp, dp, ctypes.c_int]
+        _lib.orc_compute_deriv_axis.argtypes = [ctypes.POINTER(Grid), dp, dp, ctypes.c_int, ctypes.c_int]
         _lib.orc_type_info_get.argtypes = [ctypes.c_int, ctypes.POINTER(TypeInfo)]
         _lib.orc_swap0.argtypes = [ctypes.POINTER(ctypes.c_int * 3), ctypes.POINTER(ctypes.c_int * 3), ctypes.c_int]
         _lib.orc_find_order.argtypes = [ctypes.POINTER(ctypes.c_int * 3), ctypes.POINTER(Grid),
@@ -219,11 +220,13 @@ def exec_stage(type_id, dim, gdims1, mo1, gdims2, mo2, x, deriv=False, nthreads=
     return out.reshape(storage_shape(gdims2, mo2))
 
 
-def compute_deriv(x, gdims, mo, dcs, idir):
+def compute_deriv(x, gdims, mo, dcs, idir, ref_axis=False):
+    """ref_axis=True: the storage axis the reference differentiates along (build/deriv.C:89-93)."""
     g = Grid.make(gdims, mo, dcs)
     xin = _as_f64(x)
     out = np.empty(int(np.prod(gdims)), np.complex128)
-    rc = lib().orc_compute_deriv(ctypes.byref(g), _dp(xin), _dp(out.view(np.float64)), int(idir))
+    rc = lib().orc_compute_deriv_axis(ctypes.byref(g), _dp(xin), _dp(out.view(np.float64)), int(idir),
+                                      int(bool(ref_axis)))
     if rc != 0:
         raise RuntimeError("oracle compute_deriv failed")
     return out.reshape(storage_shape(gdims, mo))

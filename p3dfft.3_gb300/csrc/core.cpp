@@ -241,6 +241,24 @@ static int arith_mode() {
   return g_arith;
 }
 
+// Reference-compatible behaviour for two reference defects that give deterministic results
+// (on by default, so that outputs are the reference's; P3DFFT_GB300_REFERENCE_COMPAT=0 or
+// p3dfft_gb300_set_reference_compat(0) selects the corrected behaviour):
+//  - compute_deriv differentiates along storage axis imo[idir] (the logical dim whose storage
+//    rank is idir, build/deriv.C:89-93), not along the storage axis of logical dim idir; the two
+//    differ only for the 3-cycle memory orders (1,2,0) and (2,0,1);
+//  - a 1D plan whose input and output orders both have the transform dim non-leading reads its
+//    input as if stored in order swap0(mo1, dim): find_m overwrites the plan's own mo1
+//    (build/templ.C:1015-1023) and exec then reorders from that order (exec.C:582-611).
+static int g_ref_compat = -1;
+static int ref_compat() {
+  if (g_ref_compat < 0) {
+    const char *s = getenv("P3DFFT_GB300_REFERENCE_COMPAT");
+    g_ref_compat = (s && s[0] == '0') ? 0 : 1;
+  }
+  return g_ref_compat;
+}
+
 static long long elems(const GridDesc &g) { return (long long)g.gdims[0] * g.gdims[1] * g.gdims[2]; }
 
 static void strides(const GridDesc &g, long long s[3]) {
@@ -544,13 +562,16 @@ static Plan *make_plan1(int type, const GridDesc &g1, const GridDesc &g2, int d)
   Plan *P = new Plan();
   P->g1 = g1;
   P->g2 = g2;
+  // find_m (templ.C:1015-1023): neither order leads with the transform dim, so the reference
+  // replaces its input order by swap0(mo1, d) and reads the input in that order
+  if (ref_compat() && t.kind != K_EMPTY && g1.mo[d] != 0 && g2.mo[d] != 0) swap0(P->g1.mo, g1.mo, d);
   P->dt1 = t.dt1;
   P->dt2 = t.dt2;
   P->prec = t.prec;
   Stage st;
   st.type = type;
   st.dim = d;
-  st.g1 = g1;
+  st.g1 = P->g1;
   st.g2 = g2;
   P->st.push_back(st);
   P->ex = P->st;
@@ -653,8 +674,9 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
   }
 }
 
+// engine_override >= 0 replaces the plan's tuned engine choice for this stage (0 = heuristic)
 static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv,
-                     const void *tw_given = nullptr, const void *aux_given = nullptr) {
+                     const void *tw_given = nullptr, const void *aux_given = nullptr, int engine_override = -1) {
   const TypeInfo &t = g_types[s.type];
   if (t_ctx && t_ctx->rec) {  // recording for a grouped launch set
     StageLaunch sl;
@@ -683,6 +705,7 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
   } else {
     StageDesc d;
     fill_stage_desc(P, s, deriv, d);
+    if (engine_override >= 0) d.engine = engine_override;
     bool reorder = !(s.g1.mo[0] == s.g2.mo[0] && s.g1.mo[1] == s.g2.mo[1] && s.g1.mo[2] == s.g2.mo[2]);
     TimerScope ts(deriv ? 3 : (reorder ? 1 : 0));
     rc = launch_stage(d, src, dst, P->prec == 8 ? arith_mode() : AR_NATIVE, cur_stream(), g_tabs, &launched, tw_given,
@@ -1028,6 +1051,14 @@ static int store_plan(std::vector<Plan *> &v, Plan *P) {
 // which are generated into `tw_host` and copied in stream order.  Makes no device allocation.
 int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *scratch0, void *scratch1,
                            size_t scratch_bytes, void *tw_dev, size_t tw_bytes, void *tw_host) {
+  // The tables are staged through the host array tw_host, which the next call overwrites: a
+  // captured graph would copy whatever it holds at replay time, so capture is refused.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(cur_stream(), &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    set_err(E_UNSUPPORTED, "this entry point stages its tables through host memory and cannot run on a capturing stream");
+    return E_UNSUPPORTED;
+  }
   Plan *P = get_plan(g_plans3, plan);
   if (!P) {
     set_err(E_BAD_ARG, "invalid 3D plan handle %d", plan);
@@ -1060,36 +1091,52 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
     set_err(E_BAD_ARG, "single-stage in-place transform needs an extra buffer; pass in != out");
     return E_BAD_ARG;
   }
-  // twiddle tables of every stage, packed into the given region
+  // twiddle tables of every stage, packed into the given region.  Each stage's needs are queried
+  // with the derivative flag and the buffers it will run with, so that the query and the launch
+  // choose the same kernel (and table format).  A tuned engine that needs cached tables (Bluestein,
+  // the specialised DCT/DST II-IV kernel) falls back to the heuristic choice.
   const void *tw[8] = {nullptr}, *aux[8] = {nullptr};
+  int eng[8];
   size_t off = 0;
   unsigned char *host = static_cast<unsigned char *>(tw_host);
+  const void *qsrc = in;
   for (int s = 0; s < n; s++) {
     const Stage &st = P->ex[s];
+    eng[s] = -1;
+    const void *ssrc = qsrc;
+    qsrc = dst[s];
     if (g_types[st.type].kind == K_EMPTY) continue;
+    const bool deriv = idir >= 0 && st.dim == idir;
     StageDesc d;
-    fill_stage_desc(P, st, false, d);
+    fill_stage_desc(P, st, deriv, d);
     TableNeed need{0, 0, 0, 0};
-    int rc = launch_stage(d, nullptr, nullptr, P->prec == 8 ? arith_mode() : AR_NATIVE, cur_stream(), nullptr, nullptr,
-                          nullptr, nullptr, &need);
+    const int arith = P->prec == 8 ? arith_mode() : AR_NATIVE;
+    int rc = launch_stage(d, ssrc, dst[s], arith, cur_stream(), nullptr, nullptr, nullptr, nullptr, &need);
+    if (rc == E_UNSUPPORTED && d.engine != 0) {
+      d.engine = 0;
+      eng[s] = 0;
+      rc = launch_stage(d, ssrc, dst[s], arith, cur_stream(), nullptr, nullptr, nullptr, nullptr, &need);
+    }
     if (rc != E_OK) {
-      set_err(rc, "stage %d cannot run (transform length unsupported)", s);
+      set_err(rc, "stage %d cannot run with caller-supplied tables (length %d unsupported on this path)", s,
+              st.g1.gdims[st.dim]);
       return rc;
     }
-    size_t b1 = table_bytes(need.tabN, need.fmt);
-    size_t b2 = need.auxN ? (need.aux_pass ? pass_table_bytes(need.auxN, need.fmt) : table_bytes(need.auxN, need.fmt)) : 0;
-    if (off + b1 + b2 > tw_bytes) {
+    const size_t b1 = table_bytes(need.tabN, need.fmt);
+    const size_t b2 = need.auxN ? (need.aux_pass ? pass_table_bytes(need.auxN, need.fmt) : table_bytes(need.auxN, need.fmt)) : 0;
+    const size_t a1 = (b1 + 255) & ~(size_t)255, a2 = (b2 + 255) & ~(size_t)255;
+    if (off + a1 + a2 > tw_bytes) {  // both tables, each starting on a 256-byte boundary
       set_err(E_TOO_LARGE, "twiddle tables exceed the %zu-byte static table region", tw_bytes);
       return E_TOO_LARGE;
     }
     fill_table(need.tabN, need.fmt, host + off);
     tw[s] = static_cast<unsigned char *>(tw_dev) + off;
-    off += (b1 + 255) & ~(size_t)255;
+    off += a1;
     if (b2) {
       if (need.aux_pass) fill_pass_table(need.auxN, need.fmt, host + off);
       else fill_table(need.auxN, need.fmt, host + off);
       aux[s] = static_cast<unsigned char *>(tw_dev) + off;
-      off += (b2 + 255) & ~(size_t)255;
+      off += a2;
     }
   }
   if (off && cudaMemcpyAsync(tw_dev, tw_host, off, cudaMemcpyHostToDevice, cur_stream()) != cudaSuccess) {
@@ -1100,7 +1147,7 @@ int exec_plan_given_memory(int plan, const void *in, void *out, int idir, void *
   for (int s = 0; s < n; s++) {
     const Stage &st = P->ex[s];
     bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
-    int rc = run_stage(P, st, src, dst[s], deriv, tw[s], aux[s]);
+    int rc = run_stage(P, st, src, dst[s], deriv, tw[s], aux[s], eng[s]);
     if (rc != E_OK) return rc;
     src = dst[s];
   }
@@ -1239,6 +1286,8 @@ void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
 void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on ? 1 : 0; }
 void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }
+void p3dfft_gb300_set_reference_compat(int on) { g_ref_compat = on ? 1 : 0; }
+int p3dfft_gb300_get_reference_compat(void) { return ref_compat(); }
 int p3dfft_gb300_get_fp64_arith(void) { return arith_mode(); }
 const char *p3dfft_gb300_version(void) { return "p3dfft-gb300 0.1 (sm_103a)"; }
 
@@ -1454,7 +1503,7 @@ int p3dfft_gb300_compute_deriv(int prec, const void *in, void *out, const int gd
     dout = B.stage_out;
   }
   int launched = 0;
-  int rc = launch_deriv(prec, g.gdims, s, idir, gg, din, dout, g_stream, &launched);
+  int rc = launch_deriv(prec, g.gdims, s, idir, gg, ref_compat(), din, dout, g_stream, &launched);
   g_kcount += launched;
   if (rc != E_OK) {
     set_err(rc, "compute_deriv launch failed");

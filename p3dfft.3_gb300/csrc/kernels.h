@@ -107,7 +107,9 @@ void launch_set_destroy(LaunchSet *set);
 int launch_permute(const int d[3], const long long s1[3], const long long s2[3], int esize,
                    const void *in, void *out, cudaStream_t stream, int *kernels_launched);
 // Standalone spectral derivative on a complex field (build/deriv.C:85-184), in may equal out.
-int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, const void *in,
+// ref_axis: differentiate along storage axis imo[idir] as build/deriv.C:89-93 does (else along
+// the storage axis of logical dim idir); the wavenumbers come from g in both cases
+int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, int ref_axis, const void *in,
                  void *out, cudaStream_t stream, int *kernels_launched);
 
 DeviceTables *tables_create();

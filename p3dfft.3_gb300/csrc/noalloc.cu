@@ -8,7 +8,10 @@
 //
 // The array is P3DFFT_GB300_NOALLOC_BYTES long and every GPU that loads the library holds it
 // until the process exits.  All calls share it and it keeps the last call's contents; calls
-// that overlap on the GPU (different streams, or several host threads) race on it.
+// that overlap on the GPU (different streams, or several host threads) race on it.  The twiddle
+// tables reach it through the static host array g_tw_host, which the next call overwrites, so
+// calls on a capturing stream are refused (a replayed graph would copy the host array as it is
+// at replay time).
 #include <cuda_runtime.h>
 
 #include <cstddef>

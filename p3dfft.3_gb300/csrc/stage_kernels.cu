@@ -1244,8 +1244,8 @@ int launch_permute(const int d[3], const long long s1[3], const long long s2[3],
   return rc;
 }
 
-int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, const void *in, void *out,
-                 cudaStream_t stream, int *kernels_launched) {
+int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, int ref_axis, const void *in,
+                 void *out, cudaStream_t stream, int *kernels_launched) {
   // storage dims (fastest first) and the storage position of idir
   int order[3] = {0, 1, 2};
   for (int i = 0; i < 3; i++)
@@ -1254,6 +1254,8 @@ int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g
   int pos = 0;
   for (int i = 0; i < 3; i++)
     if (order[i] == idir) pos = i;
+  // deriv.C:89-93 takes ldir with MemOrder[ldir] == idir and uses it as the storage axis
+  if (ref_axis) pos = order[idir];
   long long n = (long long)d[0] * d[1] * d[2];
   if (n == 0) return E_OK;
   int mid = g / 2;

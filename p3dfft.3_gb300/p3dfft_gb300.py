@@ -62,6 +62,8 @@ def lib():
         "p3dfft_gb300_set_stream": ([vp], None), "p3dfft_gb300_set_sync": ([ctypes.c_int], None),
         "p3dfft_gb300_set_host_direct": ([ctypes.c_int], None),
         "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
+        "p3dfft_gb300_set_reference_compat": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_reference_compat": ([], ctypes.c_int),
         "p3dfft_gb300_plan3d": ([ip, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_exec3d": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_destroy3d": ([ctypes.c_int], ctypes.c_int),
@@ -145,6 +147,18 @@ def cleanup():
 def set_fp64_arith(mode: int):
     """0: native FP64 (DFMA); 1: float-float on the FP32 pipe."""
     lib().p3dfft_gb300_set_fp64_arith(int(mode))
+
+
+def set_reference_compat(on: bool):
+    """True (default): compute_deriv's axis choice and the 1D input-order reinterpretation of the
+    reference (build/deriv.C:89-93, build/templ.C:1015-1023), so results equal the reference's;
+    False: the corrected behaviours (differentiate along logical dim idir; read 1D inputs in their
+    declared memory order)."""
+    lib().p3dfft_gb300_set_reference_compat(1 if on else 0)
+
+
+def get_reference_compat() -> bool:
+    return bool(lib().p3dfft_gb300_get_reference_compat())
 
 
 def set_sync(sync: bool):

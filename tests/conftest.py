@@ -8,7 +8,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "p3dfft.3_gb300")
-for p in (os.path.join(ROOT, "oracle"), PKG):
+for p in (os.path.join(ROOT, "oracle"), PKG, os.path.dirname(os.path.abspath(__file__))):
     if p not in sys.path:
         sys.path.insert(0, p)
 
@@ -35,12 +35,18 @@ def p3d():
 
 @pytest.fixture(scope="session")
 def gpu(p3d):
-    """The library on a GPU; fails (does not skip) when the CUDA path cannot run."""
+    """The library on a GPU; fails (does not skip) when the CUDA path cannot run.
+
+    The oracle-parity tests compare against the transforms' defined results, so the session runs
+    with the library's reference-compatibility mode off (compute_deriv along logical dim idir, 1D
+    inputs read in their declared order); tests against the reference's own outputs
+    (test_gpu_ref_golden.py) switch it on for their duration."""
     import ctypes
     p = p3d.lib().p3dfft_gb300_device_alloc(16)
     if not p:
         raise RuntimeError("CUDA device unavailable: " + p3d.lib().p3dfft_last_error_string().decode())
     p3d.lib().p3dfft_gb300_device_free(ctypes.c_void_p(p))
+    p3d.set_reference_compat(False)
     return p3d
 
 

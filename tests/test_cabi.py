@@ -18,7 +18,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(ROOT, "p3dfft.3_gb300", "lib")
-REF_SAMPLES = "/root/reference/sample"
+import refpin  # noqa: E402
+
+REF_SAMPLES = refpin.sample_dir()  # $P3DFFT_REFERENCE_SAMPLES, or the reference tree's sample/
 
 FUNC_RE = re.compile(r"^\s*(?:extern\s+)?[A-Za-z_][\w\s\*]*?\b((?:p3dfft|MPI|find_grid)\w*)\s*\(", re.M)
 
@@ -98,7 +100,7 @@ C_SAMPLES = ["test3D_r2c", "test_deriv", "test1D_cos", "test1D_r2c", "test2D+emp
              "test3D_c2c_inplace", "test3D_r2c_memord", "test3D_r2c_single", "test1D_cos_complex"]
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SAMPLES), reason="reference sample programs not present")
+@pytest.mark.skipif(REF_SAMPLES is None, reason="reference sample programs not present")
 @pytest.mark.parametrize("name,cxx", [(n, True) for n in CPP_SAMPLES] + [(n, False) for n in C_SAMPLES])
 def test_reference_samples_compile_unchanged(p3d, tmp_path, name, cxx):
     src = os.path.join(REF_SAMPLES, "C++" if cxx else "C", name + (".C" if cxx else ".c"))
