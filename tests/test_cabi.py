@@ -89,7 +89,17 @@ def _compile(src, out, cxx):
     assert r.returncode == 0, r.stderr[-2000:]
 
 
-@pytest.mark.parametrize("prog", ["cpp_r2c_deriv.cpp", "c_api_c2c.c"])
+def test_fortran_module_variables_are_set_by_setup(p3d, tmp_path):
+    """A Fortran program's module variables (the type IDs bound by the reference's
+    build/fp3dfft++mod.f90) live in the program; p3dfft_setup must fill them in.  The C stand-in
+    for that program defines them itself and checks their values (no GPU needed)."""
+    exe = str(tmp_path / "fabi")
+    _compile(os.path.join(ROOT, "tests", "programs", "fortran_abi.c"), exe, False)
+    r = subprocess.run([exe, "ids"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "Results are correct" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("prog", ["cpp_r2c_deriv.cpp", "c_api_c2c.c", "fortran_abi.c"])
 def test_own_programs_compile(p3d, tmp_path, prog):
     _compile(os.path.join(ROOT, "tests", "programs", prog), str(tmp_path / "a.out"), prog.endswith(".cpp"))
 

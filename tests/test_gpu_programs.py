@@ -36,3 +36,11 @@ def test_cpp_api_program(gpu, tmp_path, dims):
 def test_c_api_program(gpu, tmp_path, dims):
     r = _build_and_run(tmp_path, "c_api_c2c.c", dims)
     assert r.returncode == 0 and "Results are correct" in r.stdout, r.stdout + r.stderr
+
+
+def test_fortran_entry_points(gpu, tmp_path):
+    """Every *_f entry point (reference build/wrap.C:575-792) called as a compiled Fortran program
+    calls it (by reference, 1-based derivative direction, program-owned type-ID variables), each
+    bit-identical to the matching C entry point (tests/programs/fortran_abi.c)."""
+    r = _build_and_run(tmp_path, "fortran_abi.c", [])
+    assert r.returncode == 0 and "Results are correct" in r.stdout, r.stdout + r.stderr
