@@ -367,6 +367,18 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
     ms_nog, _ = time_batch(b_nog)
     b_br = make_batch(mixed, grouped=False)
     ms_br, k_br = time_batch(b_br)
+    # work lists: one launch per (stage level, kernel) over all jobs' tiles
+    b_wl = make_batch(mixed, grouped="list")
+    ms_wl, k_wl = time_batch(b_wl)
+    b_wl32 = make_batch(single, grouped="list")
+    ms_wl32, _ = time_batch(b_wl32)
+    # the same with persistent CTAs: each work-list launch's grid capped at the resident CTAs
+    os.environ["P3DFFT_GB300_LIST_PERSISTENT"] = "1"
+    try:
+        b_wlp = make_batch(mixed, grouped="list")
+        ms_wlp, _ = time_batch(b_wlp)
+    finally:
+        del os.environ["P3DFFT_GB300_LIST_PERSISTENT"]
 
     # 48 sequential plain FP64 calls: the reference-style synchronous exec, one job after another
     p3d.set_sync(True)
@@ -409,6 +421,13 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
                                  "speedup_vs_sequential_fp64": ms_seq / ms_b32,
                                  "speedup_vs_batch_fp64": ms_b64 / ms_b32,
                                  "max_rel_l2_vs_fp64": err32},
+        "batch_graph_work_list_mixed": {"ms": ms_wl, "round_trips_per_s": n / (ms_wl * 1e-3), "kernels_per_exec": k_wl,
+                                        "work_list_launches": b_wl.groups(),
+                                        "mode": "one launch per (stage level, kernel) over every job's tiles (device work list of (stage, tile) items); launches round-robin on the branch streams, each waiting only for the launches of its jobs' previous stage"},
+        "batch_graph_work_list_persistent_mixed": {"ms": ms_wlp, "round_trips_per_s": n / (ms_wlp * 1e-3),
+                                                   "mode": "work lists walked by persistent CTAs (grid = resident CTAs)"},
+        "batch_graph_work_list_all_fp32": {"ms": ms_wl32, "round_trips_per_s": n / (ms_wl32 * 1e-3),
+                                           "speedup_vs_sequential_fp64": ms_seq / ms_wl32},
         "batch_streams_no_graph_mixed": {"ms": ms_nog, "round_trips_per_s": n / (ms_nog * 1e-3)},
         "sequential_plain_fp64": {"ms": ms_seq, "round_trips_per_s": n / (ms_seq * 1e-3),
                                   "GB_per_s": alg_plain / (ms_seq * 1e-3) / 1e9},
@@ -417,7 +436,7 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
         "autotune": {"seconds": t_tune, "engines": "1 specialised, 2 register, 3 generic; [engine, alt tile dim, ms]",
                      "choices": tuning},
     }
-    for bt in (b_mixed, b_f64, b_f32, b_nog, b_br):
+    for bt in (b_mixed, b_f64, b_f32, b_nog, b_br, b_wl, b_wl32, b_wlp):
         del bt
     return out
 
@@ -581,6 +600,57 @@ def serve_workload(p3d, n_jobs=10000, seed=5, fractions=(0.5, 0.75, 0.9), nslots
             "failed": st["failed"], "max_running": st["max_running"], "peak_hbm_GB": st["peak_hbm_bytes"] / 1e9})
     del src, sink
     return out
+
+
+def fp32_line_errors(p3d, lengths=(64, 128, 256, 512, 1024, 2048)):
+    """FP32 C2C lines (64 x 16 of each length, U[-1,1) complex) against numpy's FP64 FFT of the
+    same FP32 inputs: relative L2 error with split and with plain twiddles."""
+    out = {}
+    rng = np.random.default_rng(32)
+    for n in lengths:
+        g = (n, 64, 16)
+        x = (rng.uniform(-1, 1, (16, 64, n)) + 1j * rng.uniform(-1, 1, (16, 64, n))).astype(np.complex64)
+        ref = np.fft.fft(x.astype(np.complex128), axis=-1)
+        row = {}
+        for split in (True, False):
+            p3d.set_fp32_split_twiddles(split)
+            y = np.empty_like(x)
+            p3d.TransPlan(p3d.CFFT_FORWARD_S, g, (0, 1, 2), g, (0, 1, 2), 0).exec(x, y)
+            row["split" if split else "plain"] = float(np.linalg.norm(y - ref) / np.linalg.norm(ref))
+        out[str(n)] = row
+    p3d.set_fp32_split_twiddles(True)
+    return out
+
+
+def full_size_parity(p3d, f, b, d_in, d_spec, d_out):
+    """The headline plans at full size against the reference: the forward transform with the
+    fused d/dz derivative of the 512^3 reference input (tests/golden/ref_golden.npz, written from
+    the reference's own build; compared by the size-independent fingerprint of tests/refpin.py),
+    and the normalised plain round trip of the same input."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import refpin
+    z = np.load(os.path.join(ROOT, "tests", "golden", "ref_golden.npz"))
+    metas = json.loads(str(z["meta"]))
+    hit = [(i, m) for i, m in enumerate(metas) if m["kind"] == "config" and m["name"] == "config2"]
+    if not hit or tuple(hit[0][1]["g1"]) != GD:
+        return {"skipped": "no 512^3 reference fixture for this grid"}
+    i, m = hit[0]
+    x = refpin.det_field(p3d.storage_shape(GD, MO1), m["seed"], False)
+    d_in.upload(x)
+    p3d.set_sync(True)
+    f.exec(d_in, d_spec, idir=m["idir"])
+    spec = d_spec.download(np.empty(p3d.storage_shape(GD2, MO2), np.complex128))
+    ref = {k: z[f"c{i}_{k}"] for k in ("idx", "val", "proj", "norm")}
+    err_ref = float(refpin.fingerprint_error(refpin.fingerprint(spec), ref))
+    del spec
+    f.exec(d_in, d_spec)
+    b.exec(d_spec, d_out)
+    back = d_out.download(np.empty(p3d.storage_shape(GD, MO1), np.float64)) / float(np.prod(GD))
+    err_rt = float(np.linalg.norm(back - x) / np.linalg.norm(x))
+    p3d.set_sync(False)
+    return {"forward_ddz_vs_reference_fingerprint": err_ref, "normalised_round_trip_rel_l2": err_rt,
+            "tolerance": 1e-12, "input": "refpin.det_field seed %d (the reference's 512^3 fixture input)" % m["seed"],
+            "reference": "reference build/*.C compiled unchanged, outputs in tests/golden/ref_golden.npz"}
 
 
 def main():
@@ -773,17 +843,42 @@ def main():
 
     # page-locked host arrays: the x stages read / write them over NVLink-C2C (default), or
     # staged through HBM with copies
-    p3d.set_host_direct(False)
-    e2e_staged_ms = e2e_run()
+    modes_ms = {}
+    for mode, key in ((False, "staged_both"), ("in", "direct_in_staged_out"), ("out", "staged_in_direct_out"),
+                      (True, "direct_both")):
+        p3d.set_host_direct(mode)
+        modes_ms[key] = e2e_run()
     p3d.set_host_direct(True)
-    e2e_ms = e2e_run()
+    e2e_staged_ms = modes_ms["staged_both"]
+    e2e_ms = modes_ms["direct_both"]
     e2e = {"value": ALG_BYTES * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": S_R,
            "d2h_bytes_per_step": S_R, "ms_per_step": e2e_ms,
            "host_io": "page-locked host arrays read by the x R2C stage and written by the x C2R stage over NVLink-C2C",
            "staged_copies": {"ms_per_step": e2e_staged_ms,
-                             "value": ALG_BYTES * world / (e2e_staged_ms * 1e-3) / 1e9}}
+                             "value": ALG_BYTES * world / (e2e_staged_ms * 1e-3) / 1e9},
+           "host_io_modes_ms": modes_ms}
     rt_err = float(np.linalg.norm(hout.array - y) / max(np.linalg.norm(y), 1e-300))
+    # per-phase breakdown of the end-to-end step (CUDA events around each stage, page-locked host
+    # arrays read / written directly by the x stages): the host-link-bound x R2C and x C2R, the
+    # on-device stages between them, and the host time outside the stages
+    ph_f, ph_b = (ctypes.c_double * 8)(), (ctypes.c_double * 8)()
+    nf = L.p3dfft_gb300_profile_stages(f.handle, ctypes.c_void_p(hin.ptr), ctypes.c_void_p(d_spec.ptr), IDIR, 3, ph_f, 8)
+    nb = L.p3dfft_gb300_profile_stages(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(hout.ptr), -1, 3, ph_b, 8)
+    if nf > 0 and nb > 0:
+        fwd_ms, bwd_ms = list(ph_f)[:nf], list(ph_b)[:nb]
+        link_ms = fwd_ms[0] + bwd_ms[-1]
+        dev_ms = sum(fwd_ms[1:]) + sum(bwd_ms[:-1])
+        e2e["phases_ms"] = {
+            "x_r2c_reading_host": fwd_ms[0], "on_device_stages": dev_ms, "x_c2r_writing_host": bwd_ms[-1],
+            "outside_stage_kernels": e2e_ms - link_ms - dev_ms,
+            "forward_stages": fwd_ms, "backward_stages": bwd_ms,
+            "host_link_GBps": {"h2d_in_x_r2c": S_R / (fwd_ms[0] * 1e-3) / 1e9,
+                               "d2h_in_x_c2r": S_R / (bwd_ms[-1] * 1e-3) / 1e9}}
     del hin, hout
+
+    # ---- full-size parity: the 512^3 forward with fused d/dz against the reference's own output ----
+    parity = full_size_parity(p3d, f, b, d_in, d_spec, d_out)
+    d_in.upload(x)
 
     # ---- the other FP64 arithmetic and the FP32 form, same workload, device-resident ----
     def timed(fh, bh, din, dspec, dout, steps):
@@ -799,6 +894,16 @@ def main():
         return L.p3dfft_gb300_event_elapsed_ms(2, 3) / steps
 
     forms = {}
+    if arith:
+        # the same float-float round trip with IEEE-double intermediate fields (A/B of the
+        # float-float intermediates)
+        p3d.set_ff_intermediates(False)
+        ms_ieee = timed(f.handle, b.handle, d_in.ptr, d_spec.ptr, d_out.ptr, max(5, args.steps // 5))
+        y_ieee = d_out.download(np.empty_like(y))
+        p3d.set_ff_intermediates(True)
+        forms["fp64_float_float_ieee_intermediates"] = {
+            "ms_per_step": ms_ieee, "value": ALG_BYTES / (ms_ieee * 1e-3) / 1e9, "unit": "GB/s",
+            "rel_l2_vs_headline": float(np.linalg.norm(y_ieee - y) / np.linalg.norm(y))}
     p3d.set_fp64_arith(1 - arith)
     ms_other = timed(f.handle, b.handle, d_in.ptr, d_spec.ptr, d_out.ptr, max(3, args.steps // 10))
     y_other = d_out.download(np.empty_like(y))
@@ -814,7 +919,16 @@ def main():
     y32 = d_out32.download(np.empty(y.shape, np.float32)).astype(np.float64)
     forms["fp32"] = {"ms_per_step": ms32, "value": (ALG_BYTES // 2) / (ms32 * 1e-3) / 1e9, "unit": "GB/s",
                      "round_trips_per_s": 1e3 / ms32, "speedup_vs_fp64_transforms_per_s": ms_step / ms32,
-                     "rel_l2_vs_fp64": float(np.linalg.norm(y32 - y) / np.linalg.norm(y))}
+                     "rel_l2_vs_fp64": float(np.linalg.norm(y32 - y) / np.linalg.norm(y)),
+                     "twiddles": "split (compensated) products on the 512-point lines, FP64-generated tables"}
+    # A/B: plain FP32 twiddles on the long lines too
+    p3d.set_fp32_split_twiddles(False)
+    ms32p = timed(f32.handle, b32.handle, d_in32.ptr, d_spec32.ptr, d_out32.ptr, args.steps)
+    y32p = d_out32.download(np.empty(y.shape, np.float32)).astype(np.float64)
+    p3d.set_fp32_split_twiddles(True)
+    forms["fp32"]["plain_twiddles"] = {"ms_per_step": ms32p,
+                                       "rel_l2_vs_fp64": float(np.linalg.norm(y32p - y) / np.linalg.norm(y))}
+    forms["fp32"]["line_error_vs_fp64_by_length"] = fp32_line_errors(p3d)
     del d_in32, d_spec32, d_out32, f32, b32
     forms["mixed_types_384x256x257"] = mixed_types_workload(p3d, L, max(5, args.steps // 5), arith)
     if not args.no_batch:
@@ -833,7 +947,7 @@ def main():
                        "input": "numpy PCG64 U[-1,1) seed 512+rank", "parallelism": f"replicas x{world}",
                        "algorithmic_bytes_per_step": ALG_BYTES},
             "roofline": roofline, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
-            "host_vs_device_rel_diff": rt_err, "other_forms": forms}
+            "host_vs_device_rel_diff": rt_err, "parity": parity, "other_forms": forms}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0:

@@ -34,8 +34,10 @@ void p3dfft_gb300_set_stream(void *cuda_stream);
 void p3dfft_gb300_set_sync(int sync);
 /* 1 (default): page-locked host arrays (cudaHostAlloc, cudaHostRegister,
  * p3dfft_gb300_host_alloc_pinned) are read by the first stage and written by the last stage
- * directly over NVLink-C2C, without staging copies; 0: always stage host arrays through HBM.
- * Pageable host arrays are always staged.  P3DFFT_GB300_HOST_DIRECT=0 sets 0 at start-up. */
+ * directly over NVLink-C2C, without staging copies; 2: inputs only; 3: outputs only; 0: always
+ * stage host arrays through HBM (slab by slab, the copies overlapped with the stage, for fields
+ * of 32 MB and more).  Pageable host arrays are always staged.  P3DFFT_GB300_HOST_DIRECT=0 /
+ * in / out sets 0 / 2 / 3 at start-up. */
 void p3dfft_gb300_set_host_direct(int on);
 /* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,
  * ~1e-14 relative L2 per 3D transform), 0 = native FP64 DFMA (slow on GB300).  The initial value
@@ -52,6 +54,19 @@ int p3dfft_gb300_get_fp64_arith(void);
  * set with P3DFFT_GB300_REFERENCE_COMPAT=0. */
 void p3dfft_gb300_set_reference_compat(int on);
 int p3dfft_gb300_get_reference_compat(void);
+/* 1 (default): with float-float FP64 arithmetic, consecutive stages that both run the specialised
+ * float-float kernels pass their intermediate field as packed float-float pairs at per-line
+ * power-of-two scales (plus a side array of the scales) instead of IEEE doubles, which saves the
+ * conversions; the caller's input and output are IEEE doubles either way.  0: every stage reads
+ * and writes IEEE doubles.  The initial value can be set with P3DFFT_GB300_FF_INTERMEDIATE=0. */
+void p3dfft_gb300_set_ff_intermediates(int on);
+int p3dfft_gb300_get_ff_intermediates(void);
+/* 1 (default): FP32 stages whose FFT length is 512, 1024 or 2048 multiply by split twiddles, each
+ * the FP32 pair (hi, lo) of its long-double value, as a * hi + a * lo (compensated twiddle
+ * products: the twiddle adds no rounding of its own); 0: FP32 twiddles, most formed as products
+ * of two table entries.  The initial value can be set with P3DFFT_GB300_FP32_SPLIT_TWIDDLES=0. */
+void p3dfft_gb300_set_fp32_split_twiddles(int on);
+int p3dfft_gb300_get_fp32_split_twiddles(void);
 
 /* ---- planning / execution by explicit grid descriptions (1x1x1 processor grid) ----
  * A grid is (gdims[3], mem_order[3], dim_conj_sym).  Returns a handle >= 0, or -1 with the
@@ -131,7 +146,14 @@ int p3dfft_gb300_batch_add(int batch, int job, int plan, const void *in, void *o
 int p3dfft_gb300_batch_set_graph(int batch, int on);
 /* 1 (default): jobs with the same steps form a cohort; each stage of a cohort is one launch of its
  * specialised kernel over all the cohort's jobs' tiles; cohorts run on `nbranches` concurrent
- * streams.  0: every job's stages launched separately, jobs spread over the streams. */
+ * streams.  2: work lists: the k-th stages of all jobs form level k, and within a level every
+ * stage that runs the same specialised kernel (arithmetic, kind, FFT length) joins one launch
+ * over all their tiles, whatever their grids, memory orders and buffers (a device list of
+ * (stage, tile) items with each stage's parameters).  The launches go round-robin to the
+ * `nbranches` streams, each waiting only for the launches that ran the previous stage of its own
+ * jobs.  Set P3DFFT_GB300_LIST_PERSISTENT=1 before the first exec to cap each such launch's grid
+ * at the resident CTAs (persistent CTAs walk the list).
+ * 0: every job's stages launched separately, jobs spread over the streams. */
 int p3dfft_gb300_batch_set_grouped(int batch, int on);
 /* grouped launches one exec makes (0 in branch mode) */
 int p3dfft_gb300_batch_groups(int batch);
@@ -154,6 +176,11 @@ int p3dfft_gb300_server_submit(int srv, int plan_fwd, int plan_bwd, int idir, co
                                double arrival_s);
 /* 0 done, 1 timeout (timeout_s < 0 waits indefinitely), < 0 failed with error -return */
 int p3dfft_gb300_server_wait(int srv, int job, double timeout_s);
+/* Failure injection on the host (for tests): the job's device allocation fails when it is
+ * admitted, as if the memory pool had no room; the job then fails with P3DFFT_ERR_CUDA, its slot
+ * and budget return to the server, and the other jobs are unaffected.  The job must still be
+ * waiting for admission (submit it with a future arrival time). */
+int p3dfft_gb300_server_inject_alloc_failure(int srv, int job);
 int p3dfft_gb300_server_drain(int srv);
 /* seconds since server creation */
 double p3dfft_gb300_server_clock(int srv);

@@ -28,8 +28,10 @@ CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "
 CFLAGS += os.environ.get("P3DFFT_GB300_NVCC_FLAGS", "").split()  # extra tuning defines
 
 SOURCES = ["stage_kernels.cu", "core.cpp", "batch.cpp", "serve.cpp", "noalloc.cu"]
-# fast_inst.cu once per (arithmetic, kind): 0 float-float / 1 FP64 / 2 FP32 x C2C / R2C / C2R
-FAST_UNITS = [(a, k) for a in range(3) for k in range(5)]
+# fast_inst.cu once per (arithmetic, kind, part): 0 float-float / 1 FP64 / 2 FP32 / 3 FP32 with
+# split twiddles x C2C / R2C / C2R / DCT-I,DST-I / DCT,DST II-IV; the float-float units in two
+# halves of the lengths
+FAST_UNITS = [(a, k, p) for a in range(4) for k in range(5) for p in range(2 if a == 0 else 1)]
 HEADERS = ["kernels.h", "runtime.h", "df_arith.cuh", "stage_common.cuh", "fast_stage.cuh"]
 
 
@@ -54,8 +56,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     jobs = []
     objs = []
     units = [(src, src + ".o", []) for src in SOURCES]
-    units += [("fast_inst.cu", f"fast_inst_a{a}_k{k}.o", [f"-DP3D_FAST_ARITH={a}", f"-DP3D_FAST_KIND={k}"])
-              for a, k in FAST_UNITS]
+    units += [("fast_inst.cu", f"fast_inst_a{a}_k{k}_p{p}.o",
+               [f"-DP3D_FAST_ARITH={a}", f"-DP3D_FAST_KIND={k}", f"-DP3D_FAST_PART={p}"])
+              for a, k, p in FAST_UNITS]
     for src, obj, defs in units:
         sp = os.path.join(CSRC, src)
         op = os.path.join(OBJ, obj)

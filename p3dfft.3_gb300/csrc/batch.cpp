@@ -45,9 +45,13 @@ struct Batch {
   cudaGraphExec_t gexec = nullptr;
   bool use_graph = true;
   bool grouped = true;          // level-synchronous grouped launches (else one stream per branch)
+  bool work_list = false;       // grouped mode over all jobs: one work-list launch per kernel per level
   std::vector<void *> job_sets;          // grouped mode: one scratch set per job
   std::vector<LaunchSet *> lsets;         // grouped mode: one launch set per cohort
   std::vector<std::vector<int>> cassign;  // grouped mode: branch -> cohorts
+  // work-list mode: the job at each position of each level, and one event per launch
+  std::vector<std::vector<int>> level_jobs;
+  std::vector<cudaEvent_t> item_ev;
   int ngroups = 0;
   bool dirty = true;
   int arith = -1;
@@ -60,6 +64,7 @@ struct Batch {
     for (auto p : job_sets) scratch_set_destroy(p);
     for (auto s : br) cudaStreamDestroy(s);
     for (auto e : join) cudaEventDestroy(e);
+    for (auto e : item_ev) cudaEventDestroy(e);
     for (auto p : sets) scratch_set_destroy(p);
     if (fork) cudaEventDestroy(fork);
     if (origin) cudaStreamDestroy(origin);
@@ -179,6 +184,36 @@ static int prepare_grouped(Batch *B) {
     cohorts[key].push_back({kv.first, rec});
     job_bytes[kv.first] = w;
   }
+  if (B->work_list) {
+    // every job's k-th stage in level k; within a level, one work-list launch per kernel
+    std::vector<std::vector<StageLaunch>> levels;
+    B->level_jobs.clear();
+    for (auto &c : cohorts)
+      for (auto &jr : c.second) {
+        if (levels.size() < jr.second.size()) {
+          levels.resize(jr.second.size());
+          B->level_jobs.resize(jr.second.size());
+        }
+        for (size_t k = 0; k < jr.second.size(); k++) {
+          levels[k].push_back(jr.second[k]);
+          B->level_jobs[k].push_back(jr.first);
+        }
+      }
+    int err = E_OK;
+    LaunchSet *ls = launch_set_build(levels, device_tables(), &err, true);
+    if (!ls) return fail(err ? err : E_CUDA, "batch: work-list launch set could not be built");
+    B->ngroups = launch_set_groups(ls);
+    B->lsets.push_back(ls);
+    size_t nitems = 0;
+    for (int l = 0; l < launch_set_levels(ls); l++) nitems += (size_t)launch_set_items(ls, l);
+    while (B->item_ev.size() < nitems) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        return fail(E_CUDA, "batch: event creation failed");
+      B->item_ev.push_back(e);
+    }
+    return E_OK;
+  }
   // Jobs large enough to fill the GPU on their own (>= 24 MB of steps' fields) gain nothing from a
   // shared launch and run better spread over the streams: they form cohorts of one.
   std::vector<std::vector<std::pair<int, std::vector<StageLaunch>>>> groups;
@@ -219,7 +254,50 @@ static int prepare_grouped(Batch *B) {
   return E_OK;
 }
 
+// Work-list mode: the launches of a level go round-robin to the branch streams (largest first); a
+// launch waits only for the launches that ran the previous stage of its own jobs.
+static int run_work_list(Batch *B, cudaStream_t st) {
+  LaunchSet *ls = B->lsets[0];
+  int launched = 0, rc = E_OK;
+  if (cudaEventRecord(B->fork, st) != cudaSuccess) return fail(E_CUDA, "batch: fork event failed");
+  std::vector<char> used(B->nbr, 0);
+  std::map<int, int> last;  // job -> event index of the launch that ran its latest stage
+  int id = 0, rr = 0;
+  for (int l = 0; l < launch_set_levels(ls) && rc == E_OK; l++) {
+    for (int i = 0; i < launch_set_items(ls, l) && rc == E_OK; i++, id++) {
+      const int b = rr++ % B->nbr;
+      cudaStream_t s = B->br[b];
+      if (!used[b]) {
+        if (cudaStreamWaitEvent(s, B->fork, 0) != cudaSuccess) return fail(E_CUDA, "batch: fork wait failed");
+        used[b] = 1;
+      }
+      std::vector<int> deps;
+      for (int pos : launch_set_item_members(ls, l, i)) {
+        auto it = last.find(B->level_jobs[l][pos]);
+        if (it != last.end()) deps.push_back(it->second);
+      }
+      std::sort(deps.begin(), deps.end());
+      deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
+      for (int d : deps)
+        if (cudaStreamWaitEvent(s, B->item_ev[d], 0) != cudaSuccess) return fail(E_CUDA, "batch: dependency wait failed");
+      rc = launch_set_run_item(ls, l, i, s, &launched);
+      if (cudaEventRecord(B->item_ev[id], s) != cudaSuccess) return fail(E_CUDA, "batch: event record failed");
+      for (int pos : launch_set_item_members(ls, l, i)) last[B->level_jobs[l][pos]] = id;
+    }
+  }
+  // always join, so a failed capture still ends on the origin stream
+  for (int b = 0; b < B->nbr; b++) {
+    if (!used[b]) continue;
+    if (cudaEventRecord(B->join[b], B->br[b]) != cudaSuccess || cudaStreamWaitEvent(st, B->join[b], 0) != cudaSuccess)
+      return fail(E_CUDA, "batch: join failed");
+  }
+  add_kernel_count(launched);
+  if (rc != E_OK) return fail(rc, "batch: work-list launch failed");
+  return E_OK;
+}
+
 static int run_grouped(Batch *B, cudaStream_t st) {
+  if (B->work_list) return run_work_list(B, st);
   int launched = 0, rc = E_OK;
   if (cudaEventRecord(B->fork, st) != cudaSuccess) return fail(E_CUDA, "batch: fork event failed");
   for (int b = 0; b < B->nbr; b++) {
@@ -339,6 +417,7 @@ int p3dfft_gb300_batch_set_grouped(int batch, int on) {
   Batch *B = get_batch(batch);
   if (!B) return fail(E_BAD_ARG, "batch: invalid handle");
   B->grouped = on != 0;
+  B->work_list = on == 2;
   B->dirty = true;
   return E_OK;
 }

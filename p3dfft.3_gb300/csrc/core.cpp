@@ -148,15 +148,27 @@ struct Buffers {
   size_t scratch_bytes = 0;
   void *stage_in = nullptr, *stage_out = nullptr;
   size_t stage_in_bytes = 0, stage_out_bytes = 0;
+  // per-line scales of float-float intermediate fields (one int per line of the producing stage)
+  void *side[2] = {nullptr, nullptr};
+  size_t side_bytes[2] = {0, 0};
   bool owned = true;  // false: scratch[] belongs to the caller (never freed or reallocated here)
   void release() {
     for (int i = 0; i < 2; i++)
       if (scratch[i] && owned) cudaFree(scratch[i]);
+    for (int i = 0; i < 2; i++)
+      if (side[i]) cudaFree(side[i]);
     if (stage_in) cudaFree(stage_in);
     if (stage_out) cudaFree(stage_out);
-    scratch[0] = scratch[1] = stage_in = stage_out = nullptr;
-    scratch_bytes = stage_in_bytes = stage_out_bytes = 0;
+    scratch[0] = scratch[1] = stage_in = stage_out = side[0] = side[1] = nullptr;
+    scratch_bytes = stage_in_bytes = stage_out_bytes = side_bytes[0] = side_bytes[1] = 0;
   }
+};
+// A stage's float-float intermediate links (the StageDesc ffin / ffout fields).
+struct FFLink {
+  int ffin = 0, ffout = 0;
+  const int *sin = nullptr;
+  int *sout = nullptr;
+  long long mi[3] = {0, 0, 0}, mo[3] = {0, 0, 0};
 };
 // Per-stage kernel choice: engine (Engine) and tile-dim flag, 0/0 = heuristic.
 struct StageTune {
@@ -592,15 +604,21 @@ static bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Page-locked host memory (cudaHostAlloc / cudaHostRegister) is addressable by kernels over
-// NVLink-C2C; returns its device-side address, or nullptr for any other pointer.
-static int g_host_direct = -1;  // -1: from P3DFFT_GB300_HOST_DIRECT (default on) at first use
-static void *mapped_host_ptr(const void *p) {
+// Page-locked host arrays read (bit 0) / written (bit 1) by the first / last stage directly over
+// NVLink-C2C instead of staged through HBM.  -1: from P3DFFT_GB300_HOST_DIRECT at first use
+// ("0" none, "in", "out", anything else both; default both).
+static int g_host_direct = -1;
+static int host_direct_mode() {
   if (g_host_direct < 0) {
     const char *e = getenv("P3DFFT_GB300_HOST_DIRECT");
-    g_host_direct = (e && e[0] == '0') ? 0 : 1;
+    g_host_direct = !e ? 3 : (e[0] == '0' ? 0 : (!strcmp(e, "in") ? 1 : (!strcmp(e, "out") ? 2 : 3)));
   }
-  if (!p || !g_host_direct) return nullptr;
+  return g_host_direct;
+}
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister) is addressable by kernels over
+// NVLink-C2C; returns its device-side address, or nullptr for any other pointer.
+static void *mapped_host_ptr(const void *p) {
+  if (!p || !host_direct_mode()) return nullptr;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
@@ -674,9 +692,11 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
   }
 }
 
-// engine_override >= 0 replaces the plan's tuned engine choice for this stage (0 = heuristic)
+// engine_override >= 0 replaces the plan's tuned engine choice for this stage (0 = heuristic);
+// ff: float-float intermediate links of this stage
 static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv,
-                     const void *tw_given = nullptr, const void *aux_given = nullptr, int engine_override = -1) {
+                     const void *tw_given = nullptr, const void *aux_given = nullptr, int engine_override = -1,
+                     const FFLink *ff = nullptr) {
   const TypeInfo &t = g_types[s.type];
   if (t_ctx && t_ctx->rec) {  // recording for a grouped launch set
     StageLaunch sl;
@@ -706,6 +726,16 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
     StageDesc d;
     fill_stage_desc(P, s, deriv, d);
     if (engine_override >= 0) d.engine = engine_override;
+    if (ff) {
+      d.ffin = ff->ffin;
+      d.ffout = ff->ffout;
+      d.sin = ff->sin;
+      d.sout = ff->sout;
+      for (int i = 0; i < 3; i++) {
+        d.mi[i] = ff->mi[i];
+        d.mo[i] = ff->mo[i];
+      }
+    }
     bool reorder = !(s.g1.mo[0] == s.g2.mo[0] && s.g1.mo[1] == s.g2.mo[1] && s.g1.mo[2] == s.g2.mo[2]);
     TimerScope ts(deriv ? 3 : (reorder ? 1 : 0));
     rc = launch_stage(d, src, dst, P->prec == 8 ? arith_mode() : AR_NATIVE, cur_stream(), g_tabs, &launched, tw_given,
@@ -739,8 +769,18 @@ static cudaEvent_t g_slab_ev[17];
 // stream: side 0 copies host `host` into `src` (the stage's staged input) slab by slab before
 // the stage reads it; side 1 copies the stage's output `dst` to host `host` slab by slab after
 // the stage writes it.  All work is ordered on the library stream when this returns.
+// The float-float links of the slab starting at coordinate c along dim sd: the scale arrays are
+// indexed by global coordinates, the slab's lines by coordinates within the slab.
+static const FFLink *slab_link(const FFLink *ff, int c, int sd, FFLink *out) {
+  if (!ff) return nullptr;
+  *out = *ff;
+  if (out->sin) out->sin += (long long)c * out->mi[sd];
+  if (out->sout) out->sout += (long long)c * out->mo[sd];
+  return out;
+}
+
 static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *host, const void *src, void *dst,
-                           bool deriv, int side) {
+                           bool deriv, int side, const FFLink *ff = nullptr) {
   const int NS = 8;
   if (!g_copy_stream) {
     if (cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking) != cudaSuccess) return E_CUDA;
@@ -761,6 +801,7 @@ static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *h
   if (cudaEventRecord(g_slab_ev[16], ms) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[16], 0) != cudaSuccess)
     return E_CUDA;
   int rc = E_OK;
+  FFLink sff;
   for (int c = 0, k = 0; c < len && rc == E_OK; c += per, k++) {
     const int m = std::min(per, len - c);
     Stage sl = st;
@@ -772,9 +813,9 @@ static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *h
                           (size_t)m * u1, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
           cudaEventRecord(g_slab_ev[k], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[k], 0) != cudaSuccess)
         return E_CUDA;
-      rc = run_stage(P, sl, sp, dp, deriv);
+      rc = run_stage(P, sl, sp, dp, deriv, nullptr, nullptr, -1, slab_link(ff, c, sd, &sff));
     } else {
-      rc = run_stage(P, sl, sp, dp, deriv);
+      rc = run_stage(P, sl, sp, dp, deriv, nullptr, nullptr, -1, slab_link(ff, c, sd, &sff));
       if (rc == E_OK &&
           (cudaEventRecord(g_slab_ev[k], ms) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[k], 0) != cudaSuccess ||
            cudaMemcpyAsync(static_cast<unsigned char *>(const_cast<void *>(host)) + (size_t)c * u2, dp, (size_t)m * u2,
@@ -892,6 +933,50 @@ static int autotune_plan(Plan *P) {
   return E_OK;
 }
 
+// Float-float intermediate fields: between two consecutive stages that both run the specialised
+// float-float kernels (C2C, or an R2C producer / C2R consumer), the producer stores its values as
+// packed float-float pairs at its own per-line power-of-two scale (the scales go to a side array)
+// instead of converting them to IEEE doubles, and the consumer rescales them instead of converting
+// back: the same 16 bytes per complex value, without the integer-heavy conversions.  The caller
+// sees IEEE doubles only: the first stage reads and the last stage writes them.
+// P3DFFT_GB300_FF_INTERMEDIATE=0 or p3dfft_gb300_set_ff_intermediates(0) turns this off.
+static int g_ff_inter = -1;
+static bool ff_intermediates() {
+  if (g_ff_inter < 0) {
+    const char *e = getenv("P3DFFT_GB300_FF_INTERMEDIATE");
+    g_ff_inter = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_ff_inter == 1;
+}
+
+// Whether the stage runs the specialised float-float kernel of a kind that can read (C2C, C2R) or
+// write (C2C, R2C) float-float intermediates, with these buffers.
+static void stage_ff_capable(const Plan *P, const Stage &st, const void *src, void *dst, bool deriv, bool *can_in,
+                             bool *can_out) {
+  *can_in = *can_out = false;
+  const int k = g_types[st.type].kind;
+  if (P->prec != 8 || arith_mode() != AR_DF) return;
+  if (k != K_C2C_FWD && k != K_C2C_BWD && k != K_R2C && k != K_C2R) return;
+  StageDesc d;
+  fill_stage_desc(P, st, deriv, d);
+  TableNeed need{0, 0, 0, 0};
+  if (launch_stage(d, src, dst, AR_DF, cur_stream(), nullptr, nullptr, nullptr, nullptr, &need) != E_OK || !need.ff)
+    return;
+  *can_in = k != K_R2C;
+  *can_out = k != K_C2R;
+}
+
+// Scale index of an intermediate field of grid g stored by lines along dim A: coordinate
+// multipliers over the two other dims (ascending), 0 along A.
+static void ff_multipliers(const GridDesc &g, int A, long long m[3]) {
+  int d1 = -1, d2 = -1;
+  for (int d = 0; d < 3; d++)
+    if (d != A) (d1 < 0 ? d1 : d2) = d;
+  m[A] = 0;
+  m[d1] = 1;
+  m[d2] = g.gdims[d1];
+}
+
 static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaEvent_t *stage_ev = nullptr) {
   if (g_autotune && !in_capture() && (P->tune.empty() || (P->prec == 8 && P->tuned_arith != arith_mode()))) {
     if (!ensure_device()) return t_err;
@@ -916,16 +1001,17 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   }
   // Page-locked host arrays are read by the first stage and written by the last stage directly
   // over NVLink-C2C, with no staging copy; pageable host arrays are staged through HBM.
-  void *in_mapped = din_dev ? nullptr : mapped_host_ptr(in);
-  void *out_mapped = dout_dev ? nullptr : mapped_host_ptr(out);
-  if (in_mapped && in != out) din = in_mapped;
+  void *in_mapped = (din_dev || !(host_direct_mode() & 1)) ? nullptr : mapped_host_ptr(in);
+  void *out_mapped = (dout_dev || !(host_direct_mode() & 2)) ? nullptr : mapped_host_ptr(out);
+  const bool in_direct = in_mapped && in != out;
+  if (in_direct) din = in_mapped;
   const bool out_direct = out_mapped && in != out;
   if (out_direct) dout = out_mapped;
   const int n = (int)P->ex.size();
   // Host staging overlapped with the first / last stage: the copy of slab c runs on the copy
   // stream while the stage works on slab c-1 (slabs along a dim that is the slowest of the
   // stage's input and output layouts, so each slab is contiguous on both sides).
-  const bool stage_host_in = !din_dev && din == in, stage_host_out = !dout_dev && !out_direct;
+  const bool stage_host_in = !din_dev && !in_direct, stage_host_out = !dout_dev && !out_direct;
   // (only for fields of 32 MB and more: below that, one copy costs less than the extra launches)
   const size_t kSlabMin = 32u << 20;
   const int sd_in = (stage_host_in && in_bytes >= kSlabMin && n >= 2 && !stage_ev && !g_timers_on)
@@ -986,6 +1072,48 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     }
     dst[s] = cand;
   }
+  // float-float links between consecutive specialised float-float stages (not for recorded or
+  // caller-owned scratch sets, slab-pipelined host stages or in-place single-stage calls)
+  std::vector<FFLink> ffl(n);
+  if (ff_intermediates() && n >= 2 && !t_ctx && B.owned && P->prec == 8 && arith_mode() == AR_DF) {
+    std::vector<char> cin(n, 0), cout_(n, 0);
+    const void *qs = din;
+    for (int s = 0; s < n; s++) {
+      const Stage &st = P->ex[s];
+      const bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
+      bool ci = false, co = false;
+      if (dst[s] != qs) stage_ff_capable(P, st, qs, dst[s], deriv, &ci, &co);
+      cin[s] = ci;
+      cout_[s] = co;
+      qs = dst[s];
+    }
+    for (int s = 0; s + 1 < n; s++) {
+      if (!cout_[s] || !cin[s + 1]) continue;
+      const Stage &st = P->ex[s];
+      const int k = s & 1;
+      const size_t bytes = (size_t)(elems(st.g2) / st.g2.gdims[st.dim]) * sizeof(int);
+      if (bytes > B.side_bytes[k] || !B.side[k]) {
+        // no allocation inside a stream capture: this boundary stays IEEE
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (in_capture() || cudaStreamIsCapturing(cur_stream(), &cs) != cudaSuccess ||
+            cs != cudaStreamCaptureStatusNone) {
+          cudaGetLastError();
+          continue;
+        }
+        if (!ensure_buf(&B.side[k], &B.side_bytes[k], bytes)) return E_CUDA;
+      }
+      long long m[3];
+      ff_multipliers(st.g2, st.dim, m);
+      ffl[s].ffout = 1;
+      ffl[s].sout = static_cast<int *>(B.side[k]);
+      ffl[s + 1].ffin = 1;
+      ffl[s + 1].sin = static_cast<const int *>(B.side[k]);
+      for (int i = 0; i < 3; i++) {
+        ffl[s].mo[i] = m[i];
+        ffl[s + 1].mi[i] = m[i];
+      }
+    }
+  }
   const void *src = din;
   int rc = E_OK;
   for (int s = 0; s < n && rc == E_OK; s++) {
@@ -993,10 +1121,11 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     bool deriv = idir >= 0 && st.dim == idir && g_types[st.type].kind != K_EMPTY;
     void *d = dst[s];
     if (stage_ev) cudaEventRecord(stage_ev[s], cur_stream());
+    const FFLink *lk = (ffl[s].ffin || ffl[s].ffout) ? &ffl[s] : nullptr;
     if (s == 0 && sd_in >= 0) {
-      rc = run_stage_slabs(P, st, sd_in, in, din, d, deriv, 0);
+      rc = run_stage_slabs(P, st, sd_in, in, din, d, deriv, 0, lk);
     } else if (s == n - 1 && sd_out >= 0) {
-      rc = run_stage_slabs(P, st, sd_out, out, src, d, deriv, 1);
+      rc = run_stage_slabs(P, st, sd_out, out, src, d, deriv, 1, lk);
     } else if (d == src && t_ctx && t_ctx->rec) {
       set_err(E_UNSUPPORTED, "an in-place single-stage plan cannot be recorded for a grouped launch");
       return E_UNSUPPORTED;
@@ -1011,7 +1140,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
       if (rc == E_OK && cudaMemcpyAsync(d, B.scratch[0], bytes, cudaMemcpyDeviceToDevice, cur_stream()) != cudaSuccess)
         rc = E_CUDA;
     } else {
-      rc = run_stage(P, st, src, d, deriv);
+      rc = run_stage(P, st, src, d, deriv, nullptr, nullptr, -1, lk);
     }
     src = d;
   }
@@ -1284,9 +1413,13 @@ void p3dfft_clear_error(void) {
 }
 void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
-void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on ? 1 : 0; }
+void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on == 1 ? 3 : (on == 2 ? 1 : (on == 3 ? 2 : 0)); }
 void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }
 void p3dfft_gb300_set_reference_compat(int on) { g_ref_compat = on ? 1 : 0; }
+void p3dfft_gb300_set_ff_intermediates(int on) { g_ff_inter = on ? 1 : 0; }
+void p3dfft_gb300_set_fp32_split_twiddles(int on) { set_fp32_split_twiddles(on != 0); }
+int p3dfft_gb300_get_fp32_split_twiddles(void) { return fp32_split_twiddles() ? 1 : 0; }
+int p3dfft_gb300_get_ff_intermediates(void) { return ff_intermediates() ? 1 : 0; }
 int p3dfft_gb300_get_reference_compat(void) { return ref_compat(); }
 int p3dfft_gb300_get_fp64_arith(void) { return arith_mode(); }
 const char *p3dfft_gb300_version(void) { return "p3dfft-gb300 0.1 (sm_103a)"; }

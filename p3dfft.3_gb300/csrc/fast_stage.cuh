@@ -24,6 +24,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "stage_common.cuh"
 
@@ -50,6 +52,15 @@ struct FParams {
   // part g & 1 of complex line g >> 1
   const void *aux;
   int rg_n, rg_a2, rg_b2, rg_sin, rg_half0, rg_half1, rg_cplx;
+  // Float-float intermediate fields (DFP kernels, FK_C2C / FK_R2C out / FK_C2R in).  ffin: the
+  // input holds packed float-float values, each scaled by 2^sin[i] of the line that stored it,
+  // i = j * fi_j + (g % dt) * fi_t + (g / dt) * fi_o for point j of line g.  ffout: store packed
+  // float-float values at this tile's scale and each line's scale at sout[(g % dt) * fo_t +
+  // (g / dt) * fo_o].
+  int ffin, ffout;
+  const int *sin;
+  int *sout;
+  long long fi_j, fi_t, fi_o, fo_t, fo_o;
 };
 
 // resident 256-thread CTAs per SM the register allocation is sized for (FP64 and float-float;
@@ -299,16 +310,16 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
         const typename O::T *pt = ptab + fast_pass_offset(N, I) + jj % Ns;
         if constexpr (O::TW_POWERS) {
           // two table twiddles per butterfly, the others as products of at most two of them
-          C w[8];
+          typename O::W w[8];
           w[1] = fk_tw<O>(pt, 0, sign);
-          if constexpr (R >= 3) w[2] = O::mul(w[1], w[1]);
-          if constexpr (R >= 4) w[3] = O::mul(w[2], w[1]);
-          if constexpr (R == 5) w[4] = O::mul(w[2], w[2]);
+          if constexpr (R >= 3) w[2] = O::wmul(w[1], w[1]);
+          if constexpr (R >= 4) w[3] = O::wmul(w[2], w[1]);
+          if constexpr (R == 5) w[4] = O::wmul(w[2], w[2]);
           if constexpr (R == 8) {
             w[4] = fk_tw<O>(pt, 3 * Ns, sign);
-            w[5] = O::mul(w[4], w[1]);
-            w[6] = O::mul(w[4], w[2]);
-            w[7] = O::mul(w[4], w[3]);
+            w[5] = O::wmul(w[4], w[1]);
+            w[6] = O::wmul(w[4], w[2]);
+            w[7] = O::wmul(w[4], w[3]);
           }
 #pragma unroll
           for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], w[r]);
@@ -385,16 +396,23 @@ __host__ __device__ constexpr int fast_min_blocks() {
                                     : FastShape<N>::MINB;
 }
 
-// A launch over the tiles of several stages that are the same but for their buffers (same
-// kernel, grids, strides and tables) from independent transforms: CTA b works on tile
-// b mod ntotal of stage b / ntotal, whose input and output are io[2j], io[2j+1].
+// A launch over the tiles of several stages of independent transforms that share the kernel
+// (arithmetic, kind, length) and may differ in everything else (buffers, grids, strides, tables):
+// plist holds each stage's parameters, work the (stage, tile) items; CTAs walk the list with a grid
+// stride (k_fast_list).
 struct FGroup {
-  const void *const *io;  // 2 nj buffer addresses (device memory)
-  int nj;
+  const struct FParams *plist;
+  const struct FWork *work;
+  int nwork;
+};
+struct FWork {
+  int stage, tile;
 };
 
-// One tile of one stage (the body of k_fast and k_fast_group).
-template <class O, int KIND, int N>
+// One tile of one stage (the body of k_fast and k_fast_list).
+// FF: float-float intermediate I/O of the DFP kernels, bit 0 input, bit 1 output (FParams ffin /
+// ffout); separate instantiations (fk_ff_variants), so that the IEEE-only kernels carry none of it
+template <class O, int KIND, int N, int FF = 0>
 __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const void *in, void *out) {
   using C = typename O::C;
   using T = typename O::T;
@@ -501,6 +519,14 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
       }
     };
 
+    // float-float input: producer-line scale of point j of this thread's line
+    constexpr bool ffin = O::SCALED && (KIND == FK_C2C || KIND == FK_C2R) && (FF & 1);
+    const long long sib = ffin ? (long long)(gl % p.dt) * p.fi_t + (long long)(gl / p.dt) * p.fi_o : 0;
+    auto sp_of = [&](int j) -> int { return __ldg(p.sin + sib + (long long)j * p.fi_j); };
+    // the scales of this thread's points, loaded with the points and kept in registers for the
+    // conversion (a second load there would put an L2 round trip after the block reduction)
+    int spv[V > 0 ? V : 1] = {};  // per-slot input line scales (float-float input only)
+    int spn = 0;
     C *lb = buf + (size_t)l * LS;
     const int fsign = KIND == FK_C2C ? p.sign : ((KIND == FK_R2C || KIND == FK_R2R1 || KIND == FK_R2RG) ? -1 : 1);
     constexpr RadixList RL = fast_radices(N);
@@ -558,7 +584,12 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         const int sj = fk_slot<PS, TT>(j0, pj0, e);
         const RAW r = load_raw(j0 + e * TT);
         if (O::SCALED) {
-          emax = max(emax, O::rexp(r));
+          if constexpr (ffin) {
+            spv[e] = sp_of(j0 + e * TT);
+            emax = max(emax, O::rexp_ff(r, spv[e]));
+          } else {
+            emax = max(emax, O::rexp(r));
+          }
           lr[sj] = r;
         } else if (KIND == FK_R2RG) {
           lb[sj] = rg_pre(O::from_raw(r, 0), j0 + e * TT);
@@ -569,7 +600,12 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
       if (KIND == FK_C2R && j0 == 0) {
         RAW r = O::ldraw(src + 2 * (long long)N * p.iL);
         if (O::SCALED) {
-          emax = max(emax, O::rexp(r));
+          if constexpr (ffin) {
+            spn = sp_of(N);
+            emax = max(emax, O::rexp_ff(r, spn));
+          } else {
+            emax = max(emax, O::rexp(r));
+          }
           lr[fk_pos<PS>(N)] = r;
         } else {
           lb[fk_pos<PS>(N)] = O::from_raw(r, 0);
@@ -604,8 +640,15 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         __syncthreads();
         int em = 0;
         if (act) {
-          fk_for<V, 1>([&](int e) { em = max(em, O::rexp_finite(lr[fk_slot<PS, TT>(j0, pj0, e)])); });
-          if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_finite(lr[fk_pos<PS>(N)]));
+          if (ffin) {
+            fk_for<V, 1>([&](int e) {
+              em = max(em, O::rexp_ff_finite(lr[fk_slot<PS, TT>(j0, pj0, e)], sp_of(j0 + e * TT)));
+            });
+            if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_ff_finite(lr[fk_pos<PS>(N)], sp_of(N)));
+          } else {
+            fk_for<V, 1>([&](int e) { em = max(em, O::rexp_finite(lr[fk_slot<PS, TT>(j0, pj0, e)])); });
+            if (KIND == FK_C2R && j0 == 0) em = max(em, O::rexp_finite(lr[fk_pos<PS>(N)]));
+          }
         }
         {
           const unsigned grp = __match_any_sync(0xffffffffu, l);
@@ -617,10 +660,11 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         if (act) {
           fk_for<V, 1>([&](int e) {
             const int j = fk_slot<PS, TT>(j0, pj0, e);
-            const C x = O::from_raw_nf(lr[j], sc);
+            const C x = ffin ? O::from_ff(lr[j], sc - sp_of(j0 + e * TT)) : O::from_raw_nf(lr[j], sc);
             lb[j] = KIND == FK_R2RG ? rg_pre(x, j0 + e * TT) : x;
           });
-          if (KIND == FK_C2R && j0 == 0) lb[fk_pos<PS>(N)] = O::from_raw_nf(lr[fk_pos<PS>(N)], sc);
+          if (KIND == FK_C2R && j0 == 0)
+            lb[fk_pos<PS>(N)] = ffin ? O::from_ff(lr[fk_pos<PS>(N)], sc - sp_of(N)) : O::from_raw_nf(lr[fk_pos<PS>(N)], sc);
         }
       } else {
         sc = 1043 - tmax;
@@ -628,10 +672,11 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
           // each thread converts its own slots in place (C2R: and slot N, which thread j0 = 0 loaded)
           fk_for<V, O::IO_UNROLL>([&](int e) {
             const int j = fk_slot<PS, TT>(j0, pj0, e);
-            const C x = O::from_raw(lr[j], sc);
+            const C x = ffin ? O::from_ff(lr[j], sc - spv[e]) : O::from_raw(lr[j], sc);
             lb[j] = KIND == FK_R2RG ? rg_pre(x, j0 + e * TT) : x;
           });
-          if (KIND == FK_C2R && j0 == 0) lb[fk_pos<PS>(N)] = O::from_raw(lr[fk_pos<PS>(N)], sc);
+          if (KIND == FK_C2R && j0 == 0)
+            lb[fk_pos<PS>(N)] = ffin ? O::from_ff(lr[fk_pos<PS>(N)], sc - spn) : O::from_raw(lr[fk_pos<PS>(N)], sc);
         }
       }
     }
@@ -663,13 +708,18 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
       }
       const long long ostride = (KIND == FK_R2RG && p.rg_cplx) ? 2 * p.oL : p.oL;  // FK_R2RG, in reals
       const int pjs = fk_pos<PS>(js), pns = fk_pos<PS>(N - js);
+      // float-float output: values at this line's scale, the scale beside them
+      constexpr bool ffout = O::SCALED && (KIND == FK_C2C || KIND == FK_R2C) && (FF & 2);
+      if (ffout && js == 0) p.sout[(long long)(gs % p.dt) * p.fo_t + (long long)(gs / p.dt) * p.fo_o] = sc_out;
+      auto store_c = [&](G *ptr, C v) {
+        if constexpr (ffout) O::stff(ptr, v);
+        else O::straw(ptr, O::to_raw(v, sc_out));
+      };
       if constexpr (KIND == FK_R2C && V % 2 == 0) {
         // X[k] = 1/2 (s - i t), X[N-k] = 1/2 conj(s + i t), with s = Z_k + conj Z_{N-k} and
         // t = W_2N^k (Z_k - conj Z_{N-k}): each thread unpacks the pairs (k, N-k), k < N/2,
         // k = 0 giving X[0] and X[N]; X[N/2] (its own partner) by the thread with js = 0
-        auto put = [&](int k, C x) {
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
-        };
+        auto put = [&](int k, C x) { store_c(gout + 2 * (obase + (long long)k * p.oL), fk_deriv<O>(p, x, k)); };
         fk_for<V / 2, O::IO_UNROLL>([&](int e) {
           const int k = js + e * TT;
           const C a = Y[fk_slot<PS, TT>(js, pjs, e)];
@@ -688,17 +738,17 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
         const int k = js + e * TT;
         const int sk = fk_slot<PS, TT>(js, pjs, e);
         if (KIND == FK_C2C) {
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, Y[sk], k), sc_out));
+          store_c(gout + 2 * (obase + (long long)k * p.oL), fk_deriv<O>(p, Y[sk], k));
         } else if (KIND == FK_R2C) {
           // X[k] = 1/2 [(Z_k + conj Z_{N-k}) - i W_2N^k (Z_k - conj Z_{N-k})]
           C a = Y[sk], b = O::conj(Y[k == 0 ? 0 : fk_slot_rev<PS, TT, N>(js, pns, e)]);
           C s = O::add(a, b), d = O::sub(a, b);
           C x = O::half(O::sub(s, O::muli(O::mul(d, O::tw(tab, k)))));
-          O::straw(gout + 2 * (obase + (long long)k * p.oL), O::to_raw(fk_deriv<O>(p, x, k), sc_out));
+          store_c(gout + 2 * (obase + (long long)k * p.oL), fk_deriv<O>(p, x, k));
           if (k == 0) {  // X[N] = Re Z_0 - Im Z_0
             C z0 = Y[fk_pos<PS>(0)];
             C xn = O::mk(O::re(O::norm(O::sub(O::mk(O::re(z0), O::rzero()), O::mk(O::im(z0), O::rzero())))), O::rzero());
-            O::straw(gout + 2 * (obase + (long long)N * p.oL), O::to_raw(fk_deriv<O>(p, xn, N), sc_out));
+            store_c(gout + 2 * (obase + (long long)N * p.oL), fk_deriv<O>(p, xn, N));
           }
         } else if (KIND == FK_R2R1) {
           // DCT-I: Y[k], k <= N/2; DST-I: i Y[k+1], k < N/2 - 1
@@ -736,15 +786,38 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   }
 }
 
-template <class O, int KIND, int N>
+template <class O, int KIND, int N, int FF = 0>
 __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast(FParams p) {
-  fk_tile<O, KIND, N>(p, blockIdx.x, p.in, p.out);
+  fk_tile<O, KIND, N, FF>(p, blockIdx.x, p.in, p.out);
 }
 
+// Lengths and kinds with float-float intermediate variants (DFP: C2C in / out / both, R2C out,
+// C2R in; the power-of-two lengths from 64, which carry the large fields)
 template <class O, int KIND, int N>
-__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast_group(FParams p, FGroup g) {
-  const int j = (int)blockIdx.x / p.ntotal;
-  fk_tile<O, KIND, N>(p, (int)blockIdx.x - j * p.ntotal, g.io[2 * j], const_cast<void *>(g.io[2 * j + 1]));
+constexpr bool fk_ff_variants() {
+  return std::is_same_v<O, DFP> && (KIND == FK_C2C || KIND == FK_R2C || KIND == FK_C2R) &&
+         (N == 64 || N == 128 || N == 256 || N == 512 || N == 1024 || N == 2048);
+}
+inline bool fast_ff_length(int n) { return n == 64 || n == 128 || n == 256 || n == 512 || n == 1024 || n == 2048; }
+
+// Work-list launch: item w is tile work[w].tile of the stage whose parameters are
+// plist[work[w].stage]; the parameters are staged in shared memory for the tile.  A grid smaller
+// than the list makes the CTAs persistent (each walks the list with a grid stride).  No CTA waits
+// on another.
+template <class O, int KIND, int N>
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>())
+    k_fast_list(const FParams *plist, const FWork *work, int nwork) {
+  __shared__ FParams sp;
+  constexpr int NW = (int)(sizeof(FParams) / sizeof(int));
+  static_assert(sizeof(FParams) % sizeof(int) == 0, "FParams copied as ints");
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const FWork it = work[w];
+    const int *src = reinterpret_cast<const int *>(plist + it.stage);
+    for (int i = threadIdx.x; i < NW; i += blockDim.x) reinterpret_cast<int *>(&sp)[i] = __ldg(src + i);
+    __syncthreads();
+    fk_tile<O, KIND, N>(sp, it.tile, sp.in, sp.out);
+    __syncthreads();
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -753,7 +826,17 @@ struct FastArgs {
   int kind;  // FastKind
   int n;     // complex FFT length N
   FParams p;
+  int split = 0;  // FP32 only: split-twiddle kernels (NativeFS; table format 2)
 };
+
+template <class O>
+struct is_split_policy : std::false_type {};
+template <bool P>
+struct is_split_policy<NativeFS<P>> : std::true_type {};
+
+// FFT lengths of the FP32 split-twiddle kernels (the long lines)
+#define P3D_FAST_SPLIT_LENGTHS(X) X(512) X(1024) X(2048)
+inline bool fast_split_length(int n) { return n == 512 || n == 1024 || n == 2048; }
 
 template <class O, int KIND, int N>
 constexpr size_t fk_smem() {
@@ -769,9 +852,16 @@ static int fk_configure() {
   if (!configured) {
     if (cudaFuncSetAttribute(k_fast<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)fk_smem<O, KIND, N>()) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fast_group<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_fast_list<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)fk_smem<O, KIND, N>()) != cudaSuccess)
       return E_CUDA;
+    if constexpr (fk_ff_variants<O, KIND, N>()) {
+      const int sm = (int)fk_smem<O, KIND, N>();
+      if (cudaFuncSetAttribute(k_fast<O, KIND, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
+          cudaFuncSetAttribute(k_fast<O, KIND, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
+          cudaFuncSetAttribute(k_fast<O, KIND, N, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+        return E_CUDA;
+    }
     configured = true;
   }
   return E_OK;
@@ -782,22 +872,73 @@ static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t s
   if (fk_configure<O, KIND, N>() != E_OK) return E_CUDA;
   if (g) {
     if (ctas <= 0) return E_OK;
-    k_fast_group<O, KIND, N><<<(unsigned)ctas, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(p, *g);
+    k_fast_list<O, KIND, N><<<(unsigned)ctas, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(g->plist, g->work,
+                                                                                               g->nwork);
   } else {
     if (p.ntotal <= 0) return E_OK;
-    k_fast<O, KIND, N><<<(unsigned)p.ntotal, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(p);
+    const int ff = (p.ffin ? 1 : 0) | (p.ffout ? 2 : 0);
+    const unsigned nb = (unsigned)p.ntotal;
+    constexpr int BL = FastShape<N>::BLOCK;
+    constexpr size_t SM = fk_smem<O, KIND, N>();
+    if constexpr (fk_ff_variants<O, KIND, N>()) {
+      if (ff == 1) k_fast<O, KIND, N, 1><<<nb, BL, SM, st>>>(p);
+      else if (ff == 2) k_fast<O, KIND, N, 2><<<nb, BL, SM, st>>>(p);
+      else if (ff == 3) k_fast<O, KIND, N, 3><<<nb, BL, SM, st>>>(p);
+      else k_fast<O, KIND, N><<<nb, BL, SM, st>>>(p);
+    } else {
+      if (ff) return E_UNSUPPORTED;
+      k_fast<O, KIND, N><<<nb, BL, SM, st>>>(p);
+    }
   }
   return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
 }
 
-// n > 0: launch the length-n kernel (one stage, or a group of stages when g is set);
-// n == 0: configure (load) every length's kernels
-template <class O, int KIND>
+// The float-float kernels are the slowest to compile; their translation units are split in two
+// by length (alternate entries of P3D_FAST_LENGTHS), so that the halves compile in parallel.
+template <class O>
+constexpr int fast_nparts() {
+  return std::is_same_v<O, DFP> ? 2 : 1;
+}
+#define P3D_FAST_ITEM(L) L,
+constexpr int kFastLengths[] = {P3D_FAST_LENGTHS(P3D_FAST_ITEM)};
+#undef P3D_FAST_ITEM
+constexpr int fast_length_index(int n) {
+  for (int i = 0; i < (int)(sizeof(kFastLengths) / sizeof(int)); i++)
+    if (kFastLengths[i] == n) return i;
+  return -1;
+}
+template <class O>
+constexpr int fast_part_of(int n) {
+  return fast_length_index(n) < 0 ? 0 : fast_length_index(n) % fast_nparts<O>();
+}
+
+// Lengths of part PART: n > 0 launches the length-n kernel (one stage, or a group of stages when g
+// is set); n == 0 configures (loads) every length's kernels.
+template <class O, int KIND, int PART>
 static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
-  if (n == 0) {
-    int rc = E_OK;
+  if constexpr (is_split_policy<O>::value) {  // long lines only
+    if (n == 0) {
+      int rc = E_OK;
 #define P3D_FAST_CASE(L) \
   if (fk_configure<O, KIND, L>() != E_OK) rc = E_CUDA;
+      P3D_FAST_SPLIT_LENGTHS(P3D_FAST_CASE)
+#undef P3D_FAST_CASE
+      return rc;
+    }
+#define P3D_FAST_CASE(L) \
+  case L: return fk_launch<O, KIND, L>(p, g, ctas, st);
+    switch (n) {
+      P3D_FAST_SPLIT_LENGTHS(P3D_FAST_CASE)
+      default: return E_UNSUPPORTED;
+    }
+#undef P3D_FAST_CASE
+  }
+  if (n == 0) {
+    int rc = E_OK;
+#define P3D_FAST_CASE(L)                                                      \
+  if constexpr (fast_part_of<O>(L) == PART) {                                 \
+    if (fk_configure<O, KIND, L>() != E_OK) rc = E_CUDA;                      \
+  }
     if constexpr (KIND == FK_R2R1 || KIND == FK_R2RG) {
       P3D_FAST_EVEN_LENGTHS(P3D_FAST_CASE)
     } else {
@@ -806,8 +947,10 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
 #undef P3D_FAST_CASE
     return rc;
   }
-#define P3D_FAST_CASE(L) \
-  case L: return fk_launch<O, KIND, L>(p, g, ctas, st);
+#define P3D_FAST_CASE(L)                                                      \
+  case L:                                                                     \
+    if constexpr (fast_part_of<O>(L) == PART) return fk_launch<O, KIND, L>(p, g, ctas, st); \
+    else return E_UNSUPPORTED;
   if constexpr (KIND == FK_R2R1 || KIND == FK_R2RG) {
     switch (n) {
       P3D_FAST_EVEN_LENGTHS(P3D_FAST_CASE)
@@ -822,28 +965,41 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
 #undef P3D_FAST_CASE
 }
 
-// One (arithmetic, kind) pair per translation unit (fast_inst.cu), so they compile in parallel.
-template <class O, int KIND>
-int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st);
-#define P3D_FAST_DECL(O, K) \
-  template <>               \
-  int fast_launch_kind<O, K>(int, const FParams &, const FGroup *, int, cudaStream_t);
-P3D_FAST_DECL(DFP, FK_C2C)
-P3D_FAST_DECL(DFP, FK_R2C)
-P3D_FAST_DECL(DFP, FK_C2R)
-P3D_FAST_DECL(DFP, FK_R2R1)
-P3D_FAST_DECL(DFP, FK_R2RG)
-P3D_FAST_DECL(Native<double>, FK_C2C)
-P3D_FAST_DECL(Native<double>, FK_R2C)
-P3D_FAST_DECL(Native<double>, FK_C2R)
-P3D_FAST_DECL(Native<double>, FK_R2R1)
-P3D_FAST_DECL(Native<double>, FK_R2RG)
-P3D_FAST_DECL(Native<float>, FK_C2C)
-P3D_FAST_DECL(Native<float>, FK_R2C)
-P3D_FAST_DECL(Native<float>, FK_C2R)
-P3D_FAST_DECL(Native<float>, FK_R2R1)
-P3D_FAST_DECL(Native<float>, FK_R2RG)
+// One (arithmetic, kind, part) per translation unit (fast_inst.cu), so they compile in parallel.
+template <class O, int KIND, int PART>
+int fast_launch_part(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st);
+#define P3D_FAST_DECL(O, K, P) \
+  template <>                  \
+  int fast_launch_part<O, K, P>(int, const FParams &, const FGroup *, int, cudaStream_t);
+#define P3D_FAST_DECL_KINDS(O, P) \
+  P3D_FAST_DECL(O, FK_C2C, P)     \
+  P3D_FAST_DECL(O, FK_R2C, P)     \
+  P3D_FAST_DECL(O, FK_C2R, P)     \
+  P3D_FAST_DECL(O, FK_R2R1, P)    \
+  P3D_FAST_DECL(O, FK_R2RG, P)
+P3D_FAST_DECL_KINDS(DFP, 0)
+P3D_FAST_DECL_KINDS(DFP, 1)
+P3D_FAST_DECL_KINDS(Native<double>, 0)
+P3D_FAST_DECL_KINDS(Native<float>, 0)
+P3D_FAST_DECL_KINDS(NativeFS<false>, 0)
+#undef P3D_FAST_DECL_KINDS
 #undef P3D_FAST_DECL
+
+template <class O, int KIND>
+inline int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
+  if constexpr (fast_nparts<O>() == 1) {
+    return fast_launch_part<O, KIND, 0>(n, p, g, ctas, st);
+  } else {
+    static_assert(fast_nparts<O>() == 2, "two parts");
+    if (n == 0) {
+      const int r0 = fast_launch_part<O, KIND, 0>(0, p, g, ctas, st);
+      const int r1 = fast_launch_part<O, KIND, 1>(0, p, g, ctas, st);
+      return r0 != E_OK ? r0 : r1;
+    }
+    return fast_part_of<O>(n) == 0 ? fast_launch_part<O, KIND, 0>(n, p, g, ctas, st)
+                                   : fast_launch_part<O, KIND, 1>(n, p, g, ctas, st);
+  }
+}
 
 template <class O>
 inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaStream_t st) {
@@ -865,8 +1021,11 @@ inline int fast_preload(int prec, int arith) {
     a.kind = k;
     a.n = 0;
     int r;
-    if (prec == 4) r = fast_launch_arith<Native<float>>(a, nullptr, 0, 0);
-    else if (arith == AR_DF) r = fast_launch_arith<DFP>(a, nullptr, 0, 0);
+    if (prec == 4) {
+      r = fast_launch_arith<Native<float>>(a, nullptr, 0, 0);
+      const int r2 = fast_launch_arith<NativeFS<false>>(a, nullptr, 0, 0);
+      if (r2 != E_OK) r = r2;
+    } else if (arith == AR_DF) r = fast_launch_arith<DFP>(a, nullptr, 0, 0);
     else r = fast_launch_arith<Native<double>>(a, nullptr, 0, 0);
     if (r != E_OK) rc = r;
   }
@@ -877,7 +1036,10 @@ inline int fast_preload(int prec, int arith) {
 // `ctas` CTAs covers the group of stages g describes (a.kind and a.n select the kernel).
 inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, const FGroup *g = nullptr,
                        int ctas = 0) {
-  if (prec == 4) return fast_launch_arith<Native<float>>(a, g, ctas, st);
+  if (prec == 4) {
+    if (a.split) return fast_launch_arith<NativeFS<false>>(a, g, ctas, st);
+    return fast_launch_arith<Native<float>>(a, g, ctas, st);
+  }
   if (arith == AR_DF) return fast_launch_arith<DFP>(a, g, ctas, st);
   return fast_launch_arith<Native<double>>(a, g, ctas, st);
 }

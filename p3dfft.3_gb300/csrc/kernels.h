@@ -47,6 +47,15 @@ struct StageDesc {
   // talt 1 takes consecutive lines of a tile along the other batch dim
   int engine = 0;
   int talt = 0;
+  // Float-float intermediate fields (float-float arithmetic, specialised C2C / R2C / C2R kernels
+  // only; other launches with these set fail with E_UNSUPPORTED).  ffin: the input field holds
+  // packed float-float values scaled per stored line; the scale of the value at logical
+  // coordinates c is sin[sum_d c[d] * mi[d]].  ffout: store packed float-float values and each
+  // line's scale at sout[sum_d c[d] * mo[d]] (mi / mo: 0 along the storing line's own dim).
+  int ffin = 0, ffout = 0;
+  const int *sin = nullptr;
+  int *sout = nullptr;
+  long long mi[3] = {0, 0, 0}, mo[3] = {0, 0, 0};
 };
 enum Engine { ENG_AUTO = 0, ENG_FAST = 1, ENG_FIXED = 2, ENG_GENERIC = 3, ENG_BLUESTEIN = 4 };
 
@@ -61,6 +70,7 @@ int preload_kernels();
 struct TableNeed {
   int fmt, tabN, auxN;
   int aux_pass;  // 1: the aux table is the specialised kernels' per-pass twiddle rows of length auxN
+  int ff = 0;    // the stage's kernel can read / write float-float intermediate fields
 };
 size_t table_bytes(int N, int fmt);
 void fill_table(int N, int fmt, void *host_dst);
@@ -93,14 +103,21 @@ struct StageLaunch {
 // levels[k] holds the k-th stage of every transform of a set (e.g. a batch cohort).  A launch set
 // runs level after level on one stream; within a level, stages that differ only in their buffers
 // and run on a specialised kernel become one grouped launch over all their tiles, the others one
-// launch each.  Building uploads the groups' buffer addresses.
+// launch each.  With work_list, stages that run the same specialised kernel (arithmetic, kind,
+// length) become one grouped launch even when their grids, strides and tables differ.  A grouped
+// launch is one k_fast_list launch over the members' (stage, tile) items
+// (P3DFFT_GB300_LIST_PERSISTENT=1 caps its grid at the resident CTAs, which then walk the list).
+// Building uploads the groups' parameters and items.
 struct LaunchSet;
-LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err);
+LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err,
+                            bool work_list = false);
 int launch_set_run(LaunchSet *set, cudaStream_t stream, int *kernels_launched);
 // the launches of level l, largest first (items 0 .. launch_set_items(set, l) - 1)
 int launch_set_levels(const LaunchSet *set);
 int launch_set_items(const LaunchSet *set, int level);
 int launch_set_run_item(LaunchSet *set, int level, int item, cudaStream_t stream, int *kernels_launched);
+// positions in levels[level] of the stages that item `item` runs
+const std::vector<int> &launch_set_item_members(const LaunchSet *set, int level, int item);
 int launch_set_groups(const LaunchSet *set);
 void launch_set_destroy(LaunchSet *set);
 // Pure permutation copy of an element size `esize` bytes field (EMPTY stages).
@@ -109,6 +126,10 @@ int launch_permute(const int d[3], const long long s1[3], const long long s2[3],
 // Standalone spectral derivative on a complex field (build/deriv.C:85-184), in may equal out.
 // ref_axis: differentiate along storage axis imo[idir] as build/deriv.C:89-93 does (else along
 // the storage axis of logical dim idir); the wavenumbers come from g in both cases
+// FP32 specialised kernels on lines of 512, 1024 and 2048 points use split (compensated)
+// twiddle products when on (the default)
+bool fp32_split_twiddles();
+void set_fp32_split_twiddles(bool on);
 int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, int ref_axis, const void *in,
                  void *out, cudaStream_t stream, int *kernels_launched);
 

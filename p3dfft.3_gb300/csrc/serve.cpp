@@ -57,6 +57,7 @@ struct SJob {
   void *d_in = nullptr, *d_spec = nullptr, *d_s0 = nullptr, *d_s1 = nullptr;
   void *set = nullptr;
   int err = E_OK;
+  bool inject_alloc_failure = false;  // test hook: its device allocation fails at launch
 };
 
 struct Server {
@@ -126,8 +127,8 @@ static int launch_job(Server *S, SJob *j) {
   auto alloc = [&](void **p, size_t b) {
     return cudaMallocFromPoolAsync(p, std::max<size_t>(b, 256), S->pool, st) == cudaSuccess;
   };
-  if (!alloc(&j->d_in, j->in_bytes) || !alloc(&j->d_spec, j->spec_bytes) || !alloc(&j->d_s0, j->scratch_bytes) ||
-      !alloc(&j->d_s1, j->scratch_bytes)) {
+  if (j->inject_alloc_failure || !alloc(&j->d_in, j->in_bytes) || !alloc(&j->d_spec, j->spec_bytes) ||
+      !alloc(&j->d_s0, j->scratch_bytes) || !alloc(&j->d_s1, j->scratch_bytes)) {
     cudaGetLastError();
     return E_CUDA;
   }
@@ -359,6 +360,22 @@ int p3dfft_gb300_server_submit(int srv, int plan_fwd, int plan_bwd, int idir, co
   }
   S->cv.notify_all();
   return j->id;
+}
+
+int p3dfft_gb300_server_inject_alloc_failure(int srv, int job) {
+  Server *S = get_server(srv);
+  if (!S) {
+    record_error(E_BAD_ARG, "server: invalid handle");
+    return E_BAD_ARG;
+  }
+  std::lock_guard<std::mutex> g(S->mu);
+  if (job < 0 || job >= (int)S->jobs.size() || S->jobs[job]->state == J_RUNNING || S->jobs[job]->state == J_DONE ||
+      S->jobs[job]->state == J_FAILED) {
+    record_error(E_BAD_ARG, "server: the job is not waiting for admission");
+    return E_BAD_ARG;
+  }
+  S->jobs[job]->inject_alloc_failure = true;
+  return E_OK;
 }
 
 // 0 done, 1 not yet (timeout), negative: the job failed with that error code negated

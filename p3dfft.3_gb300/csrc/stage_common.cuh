@@ -105,6 +105,8 @@ struct Native {
   // FP32: build most pass twiddles as products of two table entries (fewer loads through L1,
   // the FP32 kernels' bottleneck; at most two roundings more per twiddle)
   static constexpr bool TW_POWERS = sizeof(R) == 4 && FAST_TW_POWERS_FP32;
+  // product of two twiddles (twiddle powers formed in registers)
+  static __device__ __forceinline__ C wmul(C a, C b) { return mul(a, b); }
   using RAW = cx<R>;
   static __device__ __forceinline__ RAW ldraw(const G *p) { return ldg_c(reinterpret_cast<const cx<R> *>(p)); }
   static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {
@@ -138,6 +140,40 @@ struct Native {
     r.y = -r.y;
     return r;
   }
+  // float-float intermediate fields exist only for the float-float kernels (DFP)
+  static __device__ __forceinline__ int rexp_ff(RAW, int) { return 0; }
+  static __device__ __forceinline__ int rexp_ff_finite(RAW, int) { return 0; }
+  static __device__ __forceinline__ C from_ff(RAW r, int) { return mk(r.x, r.y); }
+  static __device__ __forceinline__ void stff(G *p, C v) { straw(p, to_raw(v, 0)); }
+};
+
+// FP32 data with split twiddles (the specialised kernels on long lines): each twiddle is the pair
+// (hi, lo) of FP32 values whose sum is its long-double value to ~48 bits (table format 2), and a
+// product a * w is formed as a * hi + (a * lo), the small term first, so the twiddle adds no
+// rounding of its own beyond that of the product ("compensated" twiddle products).  POW = false
+// (the one instantiated): every twiddle is read from the tables; POW = true forms the powers as
+// float-float products of two loaded twiddles instead, which measured 20% slower at 512 points
+// (register spills at the FP32 kernels' 32-register budget) against 10% for the loads.
+template <bool POW>
+struct NativeFS : Native<float> {
+  using T = cff;
+  using W = cff;
+  using Native<float>::conj;
+  using Native<float>::mul;
+  static __device__ __forceinline__ W tw(const T *t, int k) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(t + k));
+    return W{ff{v.x, v.y}, ff{v.z, v.w}};
+  }
+  static __device__ __forceinline__ W conj(const W &w) { return W{w.x, ff{-w.y.hi, -w.y.lo}}; }
+  static __device__ __forceinline__ C mul(C a, const W &w) {
+    const float cr = __fmaf_rn(a.x, w.x.lo, -a.y * w.y.lo);
+    const float ci = __fmaf_rn(a.x, w.y.lo, a.y * w.x.lo);
+    return mk(__fmaf_rn(a.x, w.x.hi, __fmaf_rn(-a.y, w.y.hi, cr)), __fmaf_rn(a.x, w.y.hi, __fmaf_rn(a.y, w.x.hi, ci)));
+  }
+  static __device__ __forceinline__ S wre(const W &w) { return w.x.hi; }
+  static __device__ __forceinline__ S wim(const W &w) { return w.y.hi; }
+  static constexpr bool TW_POWERS = POW;
+  static __device__ __forceinline__ W wmul(const W &a, const W &b) { return cff_mul(a, b); }
 };
 
 // float-float arithmetic for FP64 data (see df_arith.cuh), scalar form: the generic engines
@@ -300,6 +336,35 @@ struct DFP {
     r.y ^= (long long)0x8000000000000000ull;
     return r;
   }
+  // Float-float intermediate fields: a complex element is its packed value (hi.x, hi.y, lo.x,
+  // lo.y as four floats, the 16 bytes of a complex double) scaled by 2^sp, sp the scale of the
+  // line that stored it.  rexp_ff gives the biased double exponent the value stands for (0 for
+  // zero, 0x7ff for an infinity or NaN); from_ff rescales by 2^d, d = consumer scale - sp (the
+  // clamp only matters for values far below every line maximum, which flush as in from_raw).
+  static __device__ __forceinline__ unsigned ff_hexp(RAW r, int part) {
+    const unsigned u = part ? (unsigned)((unsigned long long)r.x >> 32) : (unsigned)r.x;
+    return (u >> 23) & 0xffu;
+  }
+  static __device__ __forceinline__ int rexp_ff(RAW r, int sp) {
+    const unsigned fx = ff_hexp(r, 0), fy = ff_hexp(r, 1);
+    const unsigned fm = fx > fy ? fx : fy;
+    if (fm == 0xffu) return 0x7ff;
+    return fm ? (int)fm + 896 - sp : 0;
+  }
+  static __device__ __forceinline__ int rexp_ff_finite(RAW r, int sp) {
+    unsigned fx = ff_hexp(r, 0), fy = ff_hexp(r, 1);
+    fx = fx == 0xffu ? 0u : fx;
+    fy = fy == 0xffu ? 0u : fy;
+    const unsigned fm = fx > fy ? fx : fy;
+    return fm ? (int)fm + 896 - sp : 0;
+  }
+  static __device__ __forceinline__ C from_ff(RAW r, int d) {
+    d = d < -126 ? -126 : (d > 127 ? 127 : d);
+    const float2 f = f2dup(__int_as_float((d + 127) << 23));
+    const C v = *reinterpret_cast<const C *>(&r);
+    return C{f2mul(v.hi, f), f2mul(v.lo, f)};
+  }
+  static __device__ __forceinline__ void stff(G *p, C v) { *reinterpret_cast<C *>(p) = pcf_norm(v); }
 };
 
 

@@ -749,6 +749,17 @@ static int factorize(int n, int *rad, int cap) {
 
 int max_line_len(int prec) { return prec == 8 ? 6144 : 12288; }
 
+// FP32 split twiddles on the long lines (P3DFFT_GB300_FP32_SPLIT_TWIDDLES=0 turns them off)
+static int g_fp32_split = -1;
+bool fp32_split_twiddles() {
+  if (g_fp32_split < 0) {
+    const char *e = getenv("P3DFFT_GB300_FP32_SPLIT_TWIDDLES");
+    g_fp32_split = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_fp32_split == 1;
+}
+void set_fp32_split_twiddles(bool on) { g_fp32_split = on ? 1 : 0; }
+
 template <class O, class E>
 static int launch_k(const KParams &p, size_t smem, int grid, int threads, cudaStream_t st) {
   static int configured_smem = 0;  // per instantiation
@@ -908,10 +919,16 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
                         bM <= (d.prec == 4 ? 4096 : 2048);
   if (d.engine == ENG_BLUESTEIN && !use_blue) return E_UNSUPPORTED;
 
+  // FP32 specialised kernels on long lines: split (compensated) twiddle products, tables in
+  // float-float pairs (format 2)
+  const bool split = d.prec == 4 && use_fast && fp32_split_twiddles() && fast_split_length(p.nfft);
   // float-float tables: packed product form for the specialised kernels
-  const int fmt = d.prec == 4 ? 1 : (arith == AR_DF ? (use_fast ? 3 : 2) : 0);
+  const int fmt = d.prec == 4 ? (split ? 2 : 1) : (arith == AR_DF ? (use_fast ? 3 : 2) : 0);
   if (tabs_out) {  // caller supplies the tables: report what is needed, launch nothing
     tabs_out->fmt = fmt;
+    // the specialised float-float kernel of this length has float-float intermediate variants
+    tabs_out->ff = (use_fast && d.prec == 8 && arith == AR_DF && !r2r1 && !r2rg && fast_ff_length(p.nfft) &&
+                    (d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || d.kind == K_R2C || d.kind == K_C2R)) ? 1 : 0;
     tabs_out->tabN = tabN;
     tabs_out->auxN = use_fast ? p.nfft : ((d.kind == K_R2R && p.r2r_np > 0) ? 8 * p.r2r_np : 0);
     tabs_out->aux_pass = use_fast ? 1 : 0;
@@ -962,9 +979,16 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   p.dother = d.d1[o];
 
   if (!aligned && (p.in_complex || p.out_complex)) return E_ALIGN;
+  // float-float intermediates: only the specialised float-float C2C / R2C (out) / C2R (in) kernels
+  if ((d.ffin || d.ffout) &&
+      (!use_fast || arith != AR_DF || d.prec != 8 || r2r1 || r2rg || fast_prep || !fast_ff_length(p.nfft) ||
+       (d.ffin && d.kind == K_R2C) ||
+       (d.ffout && d.kind == K_C2R) || !(d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || d.kind == K_R2C || d.kind == K_C2R)))
+    return E_UNSUPPORTED;
 
   if (use_fast) {
     FastArgs fa;
+    fa.split = split ? 1 : 0;
     fa.kind = (r2r1 || r2rg) ? fkind : ((d.kind == K_R2C) ? FK_R2C : (d.kind == K_C2R ? FK_C2R : FK_C2C));
     fa.n = p.nfft;
     FParams &q = fa.p;
@@ -1007,6 +1031,15 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.dmid = p.dmid;
     q.load_Lmajor = p.load_Lmajor;
     q.store_Lmajor = p.store_Lmajor;
+    q.ffin = d.ffin;
+    q.ffout = d.ffout;
+    q.sin = d.sin;
+    q.sout = d.sout;
+    q.fi_j = d.mi[L];
+    q.fi_t = d.mi[t];
+    q.fi_o = d.mi[o];
+    q.fo_t = d.mo[t];
+    q.fo_o = d.mo[o];
     if (fast_prep) {
       *fast_prep = fa;
       return E_OK;
@@ -1090,17 +1123,23 @@ static int permute_t(const int d[3], const long long s1[3], const long long s2[3
 struct LaunchItem {
   int group;  // >= 0: member of group `group`; -1: launched alone
   StageLaunch st;
+  std::vector<int> members;  // positions in the level's input list that this launch runs
 };
 struct LaunchGroupInfo {
-  FastArgs fa;  // the first member's launch; the members differ only in their buffers
+  FastArgs fa;  // the first member's launch (kernel selection)
   int prec, arith;
-  int first, count;  // buffer pairs [first, first + count)
+  int count;  // members
+  // the members' parameters [pfirst, pfirst + count) and (member, tile) items
+  // [wfirst, wfirst + nwork) in the set's device arrays
+  int pfirst = 0, wfirst = 0, nwork = 0;
 };
 struct LaunchSet {
   std::vector<std::vector<LaunchItem>> levels;
   std::vector<LaunchGroupInfo> groups;
-  void **dev_io = nullptr;  // 2 addresses per group member
+  FParams *dev_params = nullptr;  // every group's members' parameters
+  FWork *dev_work = nullptr;      // and (member, tile) items
   DeviceTables *tabs = nullptr;
+  bool persistent = false;  // work-list launches with at most (SMs x resident CTAs) CTAs
 };
 
 // everything of a specialised launch but its buffers
@@ -1112,22 +1151,39 @@ static std::vector<long long> fast_key(const StageLaunch &st, const FastArgs &fa
           (long long)(uintptr_t)q.aux, q.rg_n, q.rg_a2, q.rg_b2, q.rg_sin, q.rg_half0, q.rg_half1, q.rg_cplx};
 }
 
-LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err) {
+// the kernel a specialised launch runs: arithmetic, kind, length, twiddle form
+static std::vector<long long> kernel_key(const StageLaunch &st, const FastArgs &fa) {
+  return {st.d.prec, st.d.prec == 8 ? st.arith : 0, fa.kind, fa.n, fa.split};
+}
+
+LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err,
+                            bool work_list) {
   LaunchSet *S = new LaunchSet();
   S->tabs = tabs;
-  std::vector<void *> io;
+  {
+    const char *e = getenv("P3DFFT_GB300_LIST_PERSISTENT");
+    S->persistent = e && e[0] == '1';
+  }
+  std::vector<FParams> params;
+  std::vector<FWork> work;
   for (const auto &lv : levels) {
     std::vector<LaunchItem> items;
-    std::map<std::vector<long long>, std::vector<std::pair<FastArgs, StageLaunch>>> by_kernel;
-    for (const auto &st : lv) {
+    struct Member {
+      FastArgs fa;
+      StageLaunch st;
+      int pos;
+    };
+    std::map<std::vector<long long>, std::vector<Member>> by_kernel;
+    for (size_t pos = 0; pos < lv.size(); pos++) {
+      const StageLaunch &st = lv[pos];
       FastArgs fa;
       int rc = E_UNSUPPORTED;
       if (st.d.kind != K_EMPTY)
         rc = launch_stage(st.d, st.src, st.dst, st.arith, 0, tabs, nullptr, nullptr, nullptr, nullptr, &fa);
       if (rc == E_OK && fa.p.ntotal > 0) {
-        by_kernel[fast_key(st, fa)].push_back({fa, st});
+        by_kernel[work_list ? kernel_key(st, fa) : fast_key(st, fa)].push_back({fa, st, (int)pos});
       } else if (rc == E_OK || rc == E_UNSUPPORTED) {
-        items.push_back({-1, st});
+        items.push_back({-1, st, {(int)pos}});
       } else {
         *err = rc;
         delete S;
@@ -1136,20 +1192,25 @@ LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels,
     }
     for (auto &kv : by_kernel) {
       if (kv.second.size() == 1) {  // nothing to group
-        items.push_back({-1, kv.second[0].second});
+        items.push_back({-1, kv.second[0].st, {kv.second[0].pos}});
         continue;
       }
       LaunchGroupInfo g;
-      g.fa = kv.second[0].first;
+      g.fa = kv.second[0].fa;
       g.prec = (int)kv.first[0];
       g.arith = (int)kv.first[1];
-      g.first = (int)io.size() / 2;
       g.count = (int)kv.second.size();
+      g.pfirst = (int)params.size();
+      g.wfirst = (int)work.size();
+      std::vector<int> members;
       for (auto &m : kv.second) {
-        io.push_back(const_cast<void *>(m.first.p.in));
-        io.push_back(m.first.p.out);
+        const int member = (int)params.size() - g.pfirst;
+        params.push_back(m.fa.p);
+        for (int t = 0; t < m.fa.p.ntotal; t++) work.push_back({member, t});
+        members.push_back(m.pos);
       }
-      items.push_back({(int)S->groups.size(), kv.second[0].second});
+      g.nwork = (int)work.size() - g.wfirst;
+      items.push_back({(int)S->groups.size(), kv.second[0].st, members});
       S->groups.push_back(g);
     }
     // largest launches first, so that concurrent streams finish together
@@ -1162,14 +1223,14 @@ LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels,
                      [&](const LaunchItem &a, const LaunchItem &b) { return work(a) > work(b); });
     S->levels.push_back(items);
   }
-  if (!io.empty()) {
-    const size_t bytes = io.size() * sizeof(void *);
-    if (cudaMalloc(&S->dev_io, bytes) != cudaSuccess ||
-        cudaMemcpy(S->dev_io, io.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (!params.empty()) {
+    const size_t pb = params.size() * sizeof(FParams), wb = work.size() * sizeof(FWork);
+    if (cudaMalloc(&S->dev_params, pb) != cudaSuccess || cudaMalloc(&S->dev_work, wb) != cudaSuccess ||
+        cudaMemcpy(S->dev_params, params.data(), pb, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(S->dev_work, work.data(), wb, cudaMemcpyHostToDevice) != cudaSuccess) {
       cudaGetLastError();
-      if (S->dev_io) cudaFree(S->dev_io);
+      launch_set_destroy(S);
       *err = E_CUDA;
-      delete S;
       return nullptr;
     }
   }
@@ -1192,14 +1253,21 @@ int launch_set_items(const LaunchSet *S, int l) { return (int)S->levels[l].size(
 int launch_set_run_item(LaunchSet *S, int l, int i, cudaStream_t st, int *kernels) {
   return run_launch_item(S, S->levels[l][i], st, kernels);
 }
+const std::vector<int> &launch_set_item_members(const LaunchSet *S, int l, int i) { return S->levels[l][i].members; }
 
 static int run_launch_item(LaunchSet *S, const LaunchItem &it, cudaStream_t st, int *kernels) {
   if (it.group >= 0) {
     const LaunchGroupInfo &g = S->groups[it.group];
     FGroup fg;
-    fg.io = S->dev_io + 2 * (size_t)g.first;
-    fg.nj = g.count;
-    const long long ctas = (long long)g.count * g.fa.p.ntotal;
+    fg.plist = S->dev_params + g.pfirst;
+    fg.work = S->dev_work + g.wfirst;
+    fg.nwork = g.nwork;
+    long long ctas = g.nwork;
+    if (S->persistent) {
+      static int nsm = 0;
+      if (!nsm) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0);
+      ctas = std::min<long long>(ctas, (long long)std::max(nsm, 1) * (g.prec == 8 ? 4 : 8));
+    }
     if (ctas > 0x7fffffffLL) return E_TOO_LARGE;
     const int rc = launch_fast(g.prec, g.arith, g.fa, st, &fg, (int)ctas);
     if (rc == E_OK && kernels) (*kernels)++;
@@ -1220,7 +1288,8 @@ int launch_set_groups(const LaunchSet *S) { return (int)S->groups.size(); }
 
 void launch_set_destroy(LaunchSet *S) {
   if (!S) return;
-  if (S->dev_io) cudaFree(S->dev_io);
+  if (S->dev_params) cudaFree(S->dev_params);
+  if (S->dev_work) cudaFree(S->dev_work);
   delete S;
 }
 

@@ -64,6 +64,10 @@ def lib():
         "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
         "p3dfft_gb300_set_reference_compat": ([ctypes.c_int], None),
         "p3dfft_gb300_get_reference_compat": ([], ctypes.c_int),
+        "p3dfft_gb300_set_ff_intermediates": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_ff_intermediates": ([], ctypes.c_int),
+        "p3dfft_gb300_set_fp32_split_twiddles": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_fp32_split_twiddles": ([], ctypes.c_int),
         "p3dfft_gb300_plan3d": ([ip, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_exec3d": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_destroy3d": ([ctypes.c_int], ctypes.c_int),
@@ -110,6 +114,7 @@ def lib():
         "p3dfft_gb300_server_submit": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp,
                                         ctypes.c_double], ctypes.c_int),
         "p3dfft_gb300_server_wait": ([ctypes.c_int, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+        "p3dfft_gb300_server_inject_alloc_failure": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_server_drain": ([ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_server_clock": ([ctypes.c_int], ctypes.c_double),
         "p3dfft_gb300_server_job_times": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
@@ -157,6 +162,18 @@ def set_reference_compat(on: bool):
     lib().p3dfft_gb300_set_reference_compat(1 if on else 0)
 
 
+def set_ff_intermediates(on: bool):
+    """Float-float FP64 stages pass intermediate fields as scaled float-float pairs (True, the
+    default) or as IEEE doubles (False)."""
+    lib().p3dfft_gb300_set_ff_intermediates(1 if on else 0)
+
+
+def set_fp32_split_twiddles(on: bool):
+    """FP32 stages of FFT length 512-2048 use split (compensated) twiddle products (True, the
+    default) or plain FP32 twiddles (False)."""
+    lib().p3dfft_gb300_set_fp32_split_twiddles(1 if on else 0)
+
+
 def get_reference_compat() -> bool:
     return bool(lib().p3dfft_gb300_get_reference_compat())
 
@@ -165,9 +182,11 @@ def set_sync(sync: bool):
     lib().p3dfft_gb300_set_sync(1 if sync else 0)
 
 
-def set_host_direct(on: bool):
-    """Page-locked host arrays read / written by the kernels over NVLink-C2C (True) or staged."""
-    lib().p3dfft_gb300_set_host_direct(1 if on else 0)
+def set_host_direct(on):
+    """Page-locked host arrays read / written by the kernels over NVLink-C2C (True, or "in" /
+    "out" for one side only) or staged through HBM (False)."""
+    mode = {True: 1, False: 0, "in": 2, "out": 3}[on]
+    lib().p3dfft_gb300_set_host_direct(mode)
 
 
 def set_stream(stream_ptr: int):
@@ -389,8 +408,9 @@ class Batch:
         self._keep = []
         if not graph:
             check(lib().p3dfft_gb300_batch_set_graph(h, 0))
-        if not grouped:
-            check(lib().p3dfft_gb300_batch_set_grouped(h, 0))
+        if grouped != 1:
+            # False/0: branch streams; "list"/2: one work-list launch per kernel per level
+            check(lib().p3dfft_gb300_batch_set_grouped(h, 2 if grouped in ("list", 2) else 0))
 
     def groups(self):
         return int(lib().p3dfft_gb300_batch_groups(self.handle))
@@ -448,6 +468,10 @@ class Server:
         if rc < 0:
             raise P3DFFTError(f"job {job} failed: {ERR_NAMES.get(-rc, -rc)}")
         return rc == 0
+
+    def inject_alloc_failure(self, job):
+        """Test hook: the job's device allocation fails at admission (it must still be waiting)."""
+        check(lib().p3dfft_gb300_server_inject_alloc_failure(self.handle, int(job)))
 
     def drain(self):
         rc = lib().p3dfft_gb300_server_drain(self.handle)

@@ -1,8 +1,8 @@
 """GPU: batched execution of independent R2C -> C2R round trips (p3dfft_gb300_batch_*).
 
 Every job's forward spectrum and round trip must be bit-identical to the same plan run alone
-through p3dfft_gb300_exec3d (the batch runs the same kernels, only concurrently and from a CUDA
-graph), and the forward spectra must match the FP64 oracle (1e-12 for FP64 jobs, 1e-6 for FP32)."""
+through p3dfft_gb300_exec3d with IEEE-double intermediate fields (the batch runs the same kernels,
+only concurrently and from a CUDA graph), and the forward spectra must match the FP64 oracle (1e-12 for FP64 jobs, 1e-6 for FP32)."""
 import numpy as np
 import pytest
 
@@ -28,6 +28,7 @@ def _plans(p3d, gd, prec):
 
 class Job:
     def __init__(self, p3d, gd, prec, seed, idir=-1):
+        self.p3d = p3d
         self.gd, self.prec, self.idir = gd, prec, idir
         self.f, self.b = _plans(p3d, gd, prec)
         rdt = np.float64 if prec == 8 else np.float32
@@ -47,8 +48,14 @@ class Job:
         return self.d_s.download(np.empty_like(self.spec)), self.d_y.download(np.empty_like(self.back))
 
     def alone(self):
-        self.f.exec(self.d_x, self.d_s, idir=self.idir)
-        self.b.exec(self.d_s, self.d_y)
+        # batches pass IEEE-double intermediate fields between stages (float-float intermediates
+        # are a plain-exec optimisation); the alone run does the same, so results compare bit for bit
+        self.p3d.set_ff_intermediates(False)
+        try:
+            self.f.exec(self.d_x, self.d_s, idir=self.idir)
+            self.b.exec(self.d_s, self.d_y)
+        finally:
+            self.p3d.set_ff_intermediates(True)
         return self.download()
 
 
@@ -148,3 +155,38 @@ def test_batch_rejects_host_pointers(gpu):
     batch = p3d.Batch()
     with pytest.raises(p3d.P3DFFTError, match="device pointers"):
         batch.add(0, f, x, y)
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_work_list_batch_merges_uneven_jobs(gpu, oracle, persistent, monkeypatch):
+    """Work-list mode: each stage level runs one launch per kernel (arithmetic, kind, FFT length)
+    over the tiles of every job that needs it, whatever the jobs' grids, so uneven jobs that share a
+    line length share a launch; with persistent CTAs the grid is capped at the resident CTAs, which
+    walk the (stage, tile) list.  Results are bit-identical to each job run alone."""
+    p3d = gpu
+    p3d.set_fp64_arith(1)
+    monkeypatch.setenv("P3DFFT_GB300_LIST_PERSISTENT", "1" if persistent else "0")
+    shapes = [(64, 32, 48), (64, 48, 32), (32, 64, 40), (48, 64, 64), (64, 64, 64), (40, 32, 64)]
+    jobs = [Job(p3d, gd, prec, seed=300 + i) for i, gd in enumerate(shapes) for prec in (8, 4)]
+    alone = [j.alone() for j in jobs]
+    for j in jobs:
+        j.d_s.upload(np.zeros_like(j.spec))
+        j.d_y.upload(np.zeros_like(j.back))
+    batch = p3d.Batch(nbranches=4, graph=True, grouped="list")
+    for i, j in enumerate(jobs):
+        j.add_to(batch, i)
+    batch.exec()
+    stages = sum(len(j.f.stages()) + len(j.b.stages()) for j in jobs)
+    assert 0 < batch.groups() and batch.kernels() <= 0.75 * stages, (batch.kernels(), stages)
+    for j, (s0, y0) in zip(jobs, alone):
+        s, y = j.download()
+        assert np.array_equal(s, s0) and np.array_equal(y, y0), (j.gd, j.prec)
+    for i, j in enumerate(jobs):  # graph replay on new inputs
+        j.x = seeded_field(j.x.shape, 700 + i).astype(j.x.dtype)
+        j.d_x.upload(j.x)
+    batch.exec()
+    for j in jobs:
+        s, _ = j.download()
+        ref = oracle.OraclePlan(j.f.types if j.prec == 8 else _d_types(p3d, j.f.types), j.gd, (0, 1, 2),
+                                (j.gd[0] // 2 + 1, j.gd[1], j.gd[2]), (1, 2, 0), -1, 0).exec(j.x.astype(np.float64))
+        assert rel_l2(s, ref) < (1e-12 if j.prec == 8 else 1e-6), (j.gd, j.prec)

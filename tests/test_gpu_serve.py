@@ -134,3 +134,45 @@ def test_serve_device_resident_fields(gpu):
     y = d_out.download(np.empty_like(j.x))
     assert np.array_equal(y, j.result())
     srv.close()
+
+
+def test_serve_failures_leave_the_other_jobs_untouched(gpu):
+    """Host-side failures in a mix of concurrent jobs: one job's device allocation fails (injected
+    on the host, as if the pool had no room) and one job is malformed (its forward plan is destroyed
+    while it waits).  Both fail with their own error; every other job completes with output
+    bit-identical to its run alone, and the server keeps its budget accounting."""
+    p3d = gpu
+    p3d.set_fp64_arith(1)
+    jobs = [SJob(p3d, gd, kind, prec, seed=90 + i) for i, (gd, kind, prec) in enumerate(MIX)]
+    srv = p3d.Server(4 << 30, nslots=1)
+    alone = []
+    for j in jobs:
+        assert srv.wait(srv.submit(j.f, j.b, j.pin_in.array, j.pin_out.array, idir=0))
+        alone.append(j.result())
+        j.pin_out.array[...] = 0
+    srv.close()
+
+    srv = p3d.Server(4 << 30, nslots=8)
+    t0 = srv.clock() + 0.2  # arrivals held back until the failures are armed
+    ids = [srv.submit(j.f, j.b, j.pin_in.array, j.pin_out.array, idir=0, arrival=t0) for j in jobs]
+    victim_out = p3d.PinnedArray(jobs[2].x.shape, jobs[2].x.dtype)
+    victim = srv.submit(jobs[2].f, jobs[2].b, jobs[2].pin_in.array, victim_out.array, idir=0, arrival=t0)
+    srv.inject_alloc_failure(victim)
+    bad = SJob(p3d, MIX[3][0], MIX[3][1], MIX[3][2], seed=93)
+    malformed = srv.submit(bad.f, bad.b, bad.pin_in.array, bad.pin_out.array, idir=0, arrival=t0)
+    p3d.lib().p3dfft_gb300_destroy3d(bad.f.handle)
+    bad.f.handle = -1
+    p3d.lib().p3dfft_clear_error()
+    assert srv.drain() != 0
+    st = srv.stats()
+    assert st["failed"] == 2 and st["completed"] == len(jobs), st
+    with pytest.raises(p3d.P3DFFTError, match="CUDA"):
+        srv.wait(victim)
+    with pytest.raises(p3d.P3DFFTError, match="BAD_ARG"):
+        srv.wait(malformed)
+    for j, a, jid in zip(jobs, alone, ids):
+        assert srv.wait(jid)
+        assert np.array_equal(j.result(), a), (j.gd, j.kind, j.prec)
+    assert not np.any(victim_out.array)
+    srv.close()
+    p3d.lib().p3dfft_clear_error()
