@@ -262,12 +262,42 @@ def load_instr(kernel_key, tag="INSTR"):
     return None
 
 
-def kernel_id(stage, arith, n_dims):
-    """Name of the kernel instantiation that runs a stage (matches the ncu kernel names)."""
+def _nfft(stage):
     kind = {5: 1, 7: 2}.get(stage["type"], 0)  # R2C_D, C2R_D, else C2C
     n = stage["gdims1"][stage["dim"]] if kind != 2 else stage["gdims2"][stage["dim"]]
-    nfft = n // 2 if kind else n
-    return f"k_fast<{'DFP' if arith else 'Native<double>'},{kind},{nfft}>"
+    return kind, (n // 2 if kind else n)
+
+
+def ff_variant(stages, i, arith, ff_on=True):
+    """Float-float intermediate variant of stage i of a plan (bit 0: float-float input, bit 1:
+    float-float output): the library links two consecutive float-float stages whose specialised
+    kernels have float-float variants (C2C in / out, R2C out, C2R in; power-of-two FFT lengths
+    64..2048)."""
+    if not (arith and ff_on):
+        return 0
+
+    def capable(st):
+        return st["type"] in (5, 7, 9, 11) and _nfft(st)[1] in (64, 128, 256, 512, 1024, 2048)
+
+    def can_out(st):
+        return capable(st) and st["type"] in (5, 9, 11)
+
+    def can_in(st):
+        return capable(st) and st["type"] in (7, 9, 11)
+
+    v = 0
+    if i > 0 and can_in(stages[i]) and can_out(stages[i - 1]):
+        v |= 1
+    if i + 1 < len(stages) and can_out(stages[i]) and can_in(stages[i + 1]):
+        v |= 2
+    return v
+
+
+def kernel_id(stage, arith, n_dims, ff=0):
+    """Name of the kernel instantiation that runs a stage (matches the ncu kernel names:
+    k_fast<arithmetic, kind, FFT length, float-float variant>)."""
+    kind, nfft = _nfft(stage)
+    return f"k_fast<{'DFP' if arith else 'Native<double>'},{kind},{nfft},{ff}>"
 
 
 # ------------------------------------------------------------------------------------------
@@ -778,14 +808,15 @@ def main():
     L.p3dfft_gb300_profile_stages(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(d_out.ptr), -1, 5, ms_b, 8)
     stages = []
     for plan, msv in ((f, ms_f), (b, ms_b)):
-        for i, st in enumerate(plan.stages()):
+        pst = plan.stages(executed=True)
+        for i, st in enumerate(pst):
             dt1 = 1 if st["type"] in (5,) else 2
             dt2 = 1 if st["type"] in (7,) else 2
             bytes_ = 8 * (dt1 * int(np.prod(st["gdims1"])) + dt2 * int(np.prod(st["gdims2"])))
             # complex FFT points of the stage (an even-length R2C / C2R runs a half-length FFT)
             pts = int(np.prod(st["gdims1"] if dt2 == 2 else st["gdims2"])) // (2 if st["type"] in (5, 7) else 1)
             stages.append({"dim": st["dim"], "type": st["type"], "ms": msv[i], "bytes": bytes_,
-                           "points": pts, "kernel": kernel_id(st, arith, GD)})
+                           "points": pts, "kernel": kernel_id(st, arith, GD, ff_variant(pst, i, arith))})
     # dominant kernel = the instantiation with the largest total time per step
     per_kernel = {}
     for s in stages:
@@ -823,6 +854,15 @@ def main():
             ach, pk = fpp * per_s, 128.0 * n_sm * clk
             roofline["fp32_pipe"] = {"bound": "FMA pipe (FP32 operations)", "achieved": ach, "peak": pk,
                                      "unit": "FP32 op/s", "frac": ach / pk, "fp32_ops_per_point": fpp}
+            # the HBM fraction this kernel could reach with its FMA pipe 100% busy: the time its
+            # FP32 operations take at the pipe's peak against the time its bytes take at the
+            # HBM peak
+            t_ops = fpp * dk["points"] / dk["launches"] / pk
+            t_hbm = dk["bytes"] / dk["launches"] / (peak * 1e9)
+            roofline["compute_ceiling_frac"] = min(1.0, t_hbm / t_ops)
+    # the dominant kernel's per-point counts and DRAM traffic come from the committed ncu
+    # summaries under profiles/ (one small-case capture each), not from this run
+    roofline["counts_source"] = "profiles/ (committed ncu summaries: TRAFFIC, INSTR, FP32OPS lines)"
 
     # ---- e2e: pinned host buffers through the public API ----
     hin = p3d.PinnedArray(p3d.storage_shape(GD, MO1), np.float64)
@@ -848,6 +888,13 @@ def main():
                       (True, "direct_both")):
         p3d.set_host_direct(mode)
         modes_ms[key] = e2e_run()
+    p3d.set_host_direct(True)
+    # A/B: staged copies with the first / last two stages pipelined behind them (default) or
+    # the first / last stage alone
+    p3d.set_host_direct(False)
+    p3d.set_host_pipeline(False)
+    modes_ms["staged_both_not_pipelined"] = e2e_run()
+    p3d.set_host_pipeline(True)
     p3d.set_host_direct(True)
     e2e_staged_ms = modes_ms["staged_both"]
     e2e_ms = modes_ms["direct_both"]
@@ -929,6 +976,31 @@ def main():
     forms["fp32"]["plain_twiddles"] = {"ms_per_step": ms32p,
                                        "rel_l2_vs_fp64": float(np.linalg.norm(y32p - y) / np.linalg.norm(y))}
     forms["fp32"]["line_error_vs_fp64_by_length"] = fp32_line_errors(p3d)
+
+    # A/B: TMA-staged tile loads (the default) against per-thread global loads, in the FP32 stages
+    # whose lines are contiguous (per-stage CUDA-event times both ways)
+    def fp32_stage_ms():
+        mf, mb = (ctypes.c_double * 8)(), (ctypes.c_double * 8)()
+        nf = L.p3dfft_gb300_profile_stages(f32.handle, ctypes.c_void_p(d_in32.ptr), ctypes.c_void_p(d_spec32.ptr), IDIR, 5, mf, 8)
+        nb = L.p3dfft_gb300_profile_stages(b32.handle, ctypes.c_void_p(d_spec32.ptr), ctypes.c_void_p(d_out32.ptr), -1, 5, mb, 8)
+        return [round(v, 4) for v in list(mf)[:max(nf, 0)] + list(mb)[:max(nb, 0)]]
+
+    c0 = p3d.tma_launch_count()
+    p3d.check(L.p3dfft_gb300_exec3d(f32.handle, ctypes.c_void_p(d_in32.ptr), ctypes.c_void_p(d_spec32.ptr), IDIR, 0))
+    p3d.check(L.p3dfft_gb300_exec3d(b32.handle, ctypes.c_void_p(d_spec32.ptr), ctypes.c_void_p(d_out32.ptr), -1, 0))
+    L.p3dfft_gb300_synchronize()
+    tma_stages = p3d.tma_launch_count() - c0
+    y32_t = d_out32.download(np.empty(y.shape, np.float32))
+    st_tma = fp32_stage_ms()
+    p3d.set_fp32_tma(False)
+    ms32n = timed(f32.handle, b32.handle, d_in32.ptr, d_spec32.ptr, d_out32.ptr, args.steps)
+    y32_n = d_out32.download(np.empty(y.shape, np.float32))
+    st_lsu = fp32_stage_ms()
+    p3d.set_fp32_tma(True)
+    forms["fp32"]["tma"] = {"stages_per_round_trip": tma_stages, "ms_per_step_per_thread_loads": ms32n,
+                            "bit_identical_to_per_thread_loads": bool(np.array_equal(y32_t, y32_n)),
+                            "stages_ms_tma": st_tma, "stages_ms_per_thread_loads": st_lsu,
+                            "status_word": p3d.device_status()}
     del d_in32, d_spec32, d_out32, f32, b32
     forms["mixed_types_384x256x257"] = mixed_types_workload(p3d, L, max(5, args.steps // 5), arith)
     if not args.no_batch:

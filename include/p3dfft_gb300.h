@@ -39,6 +39,14 @@ void p3dfft_gb300_set_sync(int sync);
  * of 32 MB and more).  Pageable host arrays are always staged.  P3DFFT_GB300_HOST_DIRECT=0 /
  * in / out sets 0 / 2 / 3 at start-up. */
 void p3dfft_gb300_set_host_direct(int on);
+/* 1 (default): when host arrays are staged through HBM (pageable arrays, or host_direct 0), the
+ * first two stages run slab by slab behind the per-slab host-to-device copies (slabs along the dim
+ * neither transforms; the second stage on a second stream), and the last two stages likewise
+ * ahead of the per-slab copies back (fields of 32 MB and more, plans of 3+ stages, the slab dim
+ * the slowest of the staged layout).  0: the first / last stage alone overlaps its copies.
+ * P3DFFT_GB300_PIPELINE=0 sets 0 at start-up. */
+void p3dfft_gb300_set_host_pipeline(int on);
+int p3dfft_gb300_get_host_pipeline(void);
 /* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,
  * ~1e-14 relative L2 per 3D transform), 0 = native FP64 DFMA (slow on GB300).  The initial value
  * can be set with P3DFFT_GB300_FP64_ARITH=native. */
@@ -67,6 +75,21 @@ int p3dfft_gb300_get_ff_intermediates(void);
  * of two table entries.  The initial value can be set with P3DFFT_GB300_FP32_SPLIT_TWIDDLES=0. */
 void p3dfft_gb300_set_fp32_split_twiddles(int on);
 int p3dfft_gb300_get_fp32_split_twiddles(void);
+/* 1 (default): FP32 C2C / R2C stages whose lines are contiguous and evenly spaced in device
+ * memory (lengths 2^a*3^b*5^c from 32 whose first radix equals the points per thread, line
+ * length 2N floats <= 256 or a multiple of 256) fetch each tile by TMA (a tensor map over the
+ * input, cp.async.bulk.tensor into shared memory) instead of per-thread global loads; 0: always
+ * per-thread loads.  The initial value can be set with P3DFFT_GB300_FP32_TMA=0. */
+void p3dfft_gb300_set_fp32_tma(int on);
+int p3dfft_gb300_get_fp32_tma(void);
+/* The device status word: nonzero after a kernel's bounded wait ran out (the tile was skipped,
+ * the output is invalid).  clear != 0 resets it.  Synchronous. */
+int p3dfft_gb300_device_status(int clear);
+/* Test hook: the next TMA-staged launch waits for 16 bytes its copies never deliver, so every
+ * tile's wait runs out after 20 ms and sets the status word (no tile is transformed). */
+void p3dfft_gb300_inject_tma_stall(void);
+/* TMA-staged stage launches since the library was loaded */
+long long p3dfft_gb300_tma_launch_count(void);
 
 /* ---- planning / execution by explicit grid descriptions (1x1x1 processor grid) ----
  * A grid is (gdims[3], mem_order[3], dim_conj_sym).  Returns a handle >= 0, or -1 with the

@@ -607,6 +607,16 @@ static bool is_device_ptr(const void *p) {
 // Page-locked host arrays read (bit 0) / written (bit 1) by the first / last stage directly over
 // NVLink-C2C instead of staged through HBM.  -1: from P3DFFT_GB300_HOST_DIRECT at first use
 // ("0" none, "in", "out", anything else both; default both).
+// Pipelining of the host-link-bound end stages with their neighbour stage (default on;
+// P3DFFT_GB300_PIPELINE=0 or p3dfft_gb300_set_host_pipeline(0) turns it off)
+static int g_host_pipe = -1;
+static bool pipeline_host_stages() {
+  if (g_host_pipe < 0) {
+    const char *e = getenv("P3DFFT_GB300_PIPELINE");
+    g_host_pipe = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_host_pipe == 1;
+}
 static int g_host_direct = -1;
 static int host_direct_mode() {
   if (g_host_direct < 0) {
@@ -692,11 +702,17 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
   }
 }
 
+// A sub-box of a stage: coordinates [c, c + m) along dim sd, in the stage's full input and output
+// layouts (the strides of the whole field).
+struct SlabBox {
+  int sd, c, m;
+};
+
 // engine_override >= 0 replaces the plan's tuned engine choice for this stage (0 = heuristic);
-// ff: float-float intermediate links of this stage
+// ff: float-float intermediate links of this stage; box: run only that sub-box of the stage
 static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, bool deriv,
                      const void *tw_given = nullptr, const void *aux_given = nullptr, int engine_override = -1,
-                     const FFLink *ff = nullptr) {
+                     const FFLink *ff = nullptr, const SlabBox *box = nullptr) {
   const TypeInfo &t = g_types[s.type];
   if (t_ctx && t_ctx->rec) {  // recording for a grouped launch set
     StageLaunch sl;
@@ -735,6 +751,14 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
         d.mi[i] = ff->mi[i];
         d.mo[i] = ff->mo[i];
       }
+    }
+    if (box) {  // the sub-box keeps the full field's strides; buffers and scale arrays are offset
+      const int sd = box->sd;
+      src = static_cast<const unsigned char *>(src) + (size_t)box->c * d.s1[sd] * t.dt1 * P->prec;
+      dst = static_cast<unsigned char *>(dst) + (size_t)box->c * d.s2[sd] * t.dt2 * P->prec;
+      d.d1[sd] = d.d2[sd] = box->m;
+      if (d.sin) d.sin += (long long)box->c * d.mi[sd];
+      if (d.sout) d.sout += (long long)box->c * d.mo[sd];
     }
     bool reorder = !(s.g1.mo[0] == s.g2.mo[0] && s.g1.mo[1] == s.g2.mo[1] && s.g1.mo[2] == s.g2.mo[2]);
     TimerScope ts(deriv ? 3 : (reorder ? 1 : 0));
@@ -779,14 +803,19 @@ static const FFLink *slab_link(const FFLink *ff, int c, int sd, FFLink *out) {
   return out;
 }
 
+static int ensure_copy_stream() {
+  if (!g_copy_stream) {
+    for (auto &e : g_slab_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return E_CUDA;
+    if (cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking) != cudaSuccess) return E_CUDA;
+  }
+  return E_OK;
+}
+
 static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *host, const void *src, void *dst,
                            bool deriv, int side, const FFLink *ff = nullptr) {
   const int NS = 8;
-  if (!g_copy_stream) {
-    if (cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking) != cudaSuccess) return E_CUDA;
-    for (auto &e : g_slab_ev)
-      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return E_CUDA;
-  }
+  if (ensure_copy_stream() != E_OK) return E_CUDA;
   const TypeInfo &t = g_types[st.type];
   long long s1[3], s2[3];
   strides(st.g1, s1);
@@ -977,6 +1006,107 @@ static void ff_multipliers(const GridDesc &g, int A, long long m[3]) {
   m[d2] = g.gdims[d1];
 }
 
+// Two consecutive stages pipelined slab by slab along dim sd, which neither transforms: stage a
+// runs slab k on the library stream, stage b runs slab k on a second stream as soon as that slab
+// of a is written, so b works alongside a's later slabs.  Used with host staging copies (which
+// bound the step): both stages then hide behind the transfer.  All work is ordered on the library
+// stream when this returns.
+static int pair_slab_dim(const Stage &a, const Stage &b) {
+  if (g_types[a.type].kind == K_EMPTY || g_types[b.type].kind == K_EMPTY || a.dim == b.dim) return -1;
+  const int sd = 3 - a.dim - b.dim;
+  return a.g1.gdims[sd] >= 8 ? sd : -1;
+}
+static cudaStream_t g_pipe_stream = nullptr;
+static cudaEvent_t g_pipe_ev[9];  // one per slab, and the fork / join event
+
+// host_in: stage a's input is staged from host array host_in into src, slab k copied on the copy
+// stream just before stage a's slab k; host_out: stage b's output dst is copied to host array
+// host_out slab by slab as stage b finishes each (sd the slowest dim of that layout, so each slab
+// is one contiguous copy).
+static int ensure_copy_stream();
+static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void *dst, int idir, const FFLink *lka,
+                          const FFLink *lkb, int sd, const void *host_in = nullptr, void *host_out = nullptr) {
+  static int NS = 0;  // slabs (P3DFFT_GB300_PIPE_SLABS, 2..8, default 8)
+  if (!NS) {
+    const char *e = getenv("P3DFFT_GB300_PIPE_SLABS");
+    NS = e ? std::max(2, std::min(8, atoi(e))) : 8;
+  }
+  if (!g_pipe_stream) {
+    // the on-device stage's slabs get the highest priority, so that each starts as soon as its
+    // slab of the link-bound stage is written rather than queueing behind that stage's CTAs
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&g_pipe_stream, cudaStreamNonBlocking, hi) != cudaSuccess) return E_CUDA;
+    for (auto &e : g_pipe_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return E_CUDA;
+  }
+  if ((host_in || host_out) && ensure_copy_stream() != E_OK) return E_CUDA;
+  const Stage &a = P->ex[s], &b = P->ex[s + 1];
+  const bool da = idir >= 0 && a.dim == idir, db = idir >= 0 && b.dim == idir;
+  // slab starts stay 16-byte aligned in all four layouts
+  size_t u[4];
+  {
+    long long s1[3], s2[3];
+    strides(a.g1, s1);
+    strides(a.g2, s2);
+    u[0] = (size_t)s1[sd] * g_types[a.type].dt1 * P->prec;
+    u[1] = (size_t)s2[sd] * g_types[a.type].dt2 * P->prec;
+    strides(b.g1, s1);
+    strides(b.g2, s2);
+    u[2] = (size_t)s1[sd] * g_types[b.type].dt1 * P->prec;
+    u[3] = (size_t)s2[sd] * g_types[b.type].dt2 * P->prec;
+  }
+  int f = 1;
+  while (f < 16 && ((f * u[0]) % 16 || (f * u[1]) % 16 || (f * u[2]) % 16 || (f * u[3]) % 16)) f++;
+  const int len = a.g1.gdims[sd];
+  const int per = ((len + NS - 1) / NS + f - 1) / f * f;
+  cudaStream_t ms = cur_stream(), ps = g_pipe_stream, cs = g_copy_stream;
+  // the second stream (and the copy stream) start after everything already queued on the
+  // library stream
+  if (cudaEventRecord(g_pipe_ev[8], ms) != cudaSuccess || cudaStreamWaitEvent(ps, g_pipe_ev[8], 0) != cudaSuccess)
+    return E_CUDA;
+  if ((host_in || host_out) && cudaStreamWaitEvent(cs, g_pipe_ev[8], 0) != cudaSuccess) return E_CUDA;
+  ExecCtx pc{ps, nullptr, false, nullptr};
+  int rc = E_OK;
+  for (int c = 0, k = 0; c < len && rc == E_OK; c += per, k++) {
+    const SlabBox box{sd, c, std::min(per, len - c)};
+    if (host_in) {
+      if (cudaMemcpyAsync(static_cast<unsigned char *>(const_cast<void *>(src)) + (size_t)c * u[0],
+                          static_cast<const unsigned char *>(host_in) + (size_t)c * u[0], (size_t)box.m * u[0],
+                          cudaMemcpyHostToDevice, cs) != cudaSuccess ||
+          cudaEventRecord(g_slab_ev[k], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[k], 0) != cudaSuccess) {
+        rc = E_CUDA;
+        break;
+      }
+    }
+    rc = run_stage(P, a, src, mid, da, nullptr, nullptr, -1, lka, &box);
+    if (rc != E_OK) break;
+    if (cudaEventRecord(g_pipe_ev[k], ms) != cudaSuccess || cudaStreamWaitEvent(ps, g_pipe_ev[k], 0) != cudaSuccess) {
+      rc = E_CUDA;
+      break;
+    }
+    const ExecCtx *prev = t_ctx;
+    t_ctx = &pc;
+    rc = run_stage(P, b, mid, dst, db, nullptr, nullptr, -1, lkb, &box);
+    t_ctx = prev;
+    if (rc == E_OK && host_out) {
+      if (cudaEventRecord(g_slab_ev[8 + k], ps) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[8 + k], 0) != cudaSuccess ||
+          cudaMemcpyAsync(static_cast<unsigned char *>(host_out) + (size_t)c * u[3],
+                          static_cast<const unsigned char *>(dst) + (size_t)c * u[3], (size_t)box.m * u[3],
+                          cudaMemcpyDeviceToHost, cs) != cudaSuccess)
+        rc = E_CUDA;
+    }
+  }
+  if (host_out) {  // the library stream continues after the last copy
+    if (cudaEventRecord(g_slab_ev[16], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[16], 0) != cudaSuccess)
+      return E_CUDA;
+  }
+  // the library stream continues after the second stream's last slab (also after a failure)
+  if (cudaEventRecord(g_pipe_ev[8], ps) != cudaSuccess || cudaStreamWaitEvent(ms, g_pipe_ev[8], 0) != cudaSuccess)
+    return E_CUDA;
+  return rc;
+}
+
 static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaEvent_t *stage_ev = nullptr) {
   if (g_autotune && !in_capture() && (P->tune.empty() || (P->prec == 8 && P->tuned_arith != arith_mode()))) {
     if (!ensure_device()) return t_err;
@@ -1018,9 +1148,26 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
                         ? slab_dim(P->ex[0]) : -1;
   const int sd_out = (stage_host_out && out_bytes >= kSlabMin && n >= 2 && !stage_ev && !g_timers_on && in != out)
                          ? slab_dim(P->ex[n - 1]) : -1;
+  // Staged host arrays: the first stage and the next one run slab by slab, each slab's host copy
+  // on the copy stream just before the first stage's slab and the second stage's slab right
+  // after it on a second stream; likewise the last two stages with the copies back (the slab dim
+  // the slowest of the staged layout, so each slab is one copy).  Not for host arrays read or
+  // written directly by the kernels: there the SMs themselves move the data over the link and
+  // a concurrent stage only takes SM time from them (measured no gain, 13.69 vs 13.66 ms).
+  const bool can_pipe = !stage_ev && !g_timers_on && !t_ctx && n >= 3 && pipeline_host_stages();
+  int pipe_in = -1, pipe_out = -1;
+  if (can_pipe && stage_host_in && in_bytes >= kSlabMin) {
+    pipe_in = pair_slab_dim(P->ex[0], P->ex[1]);
+    if (pipe_in >= 0 && P->ex[0].g1.mo[pipe_in] != 2) pipe_in = -1;
+  }
+  if (can_pipe && stage_host_out && out_bytes >= kSlabMin && (pipe_in < 0 || n >= 4) && in != out) {
+    pipe_out = pair_slab_dim(P->ex[n - 2], P->ex[n - 1]);
+    if (pipe_out >= 0 && P->ex[n - 1].g2.mo[pipe_out] != 2) pipe_out = -1;
+  }
+  const bool pipe_in_staged = pipe_in >= 0 && stage_host_in, pipe_out_staged = pipe_out >= 0 && stage_host_out;
   if (stage_host_in) {
     if (!ensure_buf(&B.stage_in, &B.stage_in_bytes, in_bytes)) return E_CUDA;
-    if (sd_in < 0) {
+    if (sd_in < 0 && !pipe_in_staged) {
       TimerScope ts(4);
       if (cudaMemcpyAsync(B.stage_in, in, in_bytes, cudaMemcpyHostToDevice, cur_stream()) != cudaSuccess) {
         set_err(E_CUDA, "host-to-device copy failed");
@@ -1042,7 +1189,11 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   for (int s = n - 2; s >= 0; s--) {
     size_t bytes = stage_out_bytes(P, P->ex[s]);
     void *cand = nullptr;
-    if (!out_direct && dout != dst[s + 1] && bytes <= out_bytes && !(s == 0 && dout == din) && dout != din) cand = dout;
+    // (a staged output pipelined with the stage before the last: the slabs of stage n-2 read
+    // dst[n-3] while the last stage writes the output buffer, so they must differ)
+    if (!out_direct && dout != dst[s + 1] && bytes <= out_bytes && !(s == 0 && dout == din) && dout != din &&
+        !(pipe_out_staged && s == n - 3))
+      cand = dout;
     if (!cand) {
       int k = (dst[s + 1] == B.scratch[0] && B.scratch[0]) ? 1 : 0;
       if (need > B.scratch_bytes || !B.scratch[k]) {
@@ -1122,7 +1273,15 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     void *d = dst[s];
     if (stage_ev) cudaEventRecord(stage_ev[s], cur_stream());
     const FFLink *lk = (ffl[s].ffin || ffl[s].ffout) ? &ffl[s] : nullptr;
-    if (s == 0 && sd_in >= 0) {
+    if ((s == 0 && pipe_in >= 0) || (s == n - 2 && pipe_out >= 0)) {  // this stage and the next, pipelined
+      const FFLink *lk2 = (ffl[s + 1].ffin || ffl[s + 1].ffout) ? &ffl[s + 1] : nullptr;
+      const bool first = s == 0 && pipe_in >= 0;
+      rc = run_pair_slabs(P, s, src, d, dst[s + 1], idir, lk, lk2, first ? pipe_in : pipe_out,
+                          (first && pipe_in_staged) ? in : nullptr, (!first && pipe_out_staged) ? out : nullptr);
+      src = dst[s + 1];
+      s++;
+      continue;
+    } else if (s == 0 && sd_in >= 0) {
       rc = run_stage_slabs(P, st, sd_in, in, din, d, deriv, 0, lk);
     } else if (s == n - 1 && sd_out >= 0) {
       rc = run_stage_slabs(P, st, sd_out, out, src, d, deriv, 1, lk);
@@ -1146,7 +1305,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   }
   if (stage_ev) cudaEventRecord(stage_ev[n], cur_stream());
   if (rc != E_OK) return rc;
-  if (stage_host_out && sd_out < 0) {
+  if (stage_host_out && sd_out < 0 && !pipe_out_staged) {
     TimerScope ts(5);
     if (cudaMemcpyAsync(out, dout, out_bytes, cudaMemcpyDeviceToHost, cur_stream()) != cudaSuccess) {
       set_err(E_CUDA, "device-to-host copy failed");
@@ -1413,12 +1572,22 @@ void p3dfft_clear_error(void) {
 }
 void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
+void p3dfft_gb300_set_host_pipeline(int on) { g_host_pipe = on ? 1 : 0; }
+int p3dfft_gb300_get_host_pipeline(void) { return pipeline_host_stages() ? 1 : 0; }
 void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on == 1 ? 3 : (on == 2 ? 1 : (on == 3 ? 2 : 0)); }
 void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }
 void p3dfft_gb300_set_reference_compat(int on) { g_ref_compat = on ? 1 : 0; }
 void p3dfft_gb300_set_ff_intermediates(int on) { g_ff_inter = on ? 1 : 0; }
 void p3dfft_gb300_set_fp32_split_twiddles(int on) { set_fp32_split_twiddles(on != 0); }
 int p3dfft_gb300_get_fp32_split_twiddles(void) { return fp32_split_twiddles() ? 1 : 0; }
+void p3dfft_gb300_set_fp32_tma(int on) { set_fp32_tma(on != 0); }
+int p3dfft_gb300_get_fp32_tma(void) { return fp32_tma() ? 1 : 0; }
+int p3dfft_gb300_device_status(int clear) {
+  if (!ensure_device()) return -1;
+  return device_status(g_tabs, clear != 0);
+}
+void p3dfft_gb300_inject_tma_stall(void) { inject_tma_stall(); }
+long long p3dfft_gb300_tma_launch_count(void) { return tma_launches(); }
 int p3dfft_gb300_get_ff_intermediates(void) { return ff_intermediates() ? 1 : 0; }
 int p3dfft_gb300_get_reference_compat(void) { return ref_compat(); }
 int p3dfft_gb300_get_fp64_arith(void) { return arith_mode(); }

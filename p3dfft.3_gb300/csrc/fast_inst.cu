@@ -27,7 +27,7 @@ static_assert(P3D_FAST_PART < fast_nparts<FastArith>(), "part out of range for t
 
 template <>
 int fast_launch_part<FastArith, P3D_FAST_KIND, P3D_FAST_PART>(int n, const FParams &p, const FGroup *g, int ctas,
-                                                              cudaStream_t st) {
-  return fk_dispatch_n<FastArith, P3D_FAST_KIND, P3D_FAST_PART>(n, p, g, ctas, st);
+                                                              cudaStream_t st, const CUtensorMap *tm) {
+  return fk_dispatch_n<FastArith, P3D_FAST_KIND, P3D_FAST_PART>(n, p, g, ctas, st, tm);
 }
 }  // namespace p3d

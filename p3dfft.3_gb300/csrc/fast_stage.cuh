@@ -22,6 +22,7 @@
 //     pre-twiddled, zero-padded real line and a post-twiddle on the way out; a complex line is
 //     two real lines (its real and imaginary parts)
 #pragma once
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -61,6 +62,13 @@ struct FParams {
   const int *sin;
   int *sout;
   long long fi_j, fi_t, fi_o, fo_t, fo_o;
+  // TMA-staged loads (k_fast_tma): the wait for the tile's bytes gives up after tma_timeout_ns
+  // and sets *status to 1; tma_extra adds bytes the copies never deliver (a wait that runs out,
+  // for the failure-path test)
+  long long tma_timeout_ns;
+  int tma_extra;
+  int tma_d1;  // lines along the tensor map's second dim (line g at (g % tma_d1, g / tma_d1))
+  int *status;
 };
 
 // resident 256-thread CTAs per SM the register allocation is sized for (FP64 and float-float;
@@ -409,11 +417,53 @@ struct FWork {
   int stage, tile;
 };
 
+// TMA staging of a tile's input (FP32 C2C / R2C with line-contiguous, evenly spaced lines and a
+// first radix equal to the points per thread): a 3D tensor map (floats along the line, lines
+// along the tile dim, lines along the other batch dim) and NBOX boxes of BOXW floats x TB lines,
+// landed densely in the tile's shared-memory region box after box; one mbarrier counts the bytes.
+// Threads then read their first butterfly's inputs from shared memory instead of global memory.
+template <int N>
+struct FastTma {
+  static constexpr int FL = 2 * N;  // floats per line (complex points, or packed real pairs)
+  static constexpr int BOXW = FL <= 256 ? FL : 256;
+  static constexpr int NBOX = FL / BOXW;
+  static constexpr bool OK = FL <= 256 || FL % 256 == 0;
+};
+__host__ __device__ constexpr bool fast_tma_length(int n) {
+  // even n: a box row of 2n floats is a multiple of 16 bytes
+  return n >= 32 && n % 2 == 0 && (2 * n <= 256 || (2 * n) % 256 == 0) && fast_radices(n).n > 0 &&
+         fast_radices(n).r[0] == fast_points(n);
+}
+template <class O, int KIND, int N>
+__host__ __device__ constexpr bool fk_tma_variant() {
+  return (std::is_same_v<O, Native<float>> || std::is_same_v<O, NativeFS<false>>) &&
+         (KIND == FK_C2C || KIND == FK_R2C) && fast_tma_length(N);
+}
+// mbarrier phase wait bounded by the global timer: false after limit_ns
+__device__ __forceinline__ bool fk_mbar_wait(unsigned bar, unsigned parity, long long limit_ns) {
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if ((long long)(t - t0) > limit_ns) return false;
+  }
+}
+
 // One tile of one stage (the body of k_fast and k_fast_list).
 // FF: float-float intermediate I/O of the DFP kernels, bit 0 input, bit 1 output (FParams ffin /
 // ffout); separate instantiations (fk_ff_variants), so that the IEEE-only kernels carry none of it
-template <class O, int KIND, int N, int FF = 0>
-__device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const void *in, void *out) {
+// TMA: the tile's input arrives by the tensor map *tm (fk_tma_variant kernels only).
+template <class O, int KIND, int N, int FF = 0, bool TMA = false>
+__device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const void *in, void *out,
+                                        const CUtensorMap *tm = nullptr) {
   using C = typename O::C;
   using T = typename O::T;
   using G = typename O::G;
@@ -422,7 +472,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   constexpr int TWSTEP = (KIND == FK_C2C || KIND == FK_R2R1 || KIND == FK_R2RG) ? 1 : 2;  // W_N^m = tab[m * TWSTEP]
   constexpr int LS = fast_ls<N, (int)sizeof(C)>(), TB = SH::TB, TT = SH::T, V = SH::V;
   constexpr int PS = fast_pad_shift<(int)sizeof(C)>();
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   C *buf = reinterpret_cast<C *>(smem_raw);
   __shared__ int red[32], red2[32];
   // float-float tiles whose lines differ widely in magnitude: each line's largest biased
@@ -432,6 +482,35 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
   const T *ptab = reinterpret_cast<const T *>(p.ptw);
   // threads past TB*T (BLOCK rounded up to whole warps) hold no line
   const bool valid = SH::BLOCK == SH::USED || (int)threadIdx.x < SH::USED;
+  unsigned tbar_addr = 0;
+  // TMA writes to 128-byte aligned shared memory only; a tile region placed otherwise is loaded by
+  // the threads (the same values, by the per-thread path)
+  const bool tma_on = TMA && ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u) == 0;
+  if constexpr (TMA) {
+    // one thread starts the tile's copies first thing; the others meet it at the barrier below
+    __shared__ __align__(8) unsigned long long tbar;
+    using TM = FastTma<N>;
+    tbar_addr = (unsigned)__cvta_generic_to_shared(&tbar);
+    if (threadIdx.x == 0 && tma_on) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tbar_addr) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      constexpr unsigned BYTES = (unsigned)(TM::NBOX * TB * TM::BOXW * 4);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tbar_addr),
+                   "r"(BYTES + (unsigned)p.tma_extra)
+                   : "memory");
+      const int g0 = tile * TB, ct = g0 % p.tma_d1, co = g0 / p.tma_d1;
+      const unsigned dst0 = (unsigned)__cvta_generic_to_shared(smem_raw);
+#pragma unroll 1
+      for (int b = 0; b < TM::NBOX; b++)
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];" ::"r"(dst0 + (unsigned)(b * TB * TM::BOXW * 4)),
+            "l"(reinterpret_cast<unsigned long long>(tm)), "r"(b * TM::BOXW), "r"(ct), "r"(co), "r"(tbar_addr)
+            : "memory");
+    }
+    __syncthreads();
+  }
 
   // The float-float FFT passes of a tile synchronise per line when each line's threads are whole
   // warps or share one warp and the load gives each line to consecutive threads (then the passes
@@ -534,12 +613,43 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     // values a thread loads are exactly the inputs of its first butterfly, so the first pass runs
     // on them in registers and the tile's first trip through shared memory is skipped.
     constexpr bool FUSE1 = !O::SCALED && KIND != FK_C2R && KIND != FK_R2R1 && KIND != FK_R2RG && RL.r[0] == V;
+    static_assert(!TMA || FUSE1, "TMA staging feeds the first pass in registers");
     if constexpr (FUSE1) {
       constexpr int R0 = RL.r[0];
       C x[V];
-      if (act) {
+      bool staged = false;
+      if constexpr (TMA) {
+        if (tma_on) {
+          using TM = FastTma<N>;
+          // every thread's wait ends (bytes arrived, or the time limit); the CTA agrees on the outcome
+          const bool got = __syncthreads_and(fk_mbar_wait(tbar_addr, 0, p.tma_timeout_ns));
+          if (!got) {
+            // the tile is skipped; its copies get a second bounded wait before the CTA exits
+            if (threadIdx.x == 0) {
+              if (p.status) atomicExch(p.status, 1);
+              fk_mbar_wait(tbar_addr, 0, p.tma_timeout_ns);
+            }
+            return;
+          }
+          if (act) {
+            const float *stg = reinterpret_cast<const float *>(smem_raw);
+#pragma unroll
+            for (int e = 0; e < V; e++) {
+              const int f = 2 * (j0 + e * TT);  // point j = floats 2j, 2j + 1 of the line
+              x[e] = O::from_raw(
+                  *reinterpret_cast<const RAW *>(stg + (f / TM::BOXW) * (TB * TM::BOXW) + l * TM::BOXW + f % TM::BOXW),
+                  0);
+            }
+          }
+          __syncthreads();  // the first pass below overwrites the staged tile
+          staged = true;
+        }
+      }
+      if (!staged && act) {
 #pragma unroll
         for (int e = 0; e < V; e++) x[e] = O::from_raw(load_raw(j0 + e * TT), 0);
+      }
+      if (act) {
         if constexpr (R0 == 3) dft3<O>(x, fsign, O::tw(tab, (N / 3) * TWSTEP));
         else if constexpr (R0 == 5) dft5<O>(x, fsign, O::tw(tab, (N / 5) * TWSTEP), O::tw(tab, 2 * (N / 5) * TWSTEP));
         else dft_p2<O, R0>(x, fsign);
@@ -791,6 +901,13 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) 
   fk_tile<O, KIND, N, FF>(p, blockIdx.x, p.in, p.out);
 }
 
+// The tile's input staged by the tensor-memory accelerator (fk_tma_variant lengths and kinds).
+template <class O, int KIND, int N>
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>())
+    k_fast_tma(FParams p, const __grid_constant__ CUtensorMap tm) {
+  if constexpr (fk_tma_variant<O, KIND, N>()) fk_tile<O, KIND, N, 0, true>(p, blockIdx.x, p.in, p.out, &tm);
+}
+
 // Lengths and kinds with float-float intermediate variants (DFP: C2C in / out / both, R2C out,
 // C2R in; the power-of-two lengths from 64, which carry the large fields)
 template <class O, int KIND, int N>
@@ -827,6 +944,8 @@ struct FastArgs {
   int n;     // complex FFT length N
   FParams p;
   int split = 0;  // FP32 only: split-twiddle kernels (NativeFS; table format 2)
+  int tma = 0;    // single launches only: the tile's input staged by TMA through tm (k_fast_tma)
+  CUtensorMap tm;
 };
 
 template <class O>
@@ -855,6 +974,11 @@ static int fk_configure() {
         cudaFuncSetAttribute(k_fast_list<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)fk_smem<O, KIND, N>()) != cudaSuccess)
       return E_CUDA;
+    if constexpr (fk_tma_variant<O, KIND, N>()) {
+      if (cudaFuncSetAttribute(k_fast_tma<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)fk_smem<O, KIND, N>()) != cudaSuccess)
+        return E_CUDA;
+    }
     if constexpr (fk_ff_variants<O, KIND, N>()) {
       const int sm = (int)fk_smem<O, KIND, N>();
       if (cudaFuncSetAttribute(k_fast<O, KIND, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
@@ -868,7 +992,7 @@ static int fk_configure() {
 }
 
 template <class O, int KIND, int N>
-static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
+static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t st, const CUtensorMap *tm) {
   if (fk_configure<O, KIND, N>() != E_OK) return E_CUDA;
   if (g) {
     if (ctas <= 0) return E_OK;
@@ -880,6 +1004,15 @@ static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t s
     const unsigned nb = (unsigned)p.ntotal;
     constexpr int BL = FastShape<N>::BLOCK;
     constexpr size_t SM = fk_smem<O, KIND, N>();
+    if (tm) {
+      if constexpr (fk_tma_variant<O, KIND, N>()) {
+        if (ff) return E_UNSUPPORTED;
+        k_fast_tma<O, KIND, N><<<nb, BL, SM, st>>>(p, *tm);
+        return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+      } else {
+        return E_UNSUPPORTED;
+      }
+    }
     if constexpr (fk_ff_variants<O, KIND, N>()) {
       if (ff == 1) k_fast<O, KIND, N, 1><<<nb, BL, SM, st>>>(p);
       else if (ff == 2) k_fast<O, KIND, N, 2><<<nb, BL, SM, st>>>(p);
@@ -915,7 +1048,7 @@ constexpr int fast_part_of(int n) {
 // Lengths of part PART: n > 0 launches the length-n kernel (one stage, or a group of stages when g
 // is set); n == 0 configures (loads) every length's kernels.
 template <class O, int KIND, int PART>
-static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
+static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st, const CUtensorMap *tm) {
   if constexpr (is_split_policy<O>::value) {  // long lines only
     if (n == 0) {
       int rc = E_OK;
@@ -926,7 +1059,7 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
       return rc;
     }
 #define P3D_FAST_CASE(L) \
-  case L: return fk_launch<O, KIND, L>(p, g, ctas, st);
+  case L: return fk_launch<O, KIND, L>(p, g, ctas, st, tm);
     switch (n) {
       P3D_FAST_SPLIT_LENGTHS(P3D_FAST_CASE)
       default: return E_UNSUPPORTED;
@@ -949,7 +1082,7 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
   }
 #define P3D_FAST_CASE(L)                                                      \
   case L:                                                                     \
-    if constexpr (fast_part_of<O>(L) == PART) return fk_launch<O, KIND, L>(p, g, ctas, st); \
+    if constexpr (fast_part_of<O>(L) == PART) return fk_launch<O, KIND, L>(p, g, ctas, st, tm); \
     else return E_UNSUPPORTED;
   if constexpr (KIND == FK_R2R1 || KIND == FK_R2RG) {
     switch (n) {
@@ -967,10 +1100,10 @@ static int fk_dispatch_n(int n, const FParams &p, const FGroup *g, int ctas, cud
 
 // One (arithmetic, kind, part) per translation unit (fast_inst.cu), so they compile in parallel.
 template <class O, int KIND, int PART>
-int fast_launch_part(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st);
+int fast_launch_part(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st, const CUtensorMap *tm);
 #define P3D_FAST_DECL(O, K, P) \
   template <>                  \
-  int fast_launch_part<O, K, P>(int, const FParams &, const FGroup *, int, cudaStream_t);
+  int fast_launch_part<O, K, P>(int, const FParams &, const FGroup *, int, cudaStream_t, const CUtensorMap *);
 #define P3D_FAST_DECL_KINDS(O, P) \
   P3D_FAST_DECL(O, FK_C2C, P)     \
   P3D_FAST_DECL(O, FK_R2C, P)     \
@@ -986,29 +1119,31 @@ P3D_FAST_DECL_KINDS(NativeFS<false>, 0)
 #undef P3D_FAST_DECL
 
 template <class O, int KIND>
-inline int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st) {
+inline int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, cudaStream_t st,
+                            const CUtensorMap *tm) {
   if constexpr (fast_nparts<O>() == 1) {
-    return fast_launch_part<O, KIND, 0>(n, p, g, ctas, st);
+    return fast_launch_part<O, KIND, 0>(n, p, g, ctas, st, tm);
   } else {
     static_assert(fast_nparts<O>() == 2, "two parts");
     if (n == 0) {
-      const int r0 = fast_launch_part<O, KIND, 0>(0, p, g, ctas, st);
-      const int r1 = fast_launch_part<O, KIND, 1>(0, p, g, ctas, st);
+      const int r0 = fast_launch_part<O, KIND, 0>(0, p, g, ctas, st, tm);
+      const int r1 = fast_launch_part<O, KIND, 1>(0, p, g, ctas, st, tm);
       return r0 != E_OK ? r0 : r1;
     }
-    return fast_part_of<O>(n) == 0 ? fast_launch_part<O, KIND, 0>(n, p, g, ctas, st)
-                                   : fast_launch_part<O, KIND, 1>(n, p, g, ctas, st);
+    return fast_part_of<O>(n) == 0 ? fast_launch_part<O, KIND, 0>(n, p, g, ctas, st, tm)
+                                   : fast_launch_part<O, KIND, 1>(n, p, g, ctas, st, tm);
   }
 }
 
 template <class O>
 inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaStream_t st) {
+  const CUtensorMap *tm = (a.tma && !g) ? &a.tm : nullptr;
   switch (a.kind) {
-    case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, g, ctas, st);
-    case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, g, ctas, st);
-    case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, g, ctas, st);
-    case FK_R2R1: return fast_launch_kind<O, FK_R2R1>(a.n, a.p, g, ctas, st);
-    case FK_R2RG: return fast_launch_kind<O, FK_R2RG>(a.n, a.p, g, ctas, st);
+    case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, g, ctas, st, tm);
+    case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, g, ctas, st, tm);
+    case FK_C2R: return fast_launch_kind<O, FK_C2R>(a.n, a.p, g, ctas, st, tm);
+    case FK_R2R1: return fast_launch_kind<O, FK_R2R1>(a.n, a.p, g, ctas, st, tm);
+    case FK_R2RG: return fast_launch_kind<O, FK_R2RG>(a.n, a.p, g, ctas, st, tm);
     default: return E_UNSUPPORTED;
   }
 }

@@ -130,6 +130,17 @@ int launch_permute(const int d[3], const long long s1[3], const long long s2[3],
 // twiddle products when on (the default)
 bool fp32_split_twiddles();
 void set_fp32_split_twiddles(bool on);
+// FP32 C2C / R2C stages with contiguous, evenly spaced lines in device memory stage each tile's
+// input by TMA (cp.async.bulk.tensor) when on (the default)
+bool fp32_tma();
+void set_fp32_tma(bool on);
+// the next TMA launch's wait runs out (20 ms): the failure path of the bounded waits
+void inject_tma_stall();
+// TMA-staged launches so far
+long long tma_launches();
+// the device status word (nonzero: a kernel's bounded wait ran out and its tile was skipped);
+// clear resets it.  Synchronous.
+int device_status(DeviceTables *tabs, bool clear);
 int launch_deriv(int prec, const int d[3], const long long s[3], int idir, int g, int ref_axis, const void *in,
                  void *out, cudaStream_t stream, int *kernels_launched);
 

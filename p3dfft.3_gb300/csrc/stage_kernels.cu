@@ -14,8 +14,10 @@
 //   Native<float>   FP32 data, FFMA arithmetic, twiddles rounded from FP64/long-double tables
 //   DF              FP64 data, float-float arithmetic on the FP32 pipe (df_arith.cuh)
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -694,8 +696,10 @@ struct DeviceTables {
   std::mutex mu;
   // key: (N, format + 8 pass) format 0 = double, 1 = float, 2 = float-float, 3 = packed float-float
   std::map<std::pair<int, int>, void *> tabs;
+  int *status = nullptr;  // device status word: nonzero after a kernel's bounded wait ran out
   ~DeviceTables() {
     for (auto &kv : tabs) cudaFree(kv.second);
+    if (status) cudaFree(status);
   }
   // pass = 1: the specialised kernels' per-pass twiddle rows of FFT length N; pass = 2: the
   // Bluestein engine's tables for length N
@@ -724,8 +728,23 @@ struct DeviceTables {
   }
 };
 
-DeviceTables *tables_create() { return new DeviceTables(); }
+DeviceTables *tables_create() {
+  DeviceTables *t = new DeviceTables();
+  if (cudaMalloc(&t->status, sizeof(int)) != cudaSuccess || cudaMemset(t->status, 0, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    if (t->status) cudaFree(t->status);
+    t->status = nullptr;  // no status word: the kernels with bounded waits are not used
+  }
+  return t;
+}
 void tables_destroy(DeviceTables *t) { delete t; }
+int device_status(DeviceTables *t, bool clear) {
+  if (!t || !t->status) return 0;
+  int v = 0;
+  if (cudaMemcpy(&v, t->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (clear && v && cudaMemset(t->status, 0, sizeof(int)) != cudaSuccess) return -1;
+  return v;
+}
 
 // Radix plan of a length (8s first, then 4, 2, 3, 5, 7, larger primes); returns the count or -1
 // when more than `cap` factors would be needed.
@@ -759,6 +778,94 @@ bool fp32_split_twiddles() {
   return g_fp32_split == 1;
 }
 void set_fp32_split_twiddles(bool on) { g_fp32_split = on ? 1 : 0; }
+
+// FP32 stages whose tile is TB evenly spaced, contiguous lines in device memory load it by TMA
+// (P3DFFT_GB300_FP32_TMA=0 turns it off)
+static int g_fp32_tma = -1;
+bool fp32_tma() {
+  if (g_fp32_tma < 0) {
+    const char *e = getenv("P3DFFT_GB300_FP32_TMA");
+    g_fp32_tma = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_fp32_tma == 1;
+}
+void set_fp32_tma(bool on) { g_fp32_tma = on ? 1 : 0; }
+static std::atomic<int> g_tma_stall(0);
+void inject_tma_stall() { g_tma_stall = 1; }
+
+static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// Sets fa up for a TMA-staged load when the stage qualifies: FP32 C2C / R2C on a fast_tma_length,
+// lines contiguous (unit stride), 16-byte aligned device memory and line strides, and the tile's
+// lines evenly spaced: either all lines are (the other batch dim's stride is the tile dim's
+// times its size; partial last tile filled with zeros) or the tile dim is a multiple of the
+// tile's lines.
+static std::atomic<long long> g_tma_launches(0);
+long long tma_launches() { return g_tma_launches.load(); }
+static bool fast_tma_setup(FastArgs &fa, const void *in, DeviceTables *tabs) {
+  FParams &q = fa.p;
+  if (!fp32_tma() || !tabs || !tabs->status || (fa.kind != FK_C2C && fa.kind != FK_R2C) || !fast_tma_length(fa.n))
+    return false;
+  if (!q.load_Lmajor || q.iL != 1 || q.ffin || q.ffout || q.nlines <= 0) return false;
+  const int TB = fast_tile_lines(fa.n);
+  const long long esz = fa.kind == FK_R2C ? 4 : 8;  // R2C strides count reals, C2C complex points
+  const long long nout = (q.nlines + q.dt - 1) / q.dt;
+  long long d1, d2, s1, s2;
+  if (nout == 1 || q.io == q.it * q.dt) {  // every line evenly spaced
+    d1 = q.nlines;
+    d2 = 1;
+    s1 = q.it * esz;
+    s2 = s1 * d1;
+  } else if (q.dt % TB == 0 && q.nlines % q.dt == 0) {
+    d1 = q.dt;
+    d2 = nout;
+    s1 = q.it * esz;
+    s2 = q.io * esz;
+  } else {
+    return false;
+  }
+  if (d1 > 0x7fffffffLL || s1 % 16 || s2 % 16 || reinterpret_cast<uintptr_t>(in) % 16 || s1 < 8 * fa.n) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, in) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type != cudaMemoryTypeDevice) return false;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+  if (!enc) return false;
+  const int fl = 2 * fa.n, boxw = fl <= 256 ? fl : 256;
+  cuuint64_t dims[3] = {(cuuint64_t)fl, (cuuint64_t)d1, (cuuint64_t)d2};
+  cuuint64_t strides[2] = {(cuuint64_t)s1, (cuuint64_t)s2};
+  cuuint32_t box[3] = {(cuuint32_t)boxw, (cuuint32_t)TB, 1u};
+  cuuint32_t estr[3] = {1u, 1u, 1u};
+  if (enc(&fa.tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(in), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  // a stall injected for the failure-path test: 16 bytes more than the copies deliver, so the
+  // tile's wait runs out after 20 ms
+  const bool stall = g_tma_stall.exchange(0) != 0;
+  q.tma_extra = stall ? 16 : 0;
+  q.tma_timeout_ns = stall ? 20000000LL : 1000000000LL;
+  q.status = tabs->status;
+  q.tma_d1 = (int)d1;
+  fa.tma = 1;
+  g_tma_launches++;
+  return true;
+}
 
 template <class O, class E>
 static int launch_k(const KParams &p, size_t smem, int grid, int threads, cudaStream_t st) {
@@ -1040,11 +1147,17 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.fi_o = d.mi[o];
     q.fo_t = d.mo[t];
     q.fo_o = d.mo[o];
+    q.tma_timeout_ns = 0;
+    q.tma_extra = 0;
+    q.tma_d1 = 0;
+    q.status = nullptr;
+    fa.tma = 0;
     if (fast_prep) {
       *fast_prep = fa;
       return E_OK;
     }
     if (q.ntotal == 0) return E_OK;
+    if (d.prec == 4) fast_tma_setup(fa, in, tabs);
     const int rc = launch_fast(d.prec, arith, fa, stream);
     if (rc == E_OK && kernels_launched) (*kernels_launched)++;
     return rc;

@@ -61,6 +61,8 @@ def lib():
         "p3dfft_clear_error": ([], None),
         "p3dfft_gb300_set_stream": ([vp], None), "p3dfft_gb300_set_sync": ([ctypes.c_int], None),
         "p3dfft_gb300_set_host_direct": ([ctypes.c_int], None),
+        "p3dfft_gb300_set_host_pipeline": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_host_pipeline": ([], ctypes.c_int),
         "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
         "p3dfft_gb300_set_reference_compat": ([ctypes.c_int], None),
         "p3dfft_gb300_get_reference_compat": ([], ctypes.c_int),
@@ -68,6 +70,11 @@ def lib():
         "p3dfft_gb300_get_ff_intermediates": ([], ctypes.c_int),
         "p3dfft_gb300_set_fp32_split_twiddles": ([ctypes.c_int], None),
         "p3dfft_gb300_get_fp32_split_twiddles": ([], ctypes.c_int),
+        "p3dfft_gb300_set_fp32_tma": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_fp32_tma": ([], ctypes.c_int),
+        "p3dfft_gb300_device_status": ([ctypes.c_int], ctypes.c_int),
+        "p3dfft_gb300_inject_tma_stall": ([], None),
+        "p3dfft_gb300_tma_launch_count": ([], ctypes.c_longlong),
         "p3dfft_gb300_plan3d": ([ip, ip, ip, ctypes.c_int, ip, ip, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_exec3d": ([ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "p3dfft_gb300_destroy3d": ([ctypes.c_int], ctypes.c_int),
@@ -174,6 +181,30 @@ def set_fp32_split_twiddles(on: bool):
     lib().p3dfft_gb300_set_fp32_split_twiddles(1 if on else 0)
 
 
+def set_fp32_tma(on: bool):
+    """FP32 C2C / R2C stages with contiguous lines load their tiles by TMA (True, the default)
+    or by per-thread global loads (False)."""
+    lib().p3dfft_gb300_set_fp32_tma(1 if on else 0)
+
+
+def get_fp32_tma() -> bool:
+    return bool(lib().p3dfft_gb300_get_fp32_tma())
+
+
+def device_status(clear: bool = True) -> int:
+    """Nonzero after a kernel's bounded wait ran out (synchronous); clear resets it."""
+    return int(lib().p3dfft_gb300_device_status(1 if clear else 0))
+
+
+def tma_launch_count() -> int:
+    return int(lib().p3dfft_gb300_tma_launch_count())
+
+
+def inject_tma_stall():
+    """Test hook: the next TMA-staged launch's waits run out (20 ms) and set the status word."""
+    lib().p3dfft_gb300_inject_tma_stall()
+
+
 def get_reference_compat() -> bool:
     return bool(lib().p3dfft_gb300_get_reference_compat())
 
@@ -187,6 +218,16 @@ def set_host_direct(on):
     "out" for one side only) or staged through HBM (False)."""
     mode = {True: 1, False: 0, "in": 2, "out": 3}[on]
     lib().p3dfft_gb300_set_host_direct(mode)
+
+
+def set_host_pipeline(on: bool):
+    """Staged host copies overlapped with the first / last two stages, slab by slab (True, the
+    default) or with the first / last stage only (False)."""
+    lib().p3dfft_gb300_set_host_pipeline(1 if on else 0)
+
+
+def get_host_pipeline() -> bool:
+    return bool(lib().p3dfft_gb300_get_host_pipeline())
 
 
 def set_stream(stream_ptr: int):
