@@ -159,6 +159,15 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------------------------
+def workload_config(world):
+    """The workload both arms run (the GPU line and the CPU reference line carry the same dict)."""
+    return {"workload": WORKLOAD, "grid": list(GD), "types_forward": "R2C_D,CFFT_FORWARD_D,CFFT_FORWARD_D",
+            "types_backward": "C2R_D,CFFT_BACKWARD_D,CFFT_BACKWARD_D", "deriv": "d/dz fused",
+            "l2": "inputs larger than L2 (1.07 GB real field, 1.08 GB spectrum); no flush",
+            "input": "numpy PCG64 U[-1,1) seed 512+rank", "parallelism": f"replicas x{world}",
+            "algorithmic_bytes_per_step": ALG_BYTES}
+
+
 def run_reference(args, rank, world):
     """CPU reference arm: the oracle port of the reference path on all host cores."""
     if rank != 0:
@@ -173,7 +182,8 @@ def run_reference(args, rank, world):
         for st in pyoracle.OraclePlan(types, g1, m1, g2, m2, d1, d2).stages():
             run, b_in, b_out, nlines = pyoracle.stage_lines_runner(st, nthreads=cores)
             runners.append((run, b_in, b_out, nlines, st["dim"] == idir))
-    frac = float(os.environ.get("P3D_REF_SAMPLE", "0.0625"))
+    # every line of every stage by default: each step is the whole round trip
+    frac = float(os.environ.get("P3D_REF_SAMPLE", "1.0"))
 
     def step():
         nb = 0
@@ -191,12 +201,13 @@ def run_reference(args, rank, world):
         nbytes += step()
     dt = time.perf_counter() - t0
     value = nbytes / dt / 1e9
-    sample = (f"{frac:.4f} of the lines of each of the 6 stages of the {GD[0]}x{GD[1]}x{GD[2]} round trip per step "
-              f"(oracle C port, OpenMP {cores} threads)")
+    sample = (("all" if frac >= 1 else f"{frac:.4f} of the") +
+              f" lines of each of the 6 stages of the {GD[0]}x{GD[1]}x{GD[2]} round trip per step "
+              f"(oracle C port of the reference path, IEEE double, OpenMP {cores} threads)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": sample},
+            "config": workload_config(world), "fp64_arith": "IEEE double (CPU)",
             "cpu_baseline": {"value": value, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -795,6 +806,17 @@ def main():
     ms_step = max_over_ranks(ms / args.steps)
     value = ALG_BYTES * world / (ms_step * 1e-3) / 1e9
     clocks = clk.summary()
+    # the distribution of single steps (a separate run of the same steps, an event at each step
+    # boundary)
+    nper = max(1, min(args.steps, 40))
+    L.p3dfft_gb300_synchronize()
+    L.p3dfft_gb300_event_record(10)
+    for i in range(nper):
+        step(d_in.ptr, d_out.ptr)
+        L.p3dfft_gb300_event_record(11 + i)
+    per_step = sorted(L.p3dfft_gb300_event_elapsed_ms(10 + i, 11 + i) for i in range(nper))
+    step_dist = {"steps": nper, "median_ms": float(np.median(per_step)),
+                 "p10_ms": float(np.percentile(per_step, 10)), "p90_ms": float(np.percentile(per_step, 90))}
 
     # ---- full-size properties: normalised round trip recovers the derivative field ----
     y = np.empty(p3d.storage_shape(GD, MO1), np.float64)
@@ -835,6 +857,10 @@ def main():
                 "launches_per_step": dk["launches"], "bytes_per_launch": dk["bytes"] // dk["launches"],
                 "ms_per_launch": dk["ms"] / dk["launches"], "step_share": dk["ms"] / sum(s["ms"] for s in stages),
                 "whole_step_frac": value / world / peak,
+                # compulsory traffic (each real field and each spectrum once: 2*S_r + 2*S_c) over
+                # the step time, against the peak
+                "compulsory_bytes_per_step": 2 * S_R + 2 * S_C,
+                "compulsory_frac": (2 * S_R + 2 * S_C) / (ms_step * 1e-3) / 1e9 / peak,
                 "stages_ms": [round(s["ms"], 4) for s in stages]}
     # float-float kernels are compute-side bound: instruction issue (warp instructions per launch,
     # ncu count per point x the launch's points, over the live duration, against 4 per SM per
@@ -947,10 +973,14 @@ def main():
         p3d.set_ff_intermediates(False)
         ms_ieee = timed(f.handle, b.handle, d_in.ptr, d_spec.ptr, d_out.ptr, max(5, args.steps // 5))
         y_ieee = d_out.download(np.empty_like(y))
+        mf, mb = (ctypes.c_double * 8)(), (ctypes.c_double * 8)()
+        nf = L.p3dfft_gb300_profile_stages(f.handle, ctypes.c_void_p(d_in.ptr), ctypes.c_void_p(d_spec.ptr), IDIR, 5, mf, 8)
+        nb = L.p3dfft_gb300_profile_stages(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(d_out.ptr), -1, 5, mb, 8)
         p3d.set_ff_intermediates(True)
         forms["fp64_float_float_ieee_intermediates"] = {
             "ms_per_step": ms_ieee, "value": ALG_BYTES / (ms_ieee * 1e-3) / 1e9, "unit": "GB/s",
-            "rel_l2_vs_headline": float(np.linalg.norm(y_ieee - y) / np.linalg.norm(y))}
+            "rel_l2_vs_headline": float(np.linalg.norm(y_ieee - y) / np.linalg.norm(y)),
+            "stages_ms": [round(v, 4) for v in list(mf)[:max(nf, 0)] + list(mb)[:max(nb, 0)]]}
     p3d.set_fp64_arith(1 - arith)
     ms_other = timed(f.handle, b.handle, d_in.ptr, d_spec.ptr, d_out.ptr, max(3, args.steps // 10))
     y_other = d_out.download(np.empty_like(y))
@@ -1012,13 +1042,10 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": list(GD), "types_forward": "R2C_D,CFFT_FORWARD_D,CFFT_FORWARD_D",
-                       "types_backward": "C2R_D,CFFT_BACKWARD_D,CFFT_BACKWARD_D", "deriv": "d/dz fused",
-                       "fp64_arith": "float-float (FP32 pipe, ~48-bit)" if arith else "native FP64 (DFMA)",
-                       "l2": "inputs larger than L2 (1.07 GB real field, 1.08 GB spectrum); no flush",
-                       "input": "numpy PCG64 U[-1,1) seed 512+rank", "parallelism": f"replicas x{world}",
-                       "algorithmic_bytes_per_step": ALG_BYTES},
+            "config": workload_config(world),
+            "fp64_arith": "float-float (FP32 pipe, ~48-bit)" if arith else "native FP64 (DFMA)",
             "roofline": roofline, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+            "step_distribution": step_dist,
             "host_vs_device_rel_diff": rt_err, "parity": parity, "other_forms": forms}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()

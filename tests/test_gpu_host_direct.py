@@ -90,9 +90,11 @@ def test_large_staged_field_overlapped_in_slabs(gpu, oracle):
     assert np.array_equal(z, d_out.download(np.empty_like(z)))
 
 
-@pytest.mark.parametrize("prec,mo1,mo2", [(8, (0, 1, 2), (1, 2, 0)), (8, (2, 0, 1), (0, 1, 2)),
-                                          (4, (0, 1, 2), (1, 2, 0))])
-def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2):
+# (the (2,0,1) input layout has the x dim slowest: the x stage cannot be cut into slabs there,
+# so that plan runs stage after stage either way)
+@pytest.mark.parametrize("prec,mo1,mo2,sliced", [(8, (0, 1, 2), (1, 2, 0), True), (8, (2, 0, 1), (0, 1, 2), False),
+                                                 (4, (0, 1, 2), (1, 2, 0), True)])
+def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2, sliced):
     """Page-locked host input and output of a 3D round trip (fields over the 32 MB threshold,
     d/dz fused), read / written directly by the kernels, or staged through HBM by per-slab
     copies with the first two / last two stages pipelined behind them slab by slab (or, with
@@ -129,7 +131,10 @@ def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2):
         p3d.set_host_pipeline(True)
         p3d.set_host_direct(True)
     assert res[True, True][2] == res[True, False][2]  # direct host access: stage after stage
-    assert res[False, True][2] > res[False, False][2] > 6  # staged: the stage pairs ran in slabs
+    if sliced:  # staged: the stage pairs (pipelining on) or the end stages (off) ran in slabs
+        assert res[False, True][2] > res[False, False][2] > res[True, True][2]
+    else:
+        assert res[False, True][2] == res[False, False][2] == res[True, True][2]
     d_in, d_out = p3d.DeviceArray(x.nbytes), p3d.DeviceArray(x.nbytes)
     d_in.upload(x)
     f.exec(d_in, d_s, idir=2)
