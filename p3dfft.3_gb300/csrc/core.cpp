@@ -997,10 +997,14 @@ static void stage_ff_capable(const Plan *P, const Stage &st, const void *src, vo
 
 // Scale index of an intermediate field of grid g stored by lines along dim A: coordinate
 // multipliers over the two other dims (ascending), 0 along A.
-static void ff_multipliers(const GridDesc &g, int A, long long m[3]) {
+static void ff_multipliers(const GridDesc &g, int A, int B, long long m[3]) {
+  // B (the consuming stage's transform dim) varies fastest, so that the consumer's loads of the
+  // scales of one line's points are contiguous; its other dim is the producer's tile dim in the
+  // usual schedules, so the producer's stores of its lines' scales are contiguous too
   int d1 = -1, d2 = -1;
   for (int d = 0; d < 3; d++)
     if (d != A) (d1 < 0 ? d1 : d2) = d;
+  if (B == d2) std::swap(d1, d2);
   m[A] = 0;
   m[d1] = 1;
   m[d2] = g.gdims[d1];
@@ -1254,7 +1258,7 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
         if (!ensure_buf(&B.side[k], &B.side_bytes[k], bytes)) return E_CUDA;
       }
       long long m[3];
-      ff_multipliers(st.g2, st.dim, m);
+      ff_multipliers(st.g2, st.dim, P->ex[s + 1].dim, m);
       ffl[s].ffout = 1;
       ffl[s].sout = static_cast<int *>(B.side[k]);
       ffl[s + 1].ffin = 1;

@@ -600,8 +600,9 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
 
     // float-float input: producer-line scale of point j of this thread's line
     constexpr bool ffin = O::SCALED && (KIND == FK_C2C || KIND == FK_C2R) && (FF & 1);
-    const long long sib = ffin ? (long long)(gl % p.dt) * p.fi_t + (long long)(gl / p.dt) * p.fi_o : 0;
-    auto sp_of = [&](int j) -> int { return __ldg(p.sin + sib + (long long)j * p.fi_j); };
+    // (32-bit indices: a side array holds one scale per line, fewer than 2^31 - the launch checks)
+    const int sib = ffin ? (gl % p.dt) * (int)p.fi_t + (gl / p.dt) * (int)p.fi_o : 0;
+    auto sp_of = [&](int j) -> int { return __ldg(p.sin + (sib + j * (int)p.fi_j)); };
     // the scales of this thread's points, loaded with the points and kept in registers for the
     // conversion (a second load there would put an L2 round trip after the block reduction)
     int spv[V > 0 ? V : 1] = {};  // per-slot input line scales (float-float input only)

@@ -1092,6 +1092,11 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
        (d.ffin && d.kind == K_R2C) ||
        (d.ffout && d.kind == K_C2R) || !(d.kind == K_C2C_FWD || d.kind == K_C2C_BWD || d.kind == K_R2C || d.kind == K_C2R)))
     return E_UNSUPPORTED;
+  if (d.ffin || d.ffout) {  // the kernels index the scale arrays with 32-bit offsets
+    long long span = 0;
+    for (int i = 0; i < 3; i++) span += (long long)(d.d1[i] - 1) * std::max(d.mi[i], d.mo[i]);
+    if (span >= 0x7fffffffLL) return E_UNSUPPORTED;
+  }
 
   if (use_fast) {
     FastArgs fa;
