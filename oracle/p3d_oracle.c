@@ -568,6 +568,8 @@ int orc_exec_stage_lines(const orc_stage *S, const double *in, double *out, int 
   nin = S->g1.gdims[L];
   nout = S->g2.gdims[L];
   nlog = (kind == ORC_K_C2R) ? nout : nin; /* transplan::init_tr, templ.C:933-960 */
+  /* an empty line (e.g. the reference's C2R output length 2(M-1) for M = 1, templ.C:274-277) */
+  if (nin <= 0 || nout <= 0) return -3;
   if (kind == ORC_K_R2C && nout != nin / 2 + 1) return -3;
   if (kind == ORC_K_C2R && nin != nout / 2 + 1) return -3;
   if ((kind != ORC_K_R2C && kind != ORC_K_C2R) && nin != nout) return -3;

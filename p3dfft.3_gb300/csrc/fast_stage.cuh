@@ -71,6 +71,13 @@ struct FParams {
   int *status;
 };
 
+// Float-float C2R: form the half-length packing pairwise (k, N-k) before the first pass (1:
+// half the twiddle products; measured 0.851 -> 0.848 ms at 512^3), or per point as the first pass
+// reads (0; kept for FP32, where the extra shared-memory round trip cost 7%)
+#ifndef FAST_C2R_PAIRS
+#define FAST_C2R_PAIRS 1
+#endif
+
 // resident 256-thread CTAs per SM the register allocation is sized for (FP64 and float-float;
 // FP32 kernels, with half-width values, can afford more resident CTAs)
 #ifndef FAST_MIN_BLOCKS
@@ -793,8 +800,33 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     }
     fk_sync<TT>(sid);
 
-    // ---------------- FFT (C2R: the half-length packing is formed as the first pass reads) ----
-    fk_pass<O, N, TWSTEP, 1, 0, KIND == FK_C2R>(lb, tab, ptab, j0, act, fsign, sid);
+    // ---------------- FFT (C2R: the half-length packing first) ----
+    if constexpr (KIND == FK_C2R && FAST_C2R_PAIRS && O::SCALED) {
+      // Z[k] = s + t and Z[N-k] = conj(s - t) from the pair X[k], X[N-k]: s = X[k] + conj X[N-k],
+      // t = i conj(W_2N^k) (X[k] - conj X[N-k]); one twiddle product per pair, in place
+      // (imaginary parts of X[0], X[N] ignored; slot N keeps a value no pass reads)
+      if (act) {
+#pragma unroll 1
+        for (int k = j0; k <= N / 2; k += TT) {
+          const int pk = fk_pos<PS>(k), pm = fk_pos<PS>(N - k);
+          C xa = lb[pk], xb = lb[pm];
+          if (k == 0) {
+            xa = O::mk(O::re(xa), O::rzero());
+            xb = O::mk(O::re(xb), O::rzero());
+          }
+          const C xbc = O::conj(xb);
+          const C sv = O::add(xa, xbc), dv = O::sub(xa, xbc);
+          const C tv = O::muli(O::mul(dv, O::conj(O::tw(tab, k))));
+          lb[pk] = O::norm(O::add(sv, tv));
+          if (2 * k != N) lb[pm] = O::norm(O::conj(O::sub(sv, tv)));
+        }
+      }
+      fk_sync<TT>(sid);
+      fk_pass<O, N, TWSTEP, 1, 0, false>(lb, tab, ptab, j0, act, fsign, sid);
+    } else {
+      // (the half-length packing formed as the first pass reads)
+      fk_pass<O, N, TWSTEP, 1, 0, KIND == FK_C2R>(lb, tab, ptab, j0, act, fsign, sid);
+    }
     // the scale of the line this thread stores (the store may map threads to other lines)
     if constexpr (O::SCALED) sc_out = perline ? 1043 - lfin[ls] : sc;
     }
@@ -821,7 +853,7 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
       const int pjs = fk_pos<PS>(js), pns = fk_pos<PS>(N - js);
       // float-float output: values at this line's scale, the scale beside them
       constexpr bool ffout = O::SCALED && (KIND == FK_C2C || KIND == FK_R2C) && (FF & 2);
-      if (ffout && js == 0) p.sout[(long long)(gs % p.dt) * p.fo_t + (long long)(gs / p.dt) * p.fo_o] = sc_out;
+      if (ffout && js == 0) p.sout[(gs % p.dt) * (int)p.fo_t + (gs / p.dt) * (int)p.fo_o] = sc_out;
       auto store_c = [&](G *ptr, C v) {
         if constexpr (ffout) O::stff(ptr, v);
         else O::straw(ptr, O::to_raw(v, sc_out));

@@ -1,6 +1,6 @@
-"""CPU: host-side runtime pieces that need no GPU — the tuning-cache file format, and the batch,
-serving and tuning entry points failing loudly (not silently computing on the CPU) without a
-device."""
+"""CPU: host-side runtime pieces that need no GPU — the tuning-cache file format, plans the
+library must refuse, and the batch, serving and tuning entry points failing loudly (not silently
+computing on the CPU) without a device."""
 import ctypes
 
 import pytest
@@ -50,3 +50,18 @@ def test_runtimes_fail_loudly_without_device(p3d):
     assert L.p3dfft_gb300_preload_kernels() == 4
     L.p3dfft_clear_error()
     L.p3dfft_gb300_batch_destroy(b)
+
+
+@pytest.mark.parametrize("bad", [(0, 4, 4), (4, 0, 4), (4, 4, -1)])
+def test_empty_grid_is_rejected_at_plan_time(p3d, bad):
+    with pytest.raises(p3d.P3DFFTError, match="BAD_ARG"):
+        p3d.Transform3D([p3d.CFFT_FORWARD_D] * 3, bad, (0, 1, 2), bad, (0, 1, 2), -1, -1)
+
+
+def test_c2r_to_real_length_one_is_rejected_at_plan_time(p3d):
+    """A C2R from one complex point to one real point: the reference sizes the C2R output
+    2(M-1) = 0 from M = 1 complex points (templ.C:274-277), a zero-length stage; the library
+    refuses the plan, naming the mismatch."""
+    with pytest.raises(p3d.P3DFFTError, match="PLAN"):
+        p3d.Transform3D([p3d.C2RFFT_D, p3d.CFFT_BACKWARD_D, p3d.CFFT_BACKWARD_D], (1, 4, 4), (0, 1, 2),
+                        (1, 4, 4), (0, 1, 2), 0, -1)
