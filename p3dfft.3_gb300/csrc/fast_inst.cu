@@ -20,7 +20,7 @@ using FastArith = Native<double>;
 #elif P3D_FAST_ARITH == 2
 using FastArith = Native<float>;
 #else
-using FastArith = NativeFS<false>;  // FP32 with split twiddles, long lines only
+using FastArith = FSplit;  // FP32 with split twiddles, long lines only
 #endif
 
 static_assert(P3D_FAST_PART < fast_nparts<FastArith>(), "part out of range for this arithmetic");

@@ -71,6 +71,15 @@ struct FParams {
   int *status;
 };
 
+// The FP32 split-twiddle policy the build instantiates: twiddle powers read from the tables
+// (FAST_FS_CHAIN 0, the default) or chained in float-float from W^1 (1: same accuracy, but the
+// 512^3 FP32 round trip measured 1.680 against 1.362 ms - the float-float products and the lower
+// occupancy they need, 6 CTAs of 40 registers, cost more than the table loads they save)
+#ifndef FAST_FS_CHAIN
+#define FAST_FS_CHAIN 0
+#endif
+using FSplit = NativeFS<FAST_FS_CHAIN != 0>;
+
 // Float-float C2R: form the half-length packing pairwise (k, N-k) before the first pass (1:
 // half the twiddle products; measured 0.851 -> 0.848 ms at 512^3), or per point as the first pass
 // reads (0; kept for FP32, where the extra shared-memory round trip cost 7%)
@@ -338,6 +347,16 @@ __device__ __forceinline__ void fk_pass(typename O::C *line, const typename O::T
           }
 #pragma unroll
           for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], w[r]);
+        } else if constexpr (O::TW_CHAIN) {
+          // W^1 from the table, W^r = W^(r-1) W^1 formed one at a time
+          const typename O::W w1 = fk_tw<O>(pt, 0, sign);
+          typename O::W w = w1;
+          v[b * R + 1] = O::mul(v[b * R + 1], w1);
+#pragma unroll
+          for (int r = 2; r < R; r++) {
+            w = O::wmul(w, w1);
+            v[b * R + r] = O::mul(v[b * R + r], w);
+          }
         } else {
 #pragma unroll
           for (int r = 1; r < R; r++) v[b * R + r] = O::mul(v[b * R + r], fk_tw<O>(pt, (r - 1) * Ns, sign));
@@ -407,8 +426,10 @@ __device__ __forceinline__ typename O::C fk_deriv(const FParams &p, typename O::
 
 template <class O, int N>
 __host__ __device__ constexpr int fast_min_blocks() {
-  return sizeof(typename O::C) <= 8 ? (fast_max_values(N) > 8 ? FAST_MIN_BLOCKS_FP32 * 3 / 4 : FAST_MIN_BLOCKS_FP32)
-                                    : FastShape<N>::MINB;
+  // (the chained split twiddles hold two float-float twiddles: 6 CTAs of 40 registers)
+  return sizeof(typename O::C) <= 8
+             ? ((fast_max_values(N) > 8 || O::TW_CHAIN) ? FAST_MIN_BLOCKS_FP32 * 3 / 4 : FAST_MIN_BLOCKS_FP32)
+             : FastShape<N>::MINB;
 }
 
 // A launch over the tiles of several stages of independent transforms that share the kernel
@@ -443,7 +464,7 @@ __host__ __device__ constexpr bool fast_tma_length(int n) {
 }
 template <class O, int KIND, int N>
 __host__ __device__ constexpr bool fk_tma_variant() {
-  return (std::is_same_v<O, Native<float>> || std::is_same_v<O, NativeFS<false>>) &&
+  return (std::is_same_v<O, Native<float>> || std::is_same_v<O, FSplit>) &&
          (KIND == FK_C2C || KIND == FK_R2C) && fast_tma_length(N);
 }
 // mbarrier phase wait bounded by the global timer: false after limit_ns
@@ -1147,7 +1168,7 @@ P3D_FAST_DECL_KINDS(DFP, 0)
 P3D_FAST_DECL_KINDS(DFP, 1)
 P3D_FAST_DECL_KINDS(Native<double>, 0)
 P3D_FAST_DECL_KINDS(Native<float>, 0)
-P3D_FAST_DECL_KINDS(NativeFS<false>, 0)
+P3D_FAST_DECL_KINDS(FSplit, 0)
 #undef P3D_FAST_DECL_KINDS
 #undef P3D_FAST_DECL
 
@@ -1191,7 +1212,7 @@ inline int fast_preload(int prec, int arith) {
     int r;
     if (prec == 4) {
       r = fast_launch_arith<Native<float>>(a, nullptr, 0, 0);
-      const int r2 = fast_launch_arith<NativeFS<false>>(a, nullptr, 0, 0);
+      const int r2 = fast_launch_arith<FSplit>(a, nullptr, 0, 0);
       if (r2 != E_OK) r = r2;
     } else if (arith == AR_DF) r = fast_launch_arith<DFP>(a, nullptr, 0, 0);
     else r = fast_launch_arith<Native<double>>(a, nullptr, 0, 0);
@@ -1205,7 +1226,7 @@ inline int fast_preload(int prec, int arith) {
 inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, const FGroup *g = nullptr,
                        int ctas = 0) {
   if (prec == 4) {
-    if (a.split) return fast_launch_arith<NativeFS<false>>(a, g, ctas, st);
+    if (a.split) return fast_launch_arith<FSplit>(a, g, ctas, st);
     return fast_launch_arith<Native<float>>(a, g, ctas, st);
   }
   if (arith == AR_DF) return fast_launch_arith<DFP>(a, g, ctas, st);

@@ -105,6 +105,7 @@ struct Native {
   // FP32: build most pass twiddles as products of two table entries (fewer loads through L1,
   // the FP32 kernels' bottleneck; at most two roundings more per twiddle)
   static constexpr bool TW_POWERS = sizeof(R) == 4 && FAST_TW_POWERS_FP32;
+  static constexpr bool TW_CHAIN = false;
   // product of two twiddles (twiddle powers formed in registers)
   static __device__ __forceinline__ C wmul(C a, C b) { return mul(a, b); }
   using RAW = cx<R>;
@@ -150,11 +151,12 @@ struct Native {
 // FP32 data with split twiddles (the specialised kernels on long lines): each twiddle is the pair
 // (hi, lo) of FP32 values whose sum is its long-double value to ~48 bits (table format 2), and a
 // product a * w is formed as a * hi + (a * lo), the small term first, so the twiddle adds no
-// rounding of its own beyond that of the product ("compensated" twiddle products).  POW = false
-// (the one instantiated): every twiddle is read from the tables; POW = true forms the powers as
-// float-float products of two loaded twiddles instead, which measured 20% slower at 512 points
-// (register spills at the FP32 kernels' 32-register budget) against 10% for the loads.
-template <bool POW>
+// rounding of its own beyond that of the product ("compensated" twiddle products).  CHAIN = false
+// reads every pass twiddle W^r (r = 1 .. R-1) from the tables; CHAIN = true reads W^1 and forms
+// W^r = W^(r-1) W^1 as float-float products, one at a time (two twiddles live, ~2^-44 relative
+// after the six products of a radix-8 butterfly, far below the FP32 data's 2^-24), trading the
+// table loads through the L1 data path, which bounds the FP32 kernels, for FMA-pipe work.
+template <bool CHAIN>
 struct NativeFS : Native<float> {
   using T = cff;
   using W = cff;
@@ -172,7 +174,8 @@ struct NativeFS : Native<float> {
   }
   static __device__ __forceinline__ S wre(const W &w) { return w.x.hi; }
   static __device__ __forceinline__ S wim(const W &w) { return w.y.hi; }
-  static constexpr bool TW_POWERS = POW;
+  static constexpr bool TW_POWERS = false;
+  static constexpr bool TW_CHAIN = CHAIN;
   static __device__ __forceinline__ W wmul(const W &a, const W &b) { return cff_mul(a, b); }
 };
 
@@ -293,6 +296,7 @@ struct DFP {
   static constexpr bool SCALED = true;
   static constexpr int IO_UNROLL = FAST_IO_UNROLL_DF;
   static constexpr bool TW_POWERS = false;
+  static constexpr bool TW_CHAIN = false;
   using RAW = longlong2;
   static __device__ __forceinline__ RAW ldraw(const G *p) { return __ldg(reinterpret_cast<const longlong2 *>(p)); }
   static __device__ __forceinline__ RAW ldraw2(const G *p0, const G *p1) {

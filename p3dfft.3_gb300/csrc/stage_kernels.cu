@@ -159,7 +159,9 @@ __device__ void bfly_generic(const typename O::C *src, typename O::C *dst, int j
       C x = src[j + r * T];
       int m = r * unit + ((r * q) % R) * runit;  // twiddle * W_R^{rq}
       m %= nf;
-      acc = O::add(acc, O::mul(x, twid<O, B>(p, m, sign)));
+      // (normalised at every term: a float-float sum of R terms left unnormalised collects the
+      // rounding of every lo part, which cost 1e-12 relative at R = 2039)
+      acc = O::norm(O::add(acc, O::mul(x, twid<O, B>(p, m, sign))));
     }
     dst[base + q * Ns] = O::norm(acc);
   }
@@ -879,10 +881,11 @@ static int launch_k(const KParams &p, size_t smem, int grid, int threads, cudaSt
   return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
 }
 
-// Register engines available for a complex FFT length (power-of-two lengths 16..4096)
+// Register engines available for a complex FFT length (power-of-two lengths 16..2048: 8 points
+// per thread within k_stage's 256 threads)
 static bool fixed_engine_len(int n) {
   switch (n) {
-    case 16: case 32: case 64: case 128: case 256: case 512: case 1024: case 2048: case 4096: return true;
+    case 16: case 32: case 64: case 128: case 256: case 512: case 1024: case 2048: return true;
     default: return false;
   }
 }
@@ -898,7 +901,6 @@ static int launch_fixed(const KParams &p, size_t smem, int grid, int threads, cu
     case 512: return launch_k<O, FixedFFT<512, 8, 8, 8, 8>>(p, smem, grid, threads, st);
     case 1024: return launch_k<O, FixedFFT<1024, 8, 8, 8, 8, 2>>(p, smem, grid, threads, st);
     case 2048: return launch_k<O, FixedFFT<2048, 8, 8, 8, 8, 4>>(p, smem, grid, threads, st);
-    case 4096: return launch_k<O, FixedFFT<4096, 8, 8, 8, 8, 8>>(p, smem, grid, threads, st);
     default: return E_UNSUPPORTED;
   }
 }
@@ -1023,7 +1025,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   const int bM = blue_len(p.nfft);
   const bool use_blue = !use_fast && !tw_given && !tabs_out && !fast_prep && !generic_only &&
                         (d.engine == ENG_AUTO || d.engine == ENG_BLUESTEIN) && largest_prime_factor(p.nfft) > 16 &&
-                        bM <= (d.prec == 4 ? 4096 : 2048);
+                        bM <= (d.prec == 4 ? 8192 : 4096);  // two buffers of bM: 128 KB
   if (d.engine == ENG_BLUESTEIN && !use_blue) return E_UNSUPPORTED;
 
   // FP32 specialised kernels on long lines: split (compensated) twiddle products, tables in
@@ -1170,7 +1172,11 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   if (fast_prep) return E_UNSUPPORTED;
 
   const size_t csz = (d.prec == 4) ? 8 : 16;
-  const bool fixed = !use_blue && fixed_engine_len(p.nfft) && (d.engine == ENG_FIXED || (d.engine == ENG_AUTO && !generic_only));
+  // (k_stage runs at most 256 threads: two FFT lines of 2048 points per data line take the generic
+  // engine unless the register engine is asked for explicitly)
+  const bool fixed_fits = (p.nfft / (p.nfft == 16 ? 4 : 8)) * p.nfl <= 256;
+  const bool fixed = !use_blue && fixed_engine_len(p.nfft) &&
+                     (d.engine == ENG_FIXED || (d.engine == ENG_AUTO && !generic_only && fixed_fits));
   int slots = p.nfft;
   if (use_blue) slots = std::max(slots, bM);
   if (p.nin > slots) slots = p.nin;
@@ -1188,10 +1194,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     TB = std::max(1, 256 / (T * p.nfl));
     while (TB > 1 && per_line * TB > smem_cap) TB /= 2;
     threads = TB * p.nfl * T;
-    if (threads > 1024 || threads < 32) {
-      // fall back to the generic engine for shapes the register engine cannot tile
-      return E_UNSUPPORTED;
-    }
+    if (threads > 256 || threads < 32) return E_UNSUPPORTED;  // k_stage runs at most 256 threads
   } else if (!p.load_Lmajor || !p.store_Lmajor) {
     int esz = (int)((p.in_complex ? 2 : 1) * d.prec);
     TB = std::max(2, 64 / esz);

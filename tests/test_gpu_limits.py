@@ -1,9 +1,10 @@
 """GPU: the edges of the supported sizes.
 
-- The longest lines a stage takes (6144 points FP64, 12288 FP32; the largest prime below the
-  FP64 limit, 6143, runs on the Bluestein engine) against the CPU oracle (1e-12 relative L2 in
-  FP64, 5e-6 in FP32), and one point more rejected with P3DFFT_ERR_TOO_LARGE, leaving the
-  library usable.
+- Long lines against the CPU oracle (1e-12 relative L2 in FP64, 5e-6 in FP32): the longest a
+  stage takes (6144 points FP64, 12288 FP32), 4096 and 8192 points (past the register engine),
+  primes on the Bluestein engine at its largest convolution (2039 FP64, 4093 FP32) and primes
+  past it on the generic radix engine (4093 and 6143 FP64, one DFT of the whole line); one point
+  past the limit rejected with P3DFFT_ERR_TOO_LARGE, leaving the library usable.
 - Degenerate 3D grids (dims of 1 and 2 in every position, R2C of length 1 and 2) against the
   oracle.
 (Plans the reference cannot form either, a zero dim or a C2R to a real length of 1, are rejected
@@ -29,7 +30,8 @@ def _line(p3d, oracle, tid_d, prec, n, lines=(3, 2)):
     return rel_l2(out, ref)
 
 
-@pytest.mark.parametrize("prec,n", [(8, 6144), (8, 6143), (4, 12288)])
+@pytest.mark.parametrize("prec,n", [(8, 6144), (8, 4096), (8, 2039), (8, 4093), (8, 6143), (4, 12288), (4, 8192),
+                                    (4, 4093)])
 def test_longest_lines_against_oracle(gpu, oracle, prec, n):
     p3d = gpu
     p3d.set_fp64_arith(1)
