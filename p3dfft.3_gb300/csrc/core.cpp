@@ -1036,8 +1036,8 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
     NS = e ? std::max(2, std::min(8, atoi(e))) : 8;
   }
   if (!g_pipe_stream) {
-    // the on-device stage's slabs get the highest priority, so that each starts as soon as its
-    // slab of the link-bound stage is written rather than queueing behind that stage's CTAs
+    // the second stage's slabs get the highest priority, so that each starts as soon as its slab
+    // of the first stage is written rather than queueing behind that stage's later slabs
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (cudaStreamCreateWithPriority(&g_pipe_stream, cudaStreamNonBlocking, hi) != cudaSuccess) return E_CUDA;
