@@ -213,27 +213,31 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_sample():
-    """Oracle port timed on a bounded sample (1/8 of the lines of every stage), all host cores."""
+def cpu_baseline_sample(reps=6):
+    """Oracle port timed on whole round trips (every line of every stage, about 10 s of CPU
+    work in all), all host cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
     cores = os.cpu_count() or 1
-    frac = 0.125
-    t_tot, b_tot = 0.0, 0.0
+    runners = []
     for types, g1, m1, d1, g2, m2, d2, idir in ((FWD, GD, MO1, -1, GD2, MO2, 0, IDIR),
                                                 (BWD, GD2, MO2, 0, GD, MO1, -1, -1)):
         for st in pyoracle.OraclePlan(types, g1, m1, g2, m2, d1, d2).stages():
             run, b_in, b_out, nlines = pyoracle.stage_lines_runner(st, nthreads=cores)
-            m = max(1, int(nlines * frac))
-            run(0, m, st["dim"] == idir)  # warm
-            t0 = time.perf_counter()
-            run(0, m, st["dim"] == idir)
-            t_tot += time.perf_counter() - t0
-            b_tot += (b_in + b_out) * m / nlines
+            runners.append((run, b_in + b_out, nlines, st["dim"] == idir))
+    for run, _, nlines, deriv in runners:  # warm: one pass over every stage
+        run(0, nlines, deriv)
+    t0 = time.perf_counter()
+    b_tot = 0.0
+    for _ in range(reps):
+        for run, nb, nlines, deriv in runners:
+            run(0, nlines, deriv)
+            b_tot += nb
+    t_tot = time.perf_counter() - t0
     return {"value": b_tot / t_tot / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
-            "sample": f"1/8 of the lines of each of the 6 stages of the {GD[0]}x{GD[1]}x{GD[2]} FP64 round trip "
-                      f"(CPU oracle port, OpenMP {cores} threads, {t_tot:.2f} s)"}
+            "sample": f"{reps} whole {GD[0]}x{GD[1]}x{GD[2]} FP64 round trips, every line of the 6 stages "
+                      f"(CPU oracle port of the reference path, OpenMP {cores} threads, {t_tot:.1f} s)"}
 
 
 def load_traffic(kernel_key):
