@@ -95,6 +95,12 @@ using FSplit = NativeFS<FAST_FS_CHAIN != 0>;
 #ifndef FAST_MIN_BLOCKS_FP32
 #define FAST_MIN_BLOCKS_FP32 8
 #endif
+// float-float / FP64 R2C and C2R kernels (the real-data pack / unpack costs registers: at 4 CTAs of
+// 64 registers they spill 16-28 bytes per thread; 3 CTAs of 80 registers remove the spills but
+// measured slower at 512^3: R2C 0.755 vs 0.720 ms, C2R 0.915 vs 0.847 ms)
+#ifndef FAST_MIN_BLOCKS_RC
+#define FAST_MIN_BLOCKS_RC FAST_MIN_BLOCKS
+#endif
 
 // The FFT lengths with a specialised kernel.
 #define P3D_FAST_LENGTHS(X)                                                                              \
@@ -424,12 +430,13 @@ __device__ __forceinline__ typename O::C fk_deriv(const FParams &p, typename O::
   return O::iscale(v, (k < p.dmid) ? k : k - p.dg);
 }
 
-template <class O, int N>
+template <class O, int N, int KIND = FK_C2C>
 __host__ __device__ constexpr int fast_min_blocks() {
   // (the chained split twiddles hold two float-float twiddles: 6 CTAs of 40 registers)
   return sizeof(typename O::C) <= 8
              ? ((fast_max_values(N) > 8 || O::TW_CHAIN) ? FAST_MIN_BLOCKS_FP32 * 3 / 4 : FAST_MIN_BLOCKS_FP32)
-             : FastShape<N>::MINB;
+             : ((KIND == FK_R2C || KIND == FK_C2R) && FAST_MIN_BLOCKS_RC < FastShape<N>::MINB ? FAST_MIN_BLOCKS_RC
+                                                                                       : FastShape<N>::MINB);
 }
 
 // A launch over the tiles of several stages of independent transforms that share the kernel
@@ -951,13 +958,13 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
 }
 
 template <class O, int KIND, int N, int FF = 0>
-__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>()) k_fast(FParams p) {
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIND>()) k_fast(FParams p) {
   fk_tile<O, KIND, N, FF>(p, blockIdx.x, p.in, p.out);
 }
 
 // The tile's input staged by the tensor-memory accelerator (fk_tma_variant lengths and kinds).
 template <class O, int KIND, int N>
-__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>())
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIND>())
     k_fast_tma(FParams p, const __grid_constant__ CUtensorMap tm) {
   if constexpr (fk_tma_variant<O, KIND, N>()) fk_tile<O, KIND, N, 0, true>(p, blockIdx.x, p.in, p.out, &tm);
 }
@@ -976,7 +983,7 @@ inline bool fast_ff_length(int n) { return n == 64 || n == 128 || n == 256 || n 
 // than the list makes the CTAs persistent (each walks the list with a grid stride).  No CTA waits
 // on another.
 template <class O, int KIND, int N>
-__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N>())
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIND>())
     k_fast_list(const FParams *plist, const FWork *work, int nwork) {
   __shared__ FParams sp;
   constexpr int NW = (int)(sizeof(FParams) / sizeof(int));
