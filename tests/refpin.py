@@ -282,8 +282,8 @@ def run_sample(name, target, workdir, timeout=300):
 
 
 def sample_passed(r, name):
-    """Exit status 0, no "incorrect" verdict, and at least one "Results are correct" verdict
-    (bench_c2c's final verdict line is commented out in its source: it needs its timing line)."""
+    """Exit status 0, no "incorrect" result line, and at least one "Results are correct" line
+    (bench_c2c's final result line is commented out in its source: it needs its timing line)."""
     out = r.stdout or ""
     if r.returncode != 0 or "incorrect" in out:
         return False

@@ -1,5 +1,5 @@
 """GPU: the drop-in programs in tests/programs (C++ API and C API flows of the reference's sample
-programs) compiled against include/ and run on the GPU; each prints the samples' verdict line
+programs) compiled against include/ and run on the GPU; each prints the samples' result line
 and exits 0 only when every check passes."""
 import os
 import shutil
