@@ -67,7 +67,9 @@ struct FParams {
   // for the failure-path test)
   long long tma_timeout_ns;
   int tma_extra;
-  int tma_d1;  // lines along the tensor map's second dim (line g at (g % tma_d1, g / tma_d1))
+  int tma_d1;    // lines along the tensor map's line dim (line g at (g % tma_d1, g / tma_d1))
+  int tma_mode;  // 1: lines contiguous (boxes of one line's floats x TB lines); 2: tile dim
+                 // contiguous (C2C: boxes of TB points' floats x rows of the line dim)
   int *status;
 };
 
@@ -463,6 +465,13 @@ struct FastTma {
   static constexpr int BOXW = FL <= 256 ? FL : 256;
   static constexpr int NBOX = FL / BOXW;
   static constexpr bool OK = FL <= 256 || FL % 256 == 0;
+  // tile-dim-contiguous tiles: boxes of BOXR rows (the largest divisor of N up to 256)
+  static constexpr int BOXR = [] {
+    int r = N < 256 ? N : 256;
+    while (N % r) r--;
+    return r;
+  }();
+  static constexpr int NBR = N / BOXR;
 };
 __host__ __device__ constexpr bool fast_tma_length(int n) {
   // even n: a box row of 2n floats is a multiple of 16 bytes
@@ -536,13 +545,25 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
                    : "memory");
       const int g0 = tile * TB, ct = g0 % p.tma_d1, co = g0 / p.tma_d1;
       const unsigned dst0 = (unsigned)__cvta_generic_to_shared(smem_raw);
+      if (p.tma_mode == 2) {
+        // rows r of the line dim, TB points of the tile dim each: element (line l, point j) at
+        // float 2 (j TB + l)
 #pragma unroll 1
-      for (int b = 0; b < TM::NBOX; b++)
-        asm volatile(
-            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-            "%4}], [%5];" ::"r"(dst0 + (unsigned)(b * TB * TM::BOXW * 4)),
-            "l"(reinterpret_cast<unsigned long long>(tm)), "r"(b * TM::BOXW), "r"(ct), "r"(co), "r"(tbar_addr)
-            : "memory");
+        for (int b = 0; b < TM::NBR; b++)
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4}], [%5];" ::"r"(dst0 + (unsigned)(b * TM::BOXR * TB * 8)),
+              "l"(reinterpret_cast<unsigned long long>(tm)), "r"(2 * ct), "r"(b * TM::BOXR), "r"(co), "r"(tbar_addr)
+              : "memory");
+      } else {
+#pragma unroll 1
+        for (int b = 0; b < TM::NBOX; b++)
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4}], [%5];" ::"r"(dst0 + (unsigned)(b * TB * TM::BOXW * 4)),
+              "l"(reinterpret_cast<unsigned long long>(tm)), "r"(b * TM::BOXW), "r"(ct), "r"(co), "r"(tbar_addr)
+              : "memory");
+      }
     }
     __syncthreads();
   }
@@ -671,10 +692,11 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
             const float *stg = reinterpret_cast<const float *>(smem_raw);
 #pragma unroll
             for (int e = 0; e < V; e++) {
-              const int f = 2 * (j0 + e * TT);  // point j = floats 2j, 2j + 1 of the line
-              x[e] = O::from_raw(
-                  *reinterpret_cast<const RAW *>(stg + (f / TM::BOXW) * (TB * TM::BOXW) + l * TM::BOXW + f % TM::BOXW),
-                  0);
+              const int j = j0 + e * TT;
+              const int f = 2 * j;  // point j = floats 2j, 2j + 1 of the line
+              const int off = p.tma_mode == 2 ? 2 * (j * TB + l)
+                                              : (f / TM::BOXW) * (TB * TM::BOXW) + l * TM::BOXW + f % TM::BOXW;
+              x[e] = O::from_raw(*reinterpret_cast<const RAW *>(stg + off), 0);
             }
           }
           __syncthreads();  // the first pass below overwrites the staged tile

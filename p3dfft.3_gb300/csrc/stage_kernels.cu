@@ -810,36 +810,73 @@ static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
   return fn;
 }
 
-// Sets fa up for a TMA-staged load when the stage qualifies: FP32 C2C / R2C on a fast_tma_length,
-// lines contiguous (unit stride), 16-byte aligned device memory and line strides, and the tile's
-// lines evenly spaced: either all lines are (the other batch dim's stride is the tile dim's
-// times its size; partial last tile filled with zeros) or the tile dim is a multiple of the
-// tile's lines.
+// Sets fa up for a TMA-staged load when the stage qualifies (FP32 C2C / R2C on a
+// fast_tma_length, 16-byte aligned device memory and strides):
+// - mode 1, lines contiguous (unit stride) and the tile's lines evenly spaced: either all lines
+//   are (the other batch dim's stride is the tile dim's times its size; a partial last tile is
+//   filled with zeros) or the tile dim is a multiple of the tile's lines;
+// - mode 2 (C2C), the tile dim contiguous and a multiple of the tile's (even) line count.
 static std::atomic<long long> g_tma_launches(0);
 long long tma_launches() { return g_tma_launches.load(); }
 static bool fast_tma_setup(FastArgs &fa, const void *in, DeviceTables *tabs) {
   FParams &q = fa.p;
   if (!fp32_tma() || !tabs || !tabs->status || (fa.kind != FK_C2C && fa.kind != FK_R2C) || !fast_tma_length(fa.n))
     return false;
-  if (!q.load_Lmajor || q.iL != 1 || q.ffin || q.ffout || q.nlines <= 0) return false;
+  if (q.ffin || q.ffout || q.nlines <= 0 || reinterpret_cast<uintptr_t>(in) % 16) return false;
   const int TB = fast_tile_lines(fa.n);
   const long long esz = fa.kind == FK_R2C ? 4 : 8;  // R2C strides count reals, C2C complex points
-  const long long nout = (q.nlines + q.dt - 1) / q.dt;
-  long long d1, d2, s1, s2;
-  if (nout == 1 || q.io == q.it * q.dt) {  // every line evenly spaced
-    d1 = q.nlines;
-    d2 = 1;
-    s1 = q.it * esz;
-    s2 = s1 * d1;
-  } else if (q.dt % TB == 0 && q.nlines % q.dt == 0) {
+  long long nout = (q.nlines + q.dt - 1) / q.dt;
+  cuuint64_t dims[3];
+  cuuint64_t strides[2];
+  cuuint32_t box[3];
+  int mode, d1;
+  if (q.load_Lmajor && q.iL == 1) {  // lines contiguous
+    long long n1, s1, s2;
+    if (nout == 1 || q.io == q.it * q.dt) {  // every line evenly spaced
+      n1 = q.nlines;
+      s1 = q.it * esz;
+      s2 = s1 * n1;
+      nout = 1;
+    } else if (q.dt % TB == 0 && q.nlines % q.dt == 0) {
+      n1 = q.dt;
+      s1 = q.it * esz;
+      s2 = q.io * esz;
+    } else {
+      return false;
+    }
+    if (n1 > 0x7fffffffLL || s1 % 16 || s2 % 16 || s1 < 8 * fa.n) return false;
+    const int fl = 2 * fa.n;
+    dims[0] = (cuuint64_t)fl;
+    dims[1] = (cuuint64_t)n1;
+    dims[2] = (cuuint64_t)nout;
+    strides[0] = (cuuint64_t)s1;
+    strides[1] = (cuuint64_t)s2;
+    box[0] = (cuuint32_t)(fl <= 256 ? fl : 256);
+    box[1] = (cuuint32_t)TB;
+    box[2] = 1u;
+    mode = 1;
+    d1 = (int)n1;
+  } else if (!q.load_Lmajor && q.it == 1 && fa.kind == FK_C2C && TB % 2 == 0 && q.dt % TB == 0 &&
+             q.nlines % q.dt == 0) {
+    // tile dim contiguous (C2C): rows of TB points along the tile dim (an even count, so that a
+    // row is a multiple of 16 bytes and starts on one), one row per point of the lines
+    const long long s1 = q.iL * 8, s2 = q.io * 8;
+    if (s1 % 16 || s2 % 16 || q.dt > 0x3fffffffLL) return false;
+    int boxr = fa.n < 256 ? fa.n : 256;
+    while (fa.n % boxr) boxr--;
+    dims[0] = (cuuint64_t)(2 * q.dt);
+    dims[1] = (cuuint64_t)fa.n;
+    dims[2] = (cuuint64_t)nout;
+    strides[0] = (cuuint64_t)s1;
+    strides[1] = (cuuint64_t)s2;
+    box[0] = (cuuint32_t)(2 * TB);
+    box[1] = (cuuint32_t)boxr;
+    box[2] = 1u;
+    mode = 2;
     d1 = q.dt;
-    d2 = nout;
-    s1 = q.it * esz;
-    s2 = q.io * esz;
   } else {
     return false;
   }
-  if (d1 > 0x7fffffffLL || s1 % 16 || s2 % 16 || reinterpret_cast<uintptr_t>(in) % 16 || s1 < 8 * fa.n) return false;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, in) != cudaSuccess) {
     cudaGetLastError();
@@ -848,22 +885,19 @@ static bool fast_tma_setup(FastArgs &fa, const void *in, DeviceTables *tabs) {
   if (at.type != cudaMemoryTypeDevice) return false;
   PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
   if (!enc) return false;
-  const int fl = 2 * fa.n, boxw = fl <= 256 ? fl : 256;
-  cuuint64_t dims[3] = {(cuuint64_t)fl, (cuuint64_t)d1, (cuuint64_t)d2};
-  cuuint64_t strides[2] = {(cuuint64_t)s1, (cuuint64_t)s2};
-  cuuint32_t box[3] = {(cuuint32_t)boxw, (cuuint32_t)TB, 1u};
   cuuint32_t estr[3] = {1u, 1u, 1u};
   if (enc(&fa.tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(in), dims, strides, box, estr,
           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
+  q.tma_mode = mode;
   // a stall injected for the failure-path test: 16 bytes more than the copies deliver, so the
   // tile's wait runs out after 20 ms
   const bool stall = g_tma_stall.exchange(0) != 0;
   q.tma_extra = stall ? 16 : 0;
   q.tma_timeout_ns = stall ? 20000000LL : 1000000000LL;
   q.status = tabs->status;
-  q.tma_d1 = (int)d1;
+  q.tma_d1 = d1;
   fa.tma = 1;
   g_tma_launches++;
   return true;
@@ -1157,6 +1191,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.tma_timeout_ns = 0;
     q.tma_extra = 0;
     q.tma_d1 = 0;
+    q.tma_mode = 0;
     q.status = nullptr;
     fa.tma = 0;
     if (fast_prep) {

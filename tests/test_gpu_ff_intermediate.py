@@ -57,6 +57,34 @@ def test_round_trip_against_oracle_and_ieee_intermediates(ff, oracle, gd):
         assert rel_l2(y, y0) < 1e-13 and rel_l2(z, z0) < 1e-13, (gd, idir)
 
 
+MO_PAIRS = [((2, 0, 1), (0, 1, 2)), ((1, 0, 2), (2, 1, 0)), ((0, 2, 1), (1, 0, 2)), ((1, 2, 0), (2, 0, 1))]
+
+
+@pytest.mark.parametrize("mo1,mo2", MO_PAIRS, ids=[f"{a}-{b}" for a, b in MO_PAIRS])
+def test_memory_orders_against_oracle(ff, oracle, mo1, mo2):
+    """Float-float links between stages whose intermediate layouts follow other memory orders (the
+    scale arrays are ordered for the consuming stage): against the oracle and IEEE intermediates,
+    with d/dy fused."""
+    p3d = ff
+    gd = (128, 256, 64)
+    gd2 = (65, 256, 64)
+    fwd = [p3d.R2CFFT_D, p3d.CFFT_FORWARD_D, p3d.CFFT_FORWARD_D]
+    bwd = [p3d.C2RFFT_D, p3d.CFFT_BACKWARD_D, p3d.CFFT_BACKWARD_D]
+    f = p3d.Transform3D(fwd, gd, mo1, gd2, mo2, -1, 0)
+    b = p3d.Transform3D(bwd, gd2, mo2, gd, mo1, 0, -1)
+    x = seeded_field(p3d.storage_shape(gd, mo1), seed=73)
+    y = f.exec(x, idir=1)
+    z = b.exec(y)
+    p3d.set_ff_intermediates(False)
+    y0 = f.exec(x, idir=1)
+    z0 = b.exec(y0)
+    p3d.set_ff_intermediates(True)
+    yo = oracle.OraclePlan(fwd, gd, mo1, gd2, mo2, -1, 0).exec(x, idir=1)
+    zo = oracle.OraclePlan(bwd, gd2, mo2, gd, mo1, 0, -1).exec(yo)
+    assert rel_l2(y, yo) < 1e-12 and rel_l2(z, zo) < 1e-12
+    assert rel_l2(y, y0) < 1e-13 and rel_l2(z, z0) < 1e-13
+
+
 # x and z transformed, y EMPTY: the x -> z boundary is a float-float intermediate and the y index
 # (storage axis 1) separates slabs that no stage mixes
 G_SLAB = (256, 8, 64)
