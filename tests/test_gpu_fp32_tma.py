@@ -99,3 +99,30 @@ def test_tma_wait_runs_out_sets_status(gpu):
     p3d.set_fp32_tma(True)
     assert used == 1 and np.array_equal(y, y_l)
     assert p3d.device_status() == 0
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024])
+def test_tma_tile_dim_contiguous_c2c(gpu, oracle, n):
+    """C2C lines along dim 1 of a (0,1,2) layout: the tile dim (dim 0, 64 points) is contiguous, so
+    each tile arrives as rows of its lines' points (TMA mode 2); bit-identical to per-thread loads,
+    and a tile dim that is not a multiple of the tile's lines (63) takes the per-thread loads."""
+    p3d = gpu
+    for dt, expect in ((64, 1), (63, 0)):
+        g = (dt, n, 3)
+        tp = p3d.TransPlan(p3d.CFFT_FORWARD_S, g, (0, 1, 2), g, (0, 1, 2), 1)
+        x = seeded_field(p3d.storage_shape(g, (0, 1, 2)), seed=n + dt, dtype=np.complex64)
+        out = {}
+        try:
+            for tma in (True, False):
+                p3d.set_fp32_tma(tma)
+                y = np.empty(p3d.storage_shape(g, (0, 1, 2)), np.complex64)
+                c0 = p3d.tma_launch_count()
+                tp.exec(np.ascontiguousarray(x), y)
+                out[tma] = (y, p3d.tma_launch_count() - c0)
+        finally:
+            p3d.set_fp32_tma(True)
+        assert out[True][1] == expect and out[False][1] == 0, (n, dt, out[True][1])
+        assert np.array_equal(out[True][0], out[False][0]), (n, dt)
+        ref = oracle.exec_stage(p3d.CFFT_FORWARD_D, 1, g, (0, 1, 2), g, (0, 1, 2), x.astype(np.complex128))
+        assert rel_l2(out[True][0], ref) < 1e-6
+    assert p3d.device_status() == 0
