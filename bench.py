@@ -992,6 +992,14 @@ def main():
     forms["fp64_native" if arith else "fp64_float_float"] = {
         "ms_per_step": ms_other, "value": ALG_BYTES / (ms_other * 1e-3) / 1e9, "unit": "GB/s",
         "rel_l2_vs_headline": float(np.linalg.norm(y_other - y) / np.linalg.norm(y))}
+    if arith and n_sm and clocks.get("sm_mhz"):
+        # native FP64 against the FP64 pipe: the usual 2.5 V log2 V flops per direction, against
+        # DFMA at the 1.75 thread instructions per SM per clock measured on this part (2 flops each)
+        fl = 2 * 2.5 * GD[0] * GD[1] * GD[2] * np.log2(float(GD[0] * GD[1] * GD[2]))
+        pk = 2 * 1.75 * n_sm * clocks["sm_mhz"] * 1e6
+        forms["fp64_native"]["fp64_pipe"] = {"flops_per_step": fl, "achieved_tflops": fl / (ms_other * 1e-3) / 1e12,
+                                             "peak_tflops": pk / 1e12, "frac": fl / (ms_other * 1e-3) / pk,
+                                             "hbm_frac": ALG_BYTES / (ms_other * 1e-3) / 1e9 / peak}
     f32 = p3d.Transform3D((4, 8, 8), GD, MO1, GD2, MO2, -1, 0)
     b32 = p3d.Transform3D((6, 10, 10), GD2, MO2, GD, MO1, 0, -1)
     d_in32, d_spec32, d_out32 = p3d.DeviceArray(S_R // 2), p3d.DeviceArray(S_C // 2), p3d.DeviceArray(S_R // 2)

@@ -75,11 +75,12 @@ int p3dfft_gb300_get_ff_intermediates(void);
  * of two table entries.  The initial value can be set with P3DFFT_GB300_FP32_SPLIT_TWIDDLES=0. */
 void p3dfft_gb300_set_fp32_split_twiddles(int on);
 int p3dfft_gb300_get_fp32_split_twiddles(void);
-/* 1 (default): FP32 C2C / R2C stages whose lines are contiguous and evenly spaced in device
- * memory (lengths 2^a*3^b*5^c from 32 whose first radix equals the points per thread, line
- * length 2N floats <= 256 or a multiple of 256) fetch each tile by TMA (a tensor map over the
- * input, cp.async.bulk.tensor into shared memory) instead of per-thread global loads; 0: always
- * per-thread loads.  The initial value can be set with P3DFFT_GB300_FP32_TMA=0. */
+/* 1 (default): FP32 C2C / R2C stages in device memory fetch each tile by TMA (a tensor map over
+ * the input, cp.async.bulk.tensor into shared memory) instead of per-thread global loads, where
+ * the tile is a box: lines contiguous and evenly spaced, or (C2C) the tile dim contiguous and a
+ * multiple of the tile's lines; even lengths 2^a*3^b*5^c from 32 whose first radix equals the
+ * points per thread.  0: always per-thread loads.  The initial value can be set with
+ * P3DFFT_GB300_FP32_TMA=0. */
 void p3dfft_gb300_set_fp32_tma(int on);
 int p3dfft_gb300_get_fp32_tma(void);
 /* The device status word: nonzero after a kernel's bounded wait ran out (the tile was skipped,
