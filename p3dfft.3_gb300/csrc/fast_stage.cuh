@@ -68,6 +68,7 @@ struct FParams {
   long long tma_timeout_ns;
   int tma_extra;
   int tma_d1;    // lines along the tensor map's line dim (line g at (g % tma_d1, g / tma_d1))
+  int tma_store;  // 1: the tile's outputs leave by TMA (C2C, tile dim contiguous in the output)
   int tma_mode;  // 1: lines contiguous (boxes of one line's floats x TB lines); 2: tile dim
                  // contiguous (C2C: boxes of TB points' floats x rows of the line dim)
   int *status;
@@ -507,7 +508,7 @@ __device__ __forceinline__ bool fk_mbar_wait(unsigned bar, unsigned parity, long
 // TMA: the tile's input arrives by the tensor map *tm (fk_tma_variant kernels only).
 template <class O, int KIND, int N, int FF = 0, bool TMA = false>
 __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const void *in, void *out,
-                                        const CUtensorMap *tm = nullptr) {
+                                        const CUtensorMap *tm = nullptr, const CUtensorMap *tmo = nullptr) {
   using C = typename O::C;
   using T = typename O::T;
   using G = typename O::G;
@@ -884,6 +885,44 @@ __device__ __forceinline__ void fk_tile(const FParams &p, const int tile, const 
     if (sid != 0 && !p.store_Lmajor) __syncthreads();
 
     // ---------------- post-processing + store ----------------
+    if constexpr (TMA && KIND == FK_C2C) {
+      if (tma_on && p.tma_store) {
+        // The tile leaves by TMA: each thread takes its points into registers, the CTA lays the
+        // tile out over the region the FFT used as rows of TB points (row k: point k of the
+        // tile's lines), and one thread stores the rows box by box, then waits until the copy
+        // has read shared memory before the CTA exits.  (Full tiles only: the host checks.)
+        using TM = FastTma<N>;
+        const bool sact = valid;
+        const int pjs = fk_pos<PS>(js);
+        C yv[V];
+        if (sact) {
+          const C *Y = buf + (size_t)ls * LS;
+#pragma unroll
+          for (int e = 0; e < V; e++) yv[e] = fk_deriv<O>(p, Y[fk_slot<PS, TT>(js, pjs, e)], js + e * TT);
+        }
+        __syncthreads();
+        RAW *stg = reinterpret_cast<RAW *>(smem_raw);
+        if (sact) {
+#pragma unroll
+          for (int e = 0; e < V; e++) stg[(js + e * TT) * TB + ls] = O::to_raw(yv[e], 0);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          const int ct = g0 % p.dt, co = g0 / p.dt;
+          const unsigned src0 = (unsigned)__cvta_generic_to_shared(smem_raw);
+#pragma unroll 1
+          for (int b = 0; b < TM::NBR; b++)
+            asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                             reinterpret_cast<unsigned long long>(tmo)),
+                         "r"(2 * ct), "r"(b * TM::BOXR), "r"(co), "r"(src0 + (unsigned)(b * TM::BOXR * TB * 8))
+                         : "memory");
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+        return;
+      }
+    }
     const int gs = g0 + ls;
     const bool sact = valid && gs < p.nlines;
     if (sact) {
@@ -987,8 +1026,8 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIN
 // The tile's input staged by the tensor-memory accelerator (fk_tma_variant lengths and kinds).
 template <class O, int KIND, int N>
 __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIND>())
-    k_fast_tma(FParams p, const __grid_constant__ CUtensorMap tm) {
-  if constexpr (fk_tma_variant<O, KIND, N>()) fk_tile<O, KIND, N, 0, true>(p, blockIdx.x, p.in, p.out, &tm);
+    k_fast_tma(FParams p, const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmo) {
+  if constexpr (fk_tma_variant<O, KIND, N>()) fk_tile<O, KIND, N, 0, true>(p, blockIdx.x, p.in, p.out, &tm, &tmo);
 }
 
 // Lengths and kinds with float-float intermediate variants (DFP: C2C in / out / both, R2C out,
@@ -1027,8 +1066,8 @@ struct FastArgs {
   int n;     // complex FFT length N
   FParams p;
   int split = 0;  // FP32 only: split-twiddle kernels (NativeFS; table format 2)
-  int tma = 0;    // single launches only: the tile's input staged by TMA through tm (k_fast_tma)
-  CUtensorMap tm;
+  int tma = 0;    // single launches only: the tile's input staged by TMA through tm[0] (k_fast_tma)
+  CUtensorMap tm[2];  // the input's tensor map and (p.tma_store) the output's
 };
 
 template <class O>
@@ -1090,7 +1129,7 @@ static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t s
     if (tm) {
       if constexpr (fk_tma_variant<O, KIND, N>()) {
         if (ff) return E_UNSUPPORTED;
-        k_fast_tma<O, KIND, N><<<nb, BL, SM, st>>>(p, *tm);
+        k_fast_tma<O, KIND, N><<<nb, BL, SM, st>>>(p, tm[0], tm[1]);
         return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
       } else {
         return E_UNSUPPORTED;
@@ -1220,7 +1259,7 @@ inline int fast_launch_kind(int n, const FParams &p, const FGroup *g, int ctas, 
 
 template <class O>
 inline int fast_launch_arith(const FastArgs &a, const FGroup *g, int ctas, cudaStream_t st) {
-  const CUtensorMap *tm = (a.tma && !g) ? &a.tm : nullptr;
+  const CUtensorMap *tm = (a.tma && !g) ? a.tm : nullptr;
   switch (a.kind) {
     case FK_C2C: return fast_launch_kind<O, FK_C2C>(a.n, a.p, g, ctas, st, tm);
     case FK_R2C: return fast_launch_kind<O, FK_R2C>(a.n, a.p, g, ctas, st, tm);

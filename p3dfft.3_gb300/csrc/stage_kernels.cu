@@ -792,6 +792,15 @@ bool fp32_tma() {
   return g_fp32_tma == 1;
 }
 void set_fp32_tma(bool on) { g_fp32_tma = on ? 1 : 0; }
+// TMA stores of tile-dim-contiguous outputs with the TMA loads (P3DFFT_GB300_FP32_TMA_STORE=0 off)
+static int g_fp32_tma_store = -1;
+static bool fp32_tma_store() {
+  if (g_fp32_tma_store < 0) {
+    const char *e = getenv("P3DFFT_GB300_FP32_TMA_STORE");
+    g_fp32_tma_store = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_fp32_tma_store == 1;
+}
 static std::atomic<int> g_tma_stall(0);
 void inject_tma_stall() { g_tma_stall = 1; }
 
@@ -818,7 +827,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
 // - mode 2 (C2C), the tile dim contiguous and a multiple of the tile's (even) line count.
 static std::atomic<long long> g_tma_launches(0);
 long long tma_launches() { return g_tma_launches.load(); }
-static bool fast_tma_setup(FastArgs &fa, const void *in, DeviceTables *tabs) {
+static bool fast_tma_setup(FastArgs &fa, const void *in, void *out, DeviceTables *tabs) {
   FParams &q = fa.p;
   if (!fp32_tma() || !tabs || !tabs->status || (fa.kind != FK_C2C && fa.kind != FK_R2C) || !fast_tma_length(fa.n))
     return false;
@@ -886,11 +895,31 @@ static bool fast_tma_setup(FastArgs &fa, const void *in, DeviceTables *tabs) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
   if (!enc) return false;
   cuuint32_t estr[3] = {1u, 1u, 1u};
-  if (enc(&fa.tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(in), dims, strides, box, estr,
+  if (enc(&fa.tm[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(in), dims, strides, box, estr,
           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
   q.tma_mode = mode;
+  // the output by TMA too (C2C whose output tile dim is contiguous: each tile leaves as rows of
+  // TB points, full tiles only, 16-byte aligned rows)
+  memset(&fa.tm[1], 0, sizeof(fa.tm[1]));
+  q.tma_store = 0;
+  if (fp32_tma_store() && fa.kind == FK_C2C && !q.store_Lmajor && q.ot == 1 && TB % 2 == 0 && q.dt % TB == 0 &&
+      q.nlines % q.dt == 0 && reinterpret_cast<uintptr_t>(out) % 16 == 0 && (q.oL * 8) % 16 == 0 &&
+      (q.oo * 8) % 16 == 0 && q.dt <= 0x3fffffff) {
+    cudaPointerAttributes ao;
+    const bool dev_out = cudaPointerGetAttributes(&ao, out) == cudaSuccess && ao.type == cudaMemoryTypeDevice;
+    cudaGetLastError();
+    int boxr = fa.n < 256 ? fa.n : 256;
+    while (fa.n % boxr) boxr--;
+    cuuint64_t od[3] = {(cuuint64_t)(2 * q.dt), (cuuint64_t)fa.n, (cuuint64_t)(q.nlines / q.dt)};
+    cuuint64_t os[2] = {(cuuint64_t)(q.oL * 8), (cuuint64_t)(q.oo * 8)};
+    cuuint32_t ob[3] = {(cuuint32_t)(2 * TB), (cuuint32_t)boxr, 1u};
+    if (dev_out && enc(&fa.tm[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, out, od, os, ob, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+      q.tma_store = 1;
+  }
   // a stall injected for the failure-path test: 16 bytes more than the copies deliver, so the
   // tile's wait runs out after 20 ms
   const bool stall = g_tma_stall.exchange(0) != 0;
@@ -1192,6 +1221,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.tma_extra = 0;
     q.tma_d1 = 0;
     q.tma_mode = 0;
+    q.tma_store = 0;
     q.status = nullptr;
     fa.tma = 0;
     if (fast_prep) {
@@ -1199,7 +1229,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
       return E_OK;
     }
     if (q.ntotal == 0) return E_OK;
-    if (d.prec == 4) fast_tma_setup(fa, in, tabs);
+    if (d.prec == 4) fast_tma_setup(fa, in, out, tabs);
     const int rc = launch_fast(d.prec, arith, fa, stream);
     if (rc == E_OK && kernels_launched) (*kernels_launched)++;
     return rc;
