@@ -926,18 +926,25 @@ def main():
     modes_ms["staged_both_not_pipelined"] = e2e_run()
     p3d.set_host_pipeline(True)
     p3d.set_host_direct(True)
+    # A/B: direct host access with the x stages capped at one persistent CTA per SM and the y
+    # stages beside them slab by slab (default), or stage after stage
+    p3d.set_link_ctas(0)
+    modes_ms["direct_both_not_pipelined"] = e2e_run()
+    p3d.set_link_ctas(-1)
     e2e_staged_ms = modes_ms["staged_both"]
     e2e_ms = modes_ms["direct_both"]
     e2e = {"value": ALG_BYTES * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": S_R,
            "d2h_bytes_per_step": S_R, "ms_per_step": e2e_ms,
-           "host_io": "page-locked host arrays read by the x R2C stage and written by the x C2R stage over NVLink-C2C",
+           "host_io": "page-locked host arrays read by the x R2C stage and written by the x C2R stage over "
+                      "NVLink-C2C, each capped at one persistent CTA per SM with the y stage beside it slab by slab",
            "staged_copies": {"ms_per_step": e2e_staged_ms,
                              "value": ALG_BYTES * world / (e2e_staged_ms * 1e-3) / 1e9},
-           "host_io_modes_ms": modes_ms}
+           "host_io_modes_ms": modes_ms, "link_stage_ctas": p3d.get_link_ctas()}
     rt_err = float(np.linalg.norm(hout.array - y) / max(np.linalg.norm(y), 1e-300))
-    # per-phase breakdown of the end-to-end step (CUDA events around each stage, page-locked host
-    # arrays read / written directly by the x stages): the host-link-bound x R2C and x C2R, the
-    # on-device stages between them, and the host time outside the stages
+    # per-phase breakdown of the end-to-end step run stage after stage (CUDA events around each
+    # stage, page-locked host arrays read / written directly by the x stages): the host-link-bound
+    # x R2C and x C2R, the on-device stages between them, and the host time outside the stages
+    # (against the stage-after-stage step; the default step overlaps the y stages with the x)
     ph_f, ph_b = (ctypes.c_double * 8)(), (ctypes.c_double * 8)()
     nf = L.p3dfft_gb300_profile_stages(f.handle, ctypes.c_void_p(hin.ptr), ctypes.c_void_p(d_spec.ptr), IDIR, 3, ph_f, 8)
     nb = L.p3dfft_gb300_profile_stages(b.handle, ctypes.c_void_p(d_spec.ptr), ctypes.c_void_p(hout.ptr), -1, 3, ph_b, 8)
@@ -947,7 +954,8 @@ def main():
         dev_ms = sum(fwd_ms[1:]) + sum(bwd_ms[:-1])
         e2e["phases_ms"] = {
             "x_r2c_reading_host": fwd_ms[0], "on_device_stages": dev_ms, "x_c2r_writing_host": bwd_ms[-1],
-            "outside_stage_kernels": e2e_ms - link_ms - dev_ms,
+            "outside_stage_kernels": modes_ms["direct_both_not_pipelined"] - link_ms - dev_ms,
+            "overlapped_by_link_pipelining": modes_ms["direct_both_not_pipelined"] - e2e_ms,
             "forward_stages": fwd_ms, "backward_stages": bwd_ms,
             "host_link_GBps": {"h2d_in_x_r2c": S_R / (fwd_ms[0] * 1e-3) / 1e9,
                                "d2h_in_x_c2r": S_R / (bwd_ms[-1] * 1e-3) / 1e9}}

@@ -47,6 +47,14 @@ void p3dfft_gb300_set_host_direct(int on);
  * P3DFFT_GB300_PIPELINE=0 sets 0 at start-up. */
 void p3dfft_gb300_set_host_pipeline(int on);
 int p3dfft_gb300_get_host_pipeline(void);
+/* n > 0: a first stage that reads a page-locked host array directly (or a last stage that writes
+ * one) runs with at most n CTAs, each walking its tiles, slab by slab, while the next (previous)
+ * stage runs on the SMs it leaves free, one slab behind (fields of 32 MB and more, plans of 3+
+ * stages, host pipelining on, R2C first / C2R last stages of FFT length 64..2048).  0: those
+ * stages run alone, stage after stage.  n < 0: the default, one CTA per SM, or
+ * P3DFFT_GB300_LINK_CTAS when set. */
+void p3dfft_gb300_set_link_ctas(int n);
+int p3dfft_gb300_get_link_ctas(void);
 /* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,
  * ~1e-14 relative L2 per 3D transform), 0 = native FP64 DFMA (slow on GB300).  The initial value
  * can be set with P3DFFT_GB300_FP64_ARITH=native. */

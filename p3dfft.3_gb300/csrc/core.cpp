@@ -617,6 +617,24 @@ static bool pipeline_host_stages() {
   }
   return g_host_pipe == 1;
 }
+// Grid cap of an end stage that reads / writes a page-locked host array directly while its
+// neighbour stage runs beside it slab by slab (0: no such pipelining).  -1: from
+// P3DFFT_GB300_LINK_CTAS at first use, default one CTA per SM (measured on the 512^3 FP64
+// round trip: 38 CTAs 22.7 ms, 76 13.6, 152 12.93, 228 13.03, 304 13.24; not pipelined 13.61).
+static int g_link_ctas = -1;
+static int link_ctas() {
+  if (g_link_ctas < 0) {
+    const char *e = getenv("P3DFFT_GB300_LINK_CTAS");
+    int sms = 0, dev = 0;
+    if (!e && (cudaGetDevice(&dev) != cudaSuccess ||
+               cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)) {
+      cudaGetLastError();
+      return 0;  // asked again at the next call
+    }
+    g_link_ctas = e ? std::max(0, atoi(e)) : sms;
+  }
+  return g_link_ctas;
+}
 static int g_host_direct = -1;
 static int host_direct_mode() {
   if (g_host_direct < 0) {
@@ -706,6 +724,7 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
 // layouts (the strides of the whole field).
 struct SlabBox {
   int sd, c, m;
+  int ctas = 0;  // the stage's grid cap (StageDesc::max_ctas)
 };
 
 // engine_override >= 0 replaces the plan's tuned engine choice for this stage (0 = heuristic);
@@ -757,6 +776,7 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
       src = static_cast<const unsigned char *>(src) + (size_t)box->c * d.s1[sd] * t.dt1 * P->prec;
       dst = static_cast<unsigned char *>(dst) + (size_t)box->c * d.s2[sd] * t.dt2 * P->prec;
       d.d1[sd] = d.d2[sd] = box->m;
+      d.max_ctas = box->ctas;
       if (d.sin) d.sin += (long long)box->c * d.mi[sd];
       if (d.sout) d.sout += (long long)box->c * d.mo[sd];
     }
@@ -787,7 +807,8 @@ static int slab_dim(const Stage &st) {
 }
 
 static cudaStream_t g_copy_stream = nullptr;
-static cudaEvent_t g_slab_ev[17];
+constexpr int kMaxSlabs = 16;
+static cudaEvent_t g_slab_ev[2 * kMaxSlabs + 1];  // per slab in, per slab out, and the join
 
 // Runs one stage slab by slab along dim sd, overlapping the host copy of each slab on the copy
 // stream: side 0 copies host `host` into `src` (the stage's staged input) slab by slab before
@@ -827,7 +848,8 @@ static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *h
   const int per = ((len + NS - 1) / NS + f - 1) / f * f;
   cudaStream_t cs = g_copy_stream, ms = cur_stream();
   // the copy stream starts after everything already queued on the library stream
-  if (cudaEventRecord(g_slab_ev[16], ms) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[16], 0) != cudaSuccess)
+  if (cudaEventRecord(g_slab_ev[2 * kMaxSlabs], ms) != cudaSuccess ||
+      cudaStreamWaitEvent(cs, g_slab_ev[2 * kMaxSlabs], 0) != cudaSuccess)
     return E_CUDA;
   int rc = E_OK;
   FFLink sff;
@@ -853,7 +875,8 @@ static int run_stage_slabs(const Plan *P, const Stage &st, int sd, const void *h
     }
   }
   if (side == 1) {  // the library stream continues after the last copy
-    if (cudaEventRecord(g_slab_ev[16], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[16], 0) != cudaSuccess)
+    if (cudaEventRecord(g_slab_ev[2 * kMaxSlabs], cs) != cudaSuccess ||
+        cudaStreamWaitEvent(ms, g_slab_ev[2 * kMaxSlabs], 0) != cudaSuccess)
       return E_CUDA;
   }
   return rc;
@@ -1021,19 +1044,23 @@ static int pair_slab_dim(const Stage &a, const Stage &b) {
   return a.g1.gdims[sd] >= 8 ? sd : -1;
 }
 static cudaStream_t g_pipe_stream = nullptr;
-static cudaEvent_t g_pipe_ev[9];  // one per slab, and the fork / join event
+static cudaEvent_t g_pipe_ev[kMaxSlabs + 1];  // one per slab, and the fork / join event
 
 // host_in: stage a's input is staged from host array host_in into src, slab k copied on the copy
 // stream just before stage a's slab k; host_out: stage b's output dst is copied to host array
 // host_out slab by slab as stage b finishes each (sd the slowest dim of that layout, so each slab
 // is one contiguous copy).
 static int ensure_copy_stream();
+// link 1: stage a reads a page-locked host array directly, link 2: stage b writes one; that stage
+// bounds the pair, so it runs on the priority stream with its grid capped at link_ctas persistent
+// CTAs (enough to keep the host link busy) and the other stage's slabs take the remaining SM time.
 static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void *dst, int idir, const FFLink *lka,
-                          const FFLink *lkb, int sd, const void *host_in = nullptr, void *host_out = nullptr) {
-  static int NS = 0;  // slabs (P3DFFT_GB300_PIPE_SLABS, 2..8, default 8)
+                          const FFLink *lkb, int sd, const void *host_in = nullptr, void *host_out = nullptr,
+                          int link = 0, int link_ctas = 0) {
+  static int NS = 0;  // slabs (P3DFFT_GB300_PIPE_SLABS, 2..kMaxSlabs, default 8)
   if (!NS) {
     const char *e = getenv("P3DFFT_GB300_PIPE_SLABS");
-    NS = e ? std::max(2, std::min(8, atoi(e))) : 8;
+    NS = e ? std::max(2, std::min(kMaxSlabs, atoi(e))) : 8;
   }
   if (!g_pipe_stream) {
     // the second stage's slabs get the highest priority, so that each starts as soon as its slab
@@ -1067,34 +1094,44 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
   cudaStream_t ms = cur_stream(), ps = g_pipe_stream, cs = g_copy_stream;
   // the second stream (and the copy stream) start after everything already queued on the
   // library stream
-  if (cudaEventRecord(g_pipe_ev[8], ms) != cudaSuccess || cudaStreamWaitEvent(ps, g_pipe_ev[8], 0) != cudaSuccess)
+  if (cudaEventRecord(g_pipe_ev[kMaxSlabs], ms) != cudaSuccess ||
+      cudaStreamWaitEvent(ps, g_pipe_ev[kMaxSlabs], 0) != cudaSuccess)
     return E_CUDA;
-  if ((host_in || host_out) && cudaStreamWaitEvent(cs, g_pipe_ev[8], 0) != cudaSuccess) return E_CUDA;
+  if ((host_in || host_out) && cudaStreamWaitEvent(cs, g_pipe_ev[kMaxSlabs], 0) != cudaSuccess) return E_CUDA;
   ExecCtx pc{ps, nullptr, false, nullptr};
+  const ExecCtx *prev = t_ctx;
+  // stage a on the library stream and b on the priority stream, or the other way round when a
+  // is the link stage
+  const ExecCtx *ca = link == 1 ? &pc : prev, *cb = link == 1 ? prev : &pc;
+  cudaStream_t sa = link == 1 ? ps : ms, sb = link == 1 ? ms : ps;
   int rc = E_OK;
   for (int c = 0, k = 0; c < len && rc == E_OK; c += per, k++) {
-    const SlabBox box{sd, c, std::min(per, len - c)};
+    SlabBox box{sd, c, std::min(per, len - c)};
     if (host_in) {
       if (cudaMemcpyAsync(static_cast<unsigned char *>(const_cast<void *>(src)) + (size_t)c * u[0],
                           static_cast<const unsigned char *>(host_in) + (size_t)c * u[0], (size_t)box.m * u[0],
                           cudaMemcpyHostToDevice, cs) != cudaSuccess ||
-          cudaEventRecord(g_slab_ev[k], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[k], 0) != cudaSuccess) {
+          cudaEventRecord(g_slab_ev[k], cs) != cudaSuccess || cudaStreamWaitEvent(sa, g_slab_ev[k], 0) != cudaSuccess) {
         rc = E_CUDA;
         break;
       }
     }
+    box.ctas = link == 1 ? link_ctas : 0;
+    t_ctx = ca;
     rc = run_stage(P, a, src, mid, da, nullptr, nullptr, -1, lka, &box);
+    t_ctx = prev;
     if (rc != E_OK) break;
-    if (cudaEventRecord(g_pipe_ev[k], ms) != cudaSuccess || cudaStreamWaitEvent(ps, g_pipe_ev[k], 0) != cudaSuccess) {
+    if (cudaEventRecord(g_pipe_ev[k], sa) != cudaSuccess || cudaStreamWaitEvent(sb, g_pipe_ev[k], 0) != cudaSuccess) {
       rc = E_CUDA;
       break;
     }
-    const ExecCtx *prev = t_ctx;
-    t_ctx = &pc;
+    box.ctas = link == 2 ? link_ctas : 0;
+    t_ctx = cb;
     rc = run_stage(P, b, mid, dst, db, nullptr, nullptr, -1, lkb, &box);
     t_ctx = prev;
     if (rc == E_OK && host_out) {
-      if (cudaEventRecord(g_slab_ev[8 + k], ps) != cudaSuccess || cudaStreamWaitEvent(cs, g_slab_ev[8 + k], 0) != cudaSuccess ||
+      if (cudaEventRecord(g_slab_ev[kMaxSlabs + k], sb) != cudaSuccess ||
+          cudaStreamWaitEvent(cs, g_slab_ev[kMaxSlabs + k], 0) != cudaSuccess ||
           cudaMemcpyAsync(static_cast<unsigned char *>(host_out) + (size_t)c * u[3],
                           static_cast<const unsigned char *>(dst) + (size_t)c * u[3], (size_t)box.m * u[3],
                           cudaMemcpyDeviceToHost, cs) != cudaSuccess)
@@ -1102,13 +1139,24 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
     }
   }
   if (host_out) {  // the library stream continues after the last copy
-    if (cudaEventRecord(g_slab_ev[16], cs) != cudaSuccess || cudaStreamWaitEvent(ms, g_slab_ev[16], 0) != cudaSuccess)
+    if (cudaEventRecord(g_slab_ev[2 * kMaxSlabs], cs) != cudaSuccess ||
+        cudaStreamWaitEvent(ms, g_slab_ev[2 * kMaxSlabs], 0) != cudaSuccess)
       return E_CUDA;
   }
   // the library stream continues after the second stream's last slab (also after a failure)
-  if (cudaEventRecord(g_pipe_ev[8], ps) != cudaSuccess || cudaStreamWaitEvent(ms, g_pipe_ev[8], 0) != cudaSuccess)
+  if (cudaEventRecord(g_pipe_ev[kMaxSlabs], ps) != cudaSuccess ||
+      cudaStreamWaitEvent(ms, g_pipe_ev[kMaxSlabs], 0) != cudaSuccess)
     return E_CUDA;
   return rc;
+}
+
+// Whether stage s of the plan runs on a kernel whose grid can be capped (StageDesc::max_ctas).
+static bool link_cap_ok(const Plan *P, int s, const void *src, void *dst, int idir) {
+  const Stage &st = P->ex[s];
+  if (g_types[st.type].kind == K_EMPTY) return false;
+  StageDesc d;
+  fill_stage_desc(P, st, idir >= 0 && st.dim == idir, d);
+  return stage_cap_ok(d, src, dst, P->prec == 8 ? arith_mode() : AR_NATIVE, g_tabs);
 }
 
 static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaEvent_t *stage_ev = nullptr) {
@@ -1158,6 +1206,8 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   // the slowest of the staged layout, so each slab is one copy).  Not for host arrays read or
   // written directly by the kernels: there the SMs themselves move the data over the link and
   // a concurrent stage only takes SM time from them (measured no gain, 13.69 vs 13.66 ms).
+  // Host arrays read or written directly: with a grid cap on the link stage (link_ctas), the
+  // neighbour stage runs slab by slab on the SMs the link stage leaves free.
   const bool can_pipe = !stage_ev && !g_timers_on && !t_ctx && n >= 3 && pipeline_host_stages();
   int pipe_in = -1, pipe_out = -1;
   if (can_pipe && stage_host_in && in_bytes >= kSlabMin) {
@@ -1227,6 +1277,14 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     }
     dst[s] = cand;
   }
+  // Host arrays read or written directly: the link stage capped at lc persistent CTAs (when its
+  // kernel has that form) and its neighbour stage beside it, slab by slab.
+  const int lc = can_pipe && (in_direct || out_direct) ? link_ctas() : 0;
+  if (lc > 0 && pipe_in < 0 && in_direct && in_bytes >= kSlabMin && link_cap_ok(P, 0, din, dst[0], idir))
+    pipe_in = pair_slab_dim(P->ex[0], P->ex[1]);
+  if (lc > 0 && pipe_out < 0 && out_direct && out_bytes >= kSlabMin && (pipe_in < 0 || n >= 4) &&
+      link_cap_ok(P, n - 1, dst[n - 2], dout, idir))
+    pipe_out = pair_slab_dim(P->ex[n - 2], P->ex[n - 1]);
   // float-float links between consecutive specialised float-float stages (not for recorded or
   // caller-owned scratch sets, slab-pipelined host stages or in-place single-stage calls)
   std::vector<FFLink> ffl(n);
@@ -1280,8 +1338,10 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
     if ((s == 0 && pipe_in >= 0) || (s == n - 2 && pipe_out >= 0)) {  // this stage and the next, pipelined
       const FFLink *lk2 = (ffl[s + 1].ffin || ffl[s + 1].ffout) ? &ffl[s + 1] : nullptr;
       const bool first = s == 0 && pipe_in >= 0;
+      const int link = first ? (pipe_in_staged ? 0 : 1) : (pipe_out_staged ? 0 : 2);
       rc = run_pair_slabs(P, s, src, d, dst[s + 1], idir, lk, lk2, first ? pipe_in : pipe_out,
-                          (first && pipe_in_staged) ? in : nullptr, (!first && pipe_out_staged) ? out : nullptr);
+                          (first && pipe_in_staged) ? in : nullptr, (!first && pipe_out_staged) ? out : nullptr,
+                          link, lc);
       src = dst[s + 1];
       s++;
       continue;
@@ -1577,6 +1637,8 @@ void p3dfft_clear_error(void) {
 void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
 void p3dfft_gb300_set_host_pipeline(int on) { g_host_pipe = on ? 1 : 0; }
+void p3dfft_gb300_set_link_ctas(int n) { g_link_ctas = n < 0 ? -1 : n; }
+int p3dfft_gb300_get_link_ctas(void) { return link_ctas(); }
 int p3dfft_gb300_get_host_pipeline(void) { return pipeline_host_stages() ? 1 : 0; }
 void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on == 1 ? 3 : (on == 2 ? 1 : (on == 3 ? 2 : 0)); }
 void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }

@@ -1023,6 +1023,37 @@ __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIN
   fk_tile<O, KIND, N, FF>(p, blockIdx.x, p.in, p.out);
 }
 
+// Persistent form: a grid smaller than the tile count, each CTA walking the tiles with a grid
+// stride, which bounds the SMs held by a stage that moves its data over the host link while the
+// neighbour stage runs beside it.  A separate kernel: inside a loop the tile body no longer fits
+// 64 registers and spills, so the one-tile-per-CTA kernel stays loop-free, and this one is
+// compiled for 2 resident CTAs per SM (128 registers; a link stage needs few CTAs).
+// Instantiated for the end stages of real-to-complex plans on the large-field lengths: R2C
+// reading IEEE values (FF 0, or 2 with a float-float output) and C2R writing them (FF 0 or 1).
+template <int KIND, int N>
+constexpr bool fk_persist_variant() {
+  return (KIND == FK_R2C || KIND == FK_C2R) &&
+         (N == 64 || N == 128 || N == 256 || N == 512 || N == 1024 || N == 2048);
+}
+// Whether a launch of this kind, length and float-float sides can be capped (host side).
+inline bool fast_persist_ok(int kind, int n, int ffin, int ffout) {
+  const bool len = n == 64 || n == 128 || n == 256 || n == 512 || n == 1024 || n == 2048;
+  return len && ((kind == FK_R2C && !ffin) || (kind == FK_C2R && !ffout));
+}
+#ifndef FAST_PERSIST_MINB
+#define FAST_PERSIST_MINB 2  // resident CTAs per SM the persistent kernels are compiled for
+#endif
+template <class O, int KIND, int N, int FF = 0>
+__global__ void __launch_bounds__(FastShape<N>::BLOCK, FAST_PERSIST_MINB)
+    k_fast_persist(FParams p) {
+  for (int t = blockIdx.x;;) {
+    fk_tile<O, KIND, N, FF>(p, t, p.in, p.out);
+    t += gridDim.x;
+    if (t >= p.ntotal) break;
+    __syncthreads();
+  }
+}
+
 // The tile's input staged by the tensor-memory accelerator (fk_tma_variant lengths and kinds).
 template <class O, int KIND, int N>
 __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIND>())
@@ -1108,6 +1139,18 @@ static int fk_configure() {
           cudaFuncSetAttribute(k_fast<O, KIND, N, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
         return E_CUDA;
     }
+    if constexpr (fk_persist_variant<KIND, N>()) {
+      const int sm = (int)fk_smem<O, KIND, N>();
+      if (cudaFuncSetAttribute(k_fast_persist<O, KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) !=
+          cudaSuccess)
+        return E_CUDA;
+      if constexpr (fk_ff_variants<O, KIND, N>()) {
+        constexpr int FFV = KIND == FK_R2C ? 2 : 1;
+        if (cudaFuncSetAttribute(k_fast_persist<O, KIND, N, FFV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 sm) != cudaSuccess)
+          return E_CUDA;
+      }
+    }
     configured = true;
   }
   return E_OK;
@@ -1126,6 +1169,24 @@ static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t s
     const unsigned nb = (unsigned)p.ntotal;
     constexpr int BL = FastShape<N>::BLOCK;
     constexpr size_t SM = fk_smem<O, KIND, N>();
+    // ctas > 0 caps the grid of a single launch at that many persistent CTAs (the lengths, kinds
+    // and float-float sides of k_fast_persist; fast_persist_ok tells which)
+    if constexpr (fk_persist_variant<KIND, N>()) {
+      if (ctas > 0 && !tm && ctas < p.ntotal) {
+        const unsigned pb = (unsigned)ctas;
+        constexpr int FFV = KIND == FK_R2C ? 2 : 1;
+        if (ff == 0) {
+          k_fast_persist<O, KIND, N><<<pb, BL, SM, st>>>(p);
+          return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+        }
+        if constexpr (fk_ff_variants<O, KIND, N>()) {
+          if (ff == FFV) {
+            k_fast_persist<O, KIND, N, FFV><<<pb, BL, SM, st>>>(p);
+            return cudaGetLastError() == cudaSuccess ? E_OK : E_CUDA;
+          }
+        }
+      }
+    }
     if (tm) {
       if constexpr (fk_tma_variant<O, KIND, N>()) {
         if (ff) return E_UNSUPPORTED;
@@ -1290,7 +1351,8 @@ inline int fast_preload(int prec, int arith) {
 }
 
 // prec 4: FP32; prec 8: float-float (arith AR_DF) or native FP64.  With g set, one launch of
-// `ctas` CTAs covers the group of stages g describes (a.kind and a.n select the kernel).
+// `ctas` CTAs covers the group of stages g describes (a.kind and a.n select the kernel); without
+// g, ctas > 0 caps the stage's grid at that many persistent CTAs.
 inline int launch_fast(int prec, int arith, const FastArgs &a, cudaStream_t st, const FGroup *g = nullptr,
                        int ctas = 0) {
   if (prec == 4) {

@@ -47,6 +47,9 @@ struct StageDesc {
   // talt 1 takes consecutive lines of a tile along the other batch dim
   int engine = 0;
   int talt = 0;
+  // specialised kernels: at most this many CTAs, each walking the tiles with a grid stride
+  // (0: one CTA per tile)
+  int max_ctas = 0;
   // Float-float intermediate fields (float-float arithmetic, specialised C2C / R2C / C2R kernels
   // only; other launches with these set fail with E_UNSUPPORTED).  ffin: the input field holds
   // packed float-float values scaled per stored line; the scale of the value at logical
@@ -91,6 +94,9 @@ struct FastArgs;  // a specialised-kernel launch (fast_stage.cuh)
 int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaStream_t stream,
                  DeviceTables *tabs, int *kernels_launched, const void *tw_given = nullptr,
                  const void *aux_given = nullptr, TableNeed *tabs_out = nullptr, FastArgs *fast_prep = nullptr);
+// Whether the stage runs on a specialised kernel that honours StageDesc::max_ctas (nothing is
+// launched; the stage's tables are loaded into `tabs`).
+bool stage_cap_ok(const StageDesc &d, const void *in, void *out, int arith, DeviceTables *tabs);
 
 // ---- grouped launches (batch runtime) ----
 // One stage of one transform with its buffers, as the executor would launch it.

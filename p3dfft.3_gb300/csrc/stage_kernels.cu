@@ -1229,8 +1229,9 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
       return E_OK;
     }
     if (q.ntotal == 0) return E_OK;
-    if (d.prec == 4) fast_tma_setup(fa, in, out, tabs);
-    const int rc = launch_fast(d.prec, arith, fa, stream);
+    // (a capped grid runs the persistent k_fast: the TMA kernels take one tile per CTA)
+    if (d.prec == 4 && d.max_ctas <= 0) fast_tma_setup(fa, in, out, tabs);
+    const int rc = launch_fast(d.prec, arith, fa, stream, nullptr, std::max(0, d.max_ctas));
     if (rc == E_OK && kernels_launched) (*kernels_launched)++;
     return rc;
   }
@@ -1282,6 +1283,16 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
   else rc = launch_any<Native<double>>(p, fixed, use_blue, smem, (int)grid, threads, stream);
   if (rc == E_OK && kernels_launched) (*kernels_launched)++;
   return rc;
+}
+
+bool stage_cap_ok(const StageDesc &d, const void *in, void *out, int arith, DeviceTables *tabs) {
+  StageDesc q = d;
+  q.ffin = q.ffout = 0;  // (the query form takes none; fast_persist_ok checks the sides)
+  q.sin = nullptr;
+  q.sout = nullptr;
+  FastArgs fa;
+  if (launch_stage(q, in, out, arith, 0, tabs, nullptr, nullptr, nullptr, nullptr, &fa) != E_OK) return false;
+  return fast_persist_ok(fa.kind, fa.n, d.ffin, d.ffout);
 }
 
 template <class E>

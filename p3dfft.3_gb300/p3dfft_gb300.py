@@ -63,6 +63,8 @@ def lib():
         "p3dfft_gb300_set_host_direct": ([ctypes.c_int], None),
         "p3dfft_gb300_set_host_pipeline": ([ctypes.c_int], None),
         "p3dfft_gb300_get_host_pipeline": ([], ctypes.c_int),
+        "p3dfft_gb300_set_link_ctas": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_link_ctas": ([], ctypes.c_int),
         "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
         "p3dfft_gb300_set_reference_compat": ([ctypes.c_int], None),
         "p3dfft_gb300_get_reference_compat": ([], ctypes.c_int),
@@ -228,6 +230,17 @@ def set_host_pipeline(on: bool):
 
 def get_host_pipeline() -> bool:
     return bool(lib().p3dfft_gb300_get_host_pipeline())
+
+
+def set_link_ctas(n: int):
+    """n > 0: the end stage that reads / writes a page-locked host array directly runs on at
+    most n persistent CTAs, slab by slab, with its neighbour stage beside it; 0: stage after
+    stage; n < 0: the default (one CTA per SM)."""
+    lib().p3dfft_gb300_set_link_ctas(int(n))
+
+
+def get_link_ctas() -> int:
+    return int(lib().p3dfft_gb300_get_link_ctas())
 
 
 def set_stream(stream_ptr: int):

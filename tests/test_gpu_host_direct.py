@@ -98,8 +98,9 @@ def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2, sliced):
     """Page-locked host input and output of a 3D round trip (fields over the 32 MB threshold,
     d/dz fused), read / written directly by the kernels, or staged through HBM by per-slab
     copies with the first two / last two stages pipelined behind them slab by slab (or, with
-    pipelining off, the first / last stage alone): every variant bit-identical to device-resident
-    arrays."""
+    pipelining off, the first / last stage alone), or read / written directly by a first / last
+    stage capped at a few persistent CTAs with its neighbour stage beside it slab by slab: every
+    variant bit-identical to device-resident arrays."""
     p3d = gpu
     p3d.set_fp64_arith(1)
     gd = (256, 256, 160) if prec == 8 else (256, 256, 192)
@@ -116,6 +117,7 @@ def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2, sliced):
     d_s = p3d.DeviceArray(int(np.prod(f.out_shape())) * np.dtype(f.out_dtype()).itemsize)
     res = {}
     try:
+        p3d.set_link_ctas(0)  # direct host access stage after stage, first
         for direct in (True, False):
             p3d.set_host_direct(direct)
             for pipe in (True, False):
@@ -127,10 +129,23 @@ def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2, sliced):
                 spec = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
                 b.exec(d_s, hout.array)
                 res[direct, pipe] = (spec, hout.array.copy(), p3d.kernel_count() - k0)
+        p3d.set_host_direct(True)
+        p3d.set_host_pipeline(True)
+        for cap in (37, 152, -1):  # persistent link-stage CTAs (37: many tiles per CTA; -1 default)
+            p3d.set_link_ctas(cap)
+            hout = p3d.PinnedArray(x.shape, rdt)
+            hout.array[...] = 0
+            k0 = p3d.kernel_count()
+            f.exec(hin.array, d_s, idir=2)
+            spec = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
+            b.exec(d_s, hout.array)
+            res["link", cap] = (spec, hout.array.copy(), p3d.kernel_count() - k0)
     finally:
+        p3d.set_link_ctas(-1)
         p3d.set_host_pipeline(True)
         p3d.set_host_direct(True)
     assert res[True, True][2] == res[True, False][2]  # direct host access: stage after stage
+    assert res["link", 37][2] > res[True, True][2]  # the linked stage pairs ran in slabs
     if sliced:  # staged: the stage pairs (pipelining on) or the end stages (off) ran in slabs
         assert res[False, True][2] > res[False, False][2] > res[True, True][2]
     else:
