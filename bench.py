@@ -417,13 +417,6 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
     ms_wl, k_wl = time_batch(b_wl)
     b_wl32 = make_batch(single, grouped="list")
     ms_wl32, _ = time_batch(b_wl32)
-    # the same with persistent CTAs: each work-list launch's grid capped at the resident CTAs
-    os.environ["P3DFFT_GB300_LIST_PERSISTENT"] = "1"
-    try:
-        b_wlp = make_batch(mixed, grouped="list")
-        ms_wlp, _ = time_batch(b_wlp)
-    finally:
-        del os.environ["P3DFFT_GB300_LIST_PERSISTENT"]
 
     # 48 sequential plain FP64 calls: the reference-style synchronous exec, one job after another
     p3d.set_sync(True)
@@ -469,8 +462,6 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
         "batch_graph_work_list_mixed": {"ms": ms_wl, "round_trips_per_s": n / (ms_wl * 1e-3), "kernels_per_exec": k_wl,
                                         "work_list_launches": b_wl.groups(),
                                         "mode": "one launch per (stage level, kernel) over every job's tiles (device work list of (stage, tile) items); launches round-robin on the branch streams, each waiting only for the launches of its jobs' previous stage"},
-        "batch_graph_work_list_persistent_mixed": {"ms": ms_wlp, "round_trips_per_s": n / (ms_wlp * 1e-3),
-                                                   "mode": "work lists walked by persistent CTAs (grid = resident CTAs)"},
         "batch_graph_work_list_all_fp32": {"ms": ms_wl32, "round_trips_per_s": n / (ms_wl32 * 1e-3),
                                            "speedup_vs_sequential_fp64": ms_seq / ms_wl32},
         "batch_streams_no_graph_mixed": {"ms": ms_nog, "round_trips_per_s": n / (ms_nog * 1e-3)},
@@ -481,7 +472,7 @@ def batch_workload(p3d, L, steps, warmup, nbranches=8, seed=4):
         "autotune": {"seconds": t_tune, "engines": "1 specialised, 2 register, 3 generic; [engine, alt tile dim, ms]",
                      "choices": tuning},
     }
-    for bt in (b_mixed, b_f64, b_f32, b_nog, b_br, b_wl, b_wl32, b_wlp):
+    for bt in (b_mixed, b_f64, b_f32, b_nog, b_br, b_wl, b_wl32):
         del bt
     return out
 

@@ -444,8 +444,8 @@ __host__ __device__ constexpr int fast_min_blocks() {
 
 // A launch over the tiles of several stages of independent transforms that share the kernel
 // (arithmetic, kind, length) and may differ in everything else (buffers, grids, strides, tables):
-// plist holds each stage's parameters, work the (stage, tile) items; CTAs walk the list with a grid
-// stride (k_fast_list).
+// plist holds each stage's parameters, work the (stage, tile) items; one CTA per item
+// (k_fast_list).
 struct FGroup {
   const struct FParams *plist;
   const struct FWork *work;
@@ -1071,23 +1071,23 @@ constexpr bool fk_ff_variants() {
 inline bool fast_ff_length(int n) { return n == 64 || n == 128 || n == 256 || n == 512 || n == 1024 || n == 2048; }
 
 // Work-list launch: item w is tile work[w].tile of the stage whose parameters are
-// plist[work[w].stage]; the parameters are staged in shared memory for the tile.  A grid smaller
-// than the list makes the CTAs persistent (each walks the list with a grid stride).  No CTA waits
-// on another.
+// plist[work[w].stage]; the parameters are staged in shared memory for the tile.  One CTA per
+// item.  No CTA waits on another.
+// (A grid-stride loop over the list, for a grid smaller than the list, was measured no faster
+// and makes the tile body spill: inside a loop it no longer fits 64 registers.)
 template <class O, int KIND, int N>
 __global__ void __launch_bounds__(FastShape<N>::BLOCK, fast_min_blocks<O, N, KIND>())
     k_fast_list(const FParams *plist, const FWork *work, int nwork) {
   __shared__ FParams sp;
   constexpr int NW = (int)(sizeof(FParams) / sizeof(int));
   static_assert(sizeof(FParams) % sizeof(int) == 0, "FParams copied as ints");
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-    const FWork it = work[w];
-    const int *src = reinterpret_cast<const int *>(plist + it.stage);
-    for (int i = threadIdx.x; i < NW; i += blockDim.x) reinterpret_cast<int *>(&sp)[i] = __ldg(src + i);
-    __syncthreads();
-    fk_tile<O, KIND, N>(sp, it.tile, sp.in, sp.out);
-    __syncthreads();
-  }
+  const int w = blockIdx.x;
+  if (w >= nwork) return;
+  const FWork it = work[w];
+  const int *src = reinterpret_cast<const int *>(plist + it.stage);
+  for (int i = threadIdx.x; i < NW; i += blockDim.x) reinterpret_cast<int *>(&sp)[i] = __ldg(src + i);
+  __syncthreads();
+  fk_tile<O, KIND, N>(sp, it.tile, sp.in, sp.out);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1161,8 +1161,8 @@ static int fk_launch(const FParams &p, const FGroup *g, int ctas, cudaStream_t s
   if (fk_configure<O, KIND, N>() != E_OK) return E_CUDA;
   if (g) {
     if (ctas <= 0) return E_OK;
-    k_fast_list<O, KIND, N><<<(unsigned)ctas, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(g->plist, g->work,
-                                                                                               g->nwork);
+    k_fast_list<O, KIND, N><<<(unsigned)g->nwork, FastShape<N>::BLOCK, fk_smem<O, KIND, N>(), st>>>(
+        g->plist, g->work, g->nwork);
   } else {
     if (p.ntotal <= 0) return E_OK;
     const int ff = (p.ffin ? 1 : 0) | (p.ffout ? 2 : 0);

@@ -111,8 +111,7 @@ struct StageLaunch {
 // and run on a specialised kernel become one grouped launch over all their tiles, the others one
 // launch each.  With work_list, stages that run the same specialised kernel (arithmetic, kind,
 // length) become one grouped launch even when their grids, strides and tables differ.  A grouped
-// launch is one k_fast_list launch over the members' (stage, tile) items
-// (P3DFFT_GB300_LIST_PERSISTENT=1 caps its grid at the resident CTAs, which then walk the list).
+// launch is one k_fast_list launch over the members' (stage, tile) items, one CTA per item.
 // Building uploads the groups' parameters and items.
 struct LaunchSet;
 LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels, DeviceTables *tabs, int *err,

@@ -1336,7 +1336,6 @@ struct LaunchSet {
   FParams *dev_params = nullptr;  // every group's members' parameters
   FWork *dev_work = nullptr;      // and (member, tile) items
   DeviceTables *tabs = nullptr;
-  bool persistent = false;  // work-list launches with at most (SMs x resident CTAs) CTAs
 };
 
 // everything of a specialised launch but its buffers
@@ -1357,10 +1356,6 @@ LaunchSet *launch_set_build(const std::vector<std::vector<StageLaunch>> &levels,
                             bool work_list) {
   LaunchSet *S = new LaunchSet();
   S->tabs = tabs;
-  {
-    const char *e = getenv("P3DFFT_GB300_LIST_PERSISTENT");
-    S->persistent = e && e[0] == '1';
-  }
   std::vector<FParams> params;
   std::vector<FWork> work;
   for (const auto &lv : levels) {
@@ -1459,12 +1454,7 @@ static int run_launch_item(LaunchSet *S, const LaunchItem &it, cudaStream_t st, 
     fg.plist = S->dev_params + g.pfirst;
     fg.work = S->dev_work + g.wfirst;
     fg.nwork = g.nwork;
-    long long ctas = g.nwork;
-    if (S->persistent) {
-      static int nsm = 0;
-      if (!nsm) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0);
-      ctas = std::min<long long>(ctas, (long long)std::max(nsm, 1) * (g.prec == 8 ? 4 : 8));
-    }
+    const long long ctas = g.nwork;  // one CTA per item
     if (ctas > 0x7fffffffLL) return E_TOO_LARGE;
     const int rc = launch_fast(g.prec, g.arith, g.fa, st, &fg, (int)ctas);
     if (rc == E_OK && kernels) (*kernels)++;

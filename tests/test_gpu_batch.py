@@ -157,15 +157,13 @@ def test_batch_rejects_host_pointers(gpu):
         batch.add(0, f, x, y)
 
 
-@pytest.mark.parametrize("persistent", [False, True])
-def test_work_list_batch_merges_uneven_jobs(gpu, oracle, persistent, monkeypatch):
+def test_work_list_batch_merges_uneven_jobs(gpu, oracle):
     """Work-list mode: each stage level runs one launch per kernel (arithmetic, kind, FFT length)
     over the tiles of every job that needs it, whatever the jobs' grids, so uneven jobs that share a
-    line length share a launch; with persistent CTAs the grid is capped at the resident CTAs, which
-    walk the (stage, tile) list.  Results are bit-identical to each job run alone."""
+    line length share a launch (one CTA per (stage, tile) item).  Results are bit-identical to each
+    job run alone."""
     p3d = gpu
     p3d.set_fp64_arith(1)
-    monkeypatch.setenv("P3DFFT_GB300_LIST_PERSISTENT", "1" if persistent else "0")
     shapes = [(64, 32, 48), (64, 48, 32), (32, 64, 40), (48, 64, 64), (64, 64, 64), (40, 32, 64)]
     jobs = [Job(p3d, gd, prec, seed=300 + i) for i, gd in enumerate(shapes) for prec in (8, 4)]
     alone = [j.alone() for j in jobs]
