@@ -917,7 +917,7 @@ def main():
     modes_ms["staged_both_not_pipelined"] = e2e_run()
     p3d.set_host_pipeline(True)
     p3d.set_host_direct(True)
-    # A/B: direct host access with the x stages capped at one persistent CTA per SM and the y
+    # A/B: direct host access with the x stages on capped grids of persistent CTAs and the y
     # stages beside them slab by slab (default), or stage after stage
     p3d.set_link_ctas(0)
     modes_ms["direct_both_not_pipelined"] = e2e_run()
@@ -927,10 +927,11 @@ def main():
     e2e = {"value": ALG_BYTES * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": S_R,
            "d2h_bytes_per_step": S_R, "ms_per_step": e2e_ms,
            "host_io": "page-locked host arrays read by the x R2C stage and written by the x C2R stage over "
-                      "NVLink-C2C, each capped at one persistent CTA per SM with the y stage beside it slab by slab",
+                      "NVLink-C2C, each on a capped grid of persistent CTAs with the y stage beside it slab by slab",
            "staged_copies": {"ms_per_step": e2e_staged_ms,
                              "value": ALG_BYTES * world / (e2e_staged_ms * 1e-3) / 1e9},
-           "host_io_modes_ms": modes_ms, "link_stage_ctas": p3d.get_link_ctas()}
+           "host_io_modes_ms": modes_ms,
+           "link_stage_ctas": "1 per SM (FP64)"}
     rt_err = float(np.linalg.norm(hout.array - y) / max(np.linalg.norm(y), 1e-300))
     # per-phase breakdown of the end-to-end step run stage after stage (CUDA events around each
     # stage, page-locked host arrays read / written directly by the x stages): the host-link-bound

@@ -51,8 +51,9 @@ int p3dfft_gb300_get_host_pipeline(void);
  * one) runs with at most n CTAs, each walking its tiles, slab by slab, while the next (previous)
  * stage runs on the SMs it leaves free, one slab behind (fields of 32 MB and more, plans of 3+
  * stages, host pipelining on, R2C first / C2R last stages of FFT length 64..2048).  0: those
- * stages run alone, stage after stage.  n < 0: the default, one CTA per SM, or
- * P3DFFT_GB300_LINK_CTAS when set. */
+ * stages run alone, stage after stage.  n < 0: the default, P3DFFT_GB300_LINK_CTAS when set,
+ * else one CTA per SM for FP64 stages and two per SM for FP32.  get returns the cap set (or the
+ * variable's), -1 for the default. */
 void p3dfft_gb300_set_link_ctas(int n);
 int p3dfft_gb300_get_link_ctas(void);
 /* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,

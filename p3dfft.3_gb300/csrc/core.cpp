@@ -618,22 +618,34 @@ static bool pipeline_host_stages() {
   return g_host_pipe == 1;
 }
 // Grid cap of an end stage that reads / writes a page-locked host array directly while its
-// neighbour stage runs beside it slab by slab (0: no such pipelining).  -1: from
-// P3DFFT_GB300_LINK_CTAS at first use, default one CTA per SM (measured on the 512^3 FP64
-// round trip: 38 CTAs 22.7 ms, 76 13.6, 152 12.93, 228 13.03, 304 13.24; not pipelined 13.61).
+// neighbour stage runs beside it slab by slab (0: no such pipelining).  -1 (default): from
+// P3DFFT_GB300_LINK_CTAS when set, else one CTA per SM for FP64 stages and two for FP32.
+// Measured on the 512^3 round trip (forward / backward ms, +-0.05 between runs): FP64 38 CTAs
+// 22.7 ms in all, 76 13.6, 152 6.13 / 6.75, 228 6.25 / 6.74, 304 6.45 / 6.71, stage after stage
+// 6.59 / 7.02; FP32 152 2.92 / 3.16, 304 2.86 / 3.13, 456 2.88 / 3.14, stage after stage
+// 2.99 / 3.22.
 static int g_link_ctas = -1;
-static int link_ctas() {
+static int link_ctas_set() {  // the explicit cap, or -1
   if (g_link_ctas < 0) {
     const char *e = getenv("P3DFFT_GB300_LINK_CTAS");
-    int sms = 0, dev = 0;
-    if (!e && (cudaGetDevice(&dev) != cudaSuccess ||
-               cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)) {
-      cudaGetLastError();
-      return 0;  // asked again at the next call
-    }
-    g_link_ctas = e ? std::max(0, atoi(e)) : sms;
+    if (e) return std::max(0, atoi(e));
   }
   return g_link_ctas;
+}
+static int link_ctas(int prec) {
+  const int n = link_ctas_set();
+  if (n >= 0) return n;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      sms = 0;
+      return 0;  // asked again at the next call
+    }
+  }
+  return sms * (prec == 4 ? 2 : 1);
 }
 static int g_host_direct = -1;
 static int host_direct_mode() {
@@ -1279,10 +1291,10 @@ static int exec_plan(Plan *P, const void *in, void *out, int idir, int OW, cudaE
   }
   // Host arrays read or written directly: the link stage capped at lc persistent CTAs (when its
   // kernel has that form) and its neighbour stage beside it, slab by slab.
-  const int lc = can_pipe && (in_direct || out_direct) ? link_ctas() : 0;
-  if (lc > 0 && pipe_in < 0 && in_direct && in_bytes >= kSlabMin && link_cap_ok(P, 0, din, dst[0], idir))
+  const int lc = can_pipe && (in_direct || out_direct) ? link_ctas(P->prec) : 0;
+  if (lc > 0 && in_direct && pipe_in < 0 && in_bytes >= kSlabMin && link_cap_ok(P, 0, din, dst[0], idir))
     pipe_in = pair_slab_dim(P->ex[0], P->ex[1]);
-  if (lc > 0 && pipe_out < 0 && out_direct && out_bytes >= kSlabMin && (pipe_in < 0 || n >= 4) &&
+  if (lc > 0 && out_direct && pipe_out < 0 && out_bytes >= kSlabMin && (pipe_in < 0 || n >= 4) &&
       link_cap_ok(P, n - 1, dst[n - 2], dout, idir))
     pipe_out = pair_slab_dim(P->ex[n - 2], P->ex[n - 1]);
   // float-float links between consecutive specialised float-float stages (not for recorded or
@@ -1638,7 +1650,7 @@ void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
 void p3dfft_gb300_set_host_pipeline(int on) { g_host_pipe = on ? 1 : 0; }
 void p3dfft_gb300_set_link_ctas(int n) { g_link_ctas = n < 0 ? -1 : n; }
-int p3dfft_gb300_get_link_ctas(void) { return link_ctas(); }
+int p3dfft_gb300_get_link_ctas(void) { return link_ctas_set(); }
 int p3dfft_gb300_get_host_pipeline(void) { return pipeline_host_stages() ? 1 : 0; }
 void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on == 1 ? 3 : (on == 2 ? 1 : (on == 3 ? 2 : 0)); }
 void p3dfft_gb300_set_fp64_arith(int m) { g_arith = m ? AR_DF : AR_NATIVE; }

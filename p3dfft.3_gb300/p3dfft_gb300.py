@@ -235,7 +235,7 @@ def get_host_pipeline() -> bool:
 def set_link_ctas(n: int):
     """n > 0: the end stage that reads / writes a page-locked host array directly runs on at
     most n persistent CTAs, slab by slab, with its neighbour stage beside it; 0: stage after
-    stage; n < 0: the default (one CTA per SM)."""
+    stage; n < 0: the default (one CTA per SM for FP64, two per SM for FP32)."""
     lib().p3dfft_gb300_set_link_ctas(int(n))
 
 

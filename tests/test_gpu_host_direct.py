@@ -160,3 +160,54 @@ def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2, sliced):
         assert np.array_equal(spec, spec_dev), key
         assert np.array_equal(y, y_dev), key
     assert np.array_equal(hin.array, x)
+
+
+@pytest.mark.parametrize("arith,gd,mo1,mo2", [(1, (512, 128, 70), (0, 1, 2), (1, 2, 0)),
+                                              (0, (256, 256, 136), (0, 1, 2), (1, 2, 0)),
+                                              (1, (512, 96, 90), (1, 0, 2), (2, 1, 0))])
+def test_link_pipelined_ragged_slabs_and_native_fp64(gpu, arith, gd, mo1, mo2):
+    """Direct host input / output with the link stages on capped persistent grids beside their
+    neighbour stages: slab counts that do not divide the slab dim (70 and 90 planes in 8 slabs),
+    native FP64 arithmetic (IEEE intermediates), and another memory-order pair; each equal bit for
+    bit to the same round trip stage after stage (cap 0) and to device-resident arrays."""
+    p3d = gpu
+    p3d.set_fp64_arith(arith)
+    gd2 = (gd[0] // 2 + 1, gd[1], gd[2])
+    f = p3d.Transform3D([p3d.TYPE_IDS["R2CFFT_D"], p3d.TYPE_IDS["CFFT_FORWARD_D"],
+                         p3d.TYPE_IDS["CFFT_FORWARD_D"]], gd, mo1, gd2, mo2, -1, 0)
+    b = p3d.Transform3D([p3d.TYPE_IDS["C2RFFT_D"], p3d.TYPE_IDS["CFFT_BACKWARD_D"],
+                         p3d.TYPE_IDS["CFFT_BACKWARD_D"]], gd2, mo2, gd, mo1, 0, -1)
+    x = seeded_field(f.in_shape(), seed=sum(gd) + arith)
+    hin = p3d.PinnedArray(x.shape, np.float64)
+    hin.array[...] = x
+    d_s = p3d.DeviceArray(int(np.prod(f.out_shape())) * 16)
+    res = {}
+    try:
+        for cap in (0, -1, 61):
+            p3d.set_link_ctas(cap)
+            hout = p3d.PinnedArray(x.shape, np.float64)
+            hout.array[...] = 0
+            k0 = p3d.kernel_count()
+            f.exec(hin.array, d_s)
+            spec = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
+            b.exec(d_s, hout.array)
+            res[cap] = (spec, hout.array.copy(), p3d.kernel_count() - k0)
+    finally:
+        p3d.set_link_ctas(-1)
+        p3d.set_fp64_arith(1)
+    assert res[-1][2] > res[0][2] and res[61][2] == res[-1][2]  # slab launches in the linked pairs
+    d_in, d_out = p3d.DeviceArray(x.nbytes), p3d.DeviceArray(x.nbytes)
+    d_in.upload(x)
+    p3d.set_fp64_arith(arith)
+    try:
+        f.exec(d_in, d_s)
+        spec_dev = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
+        b.exec(d_s, d_out)
+        y_dev = d_out.download(np.empty_like(x))
+    finally:
+        p3d.set_fp64_arith(1)
+    for cap, (spec, y, _) in res.items():
+        assert np.array_equal(spec, spec_dev), cap
+        assert np.array_equal(y, y_dev), cap
+    rel = np.linalg.norm(y_dev / np.prod(gd) - x) / np.linalg.norm(x)
+    assert rel < 1e-13, rel
