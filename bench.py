@@ -203,7 +203,8 @@ def run_reference(args, rank, world):
     value = nbytes / dt / 1e9
     sample = (("all" if frac >= 1 else f"{frac:.4f} of the") +
               f" lines of each of the 6 stages of the {GD[0]}x{GD[1]}x{GD[2]} round trip per step "
-              f"(oracle C port of the reference path, IEEE double, OpenMP {cores} threads)")
+              f"(oracle C port of the reference path, IEEE double, batched line engine: 16 lines per "
+              f"vectorised Stockham FFT, OpenMP {cores} threads)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -213,8 +214,8 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_sample(reps=6):
-    """Oracle port timed on whole round trips (every line of every stage, about 10 s of CPU
+def cpu_baseline_sample(target_s=10.0):
+    """Oracle port timed on whole round trips (every line of every stage, about target_s of CPU
     work in all), all host cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
@@ -226,8 +227,10 @@ def cpu_baseline_sample(reps=6):
         for st in pyoracle.OraclePlan(types, g1, m1, g2, m2, d1, d2).stages():
             run, b_in, b_out, nlines = pyoracle.stage_lines_runner(st, nthreads=cores)
             runners.append((run, b_in + b_out, nlines, st["dim"] == idir))
+    t0 = time.perf_counter()
     for run, _, nlines, deriv in runners:  # warm: one pass over every stage
         run(0, nlines, deriv)
+    reps = max(3, int(target_s / max(time.perf_counter() - t0, 1e-3)))
     t0 = time.perf_counter()
     b_tot = 0.0
     for _ in range(reps):
@@ -237,7 +240,8 @@ def cpu_baseline_sample(reps=6):
     t_tot = time.perf_counter() - t0
     return {"value": b_tot / t_tot / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
             "sample": f"{reps} whole {GD[0]}x{GD[1]}x{GD[2]} FP64 round trips, every line of the 6 stages "
-                      f"(CPU oracle port of the reference path, OpenMP {cores} threads, {t_tot:.1f} s)"}
+                      f"(CPU oracle port of the reference path, batched line engine, OpenMP {cores} threads, "
+                      f"{t_tot:.1f} s)"}
 
 
 def load_traffic(kernel_key):

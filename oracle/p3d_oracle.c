@@ -394,6 +394,312 @@ static void deriv_line(double *x, int M, int r2c)
 }
 
 /* ------------------------------------------------------------------------------------------ */
+/* Batched line engine (the same definitions as fft_rec / r2c_line / c2r_line, computed B lines at
+ * a time): the lines are gathered into split re / im arrays with the line index fastest, so that
+ * every butterfly is a loop over B lines that the compiler vectorises, and a stage's lines are
+ * taken in blocks of B neighbours in memory.  Stockham passes of radix 4, 2 and 3, any other
+ * factor as a direct DFT of its length; twiddles from long double tables.  Used by the stage
+ * executor for C2C lines of any length and R2C / C2R lines of even length (half-length complex
+ * FFT with the standard even / odd split); results agree with the per-line path to rounding. */
+#define ORC_NB 16
+static int g_batched = 1;
+void orc_set_batched(int on) { g_batched = on ? 1 : 0; }
+
+typedef struct {
+  int h;            /* complex FFT length */
+  int ts;           /* table stride: the table holds N = h * ts points */
+  int nf, fac[40];
+  double *wr, *wi;  /* wr[t] = cos(2 pi t / N), wi[t] = -sin(2 pi t / N), t < N */
+} bplan;
+
+static void bplan_init(bplan *P, int h, int ts)
+{
+  static const long double TWO_PI = 6.283185307179586476925286766559005768L;
+  int m = h, t, N = h * ts;
+  P->h = h;
+  P->ts = ts;
+  P->nf = 0;
+  while (m > 1) {
+    int p;
+    if (m % 4 == 0) p = 4;
+    else if (m % 2 == 0) p = 2;
+    else if (m % 3 == 0) p = 3;
+    else {
+      for (p = 5; p * p <= m; p += 2)
+        if (m % p == 0) break;
+      if (p * p > m) p = m;
+    }
+    P->fac[P->nf++] = p;
+    m /= p;
+  }
+  P->wr = (double *)malloc(sizeof(double) * (size_t)(N > 0 ? N : 1));
+  P->wi = (double *)malloc(sizeof(double) * (size_t)(N > 0 ? N : 1));
+  for (t = 0; t < N; t++) {
+    long double a = TWO_PI * (long double)t / (long double)N;
+    P->wr[t] = (double)cosl(a);
+    P->wi[t] = (double)-sinl(a);
+  }
+}
+static void bplan_free(bplan *P)
+{
+  free(P->wr);
+  free(P->wi);
+}
+
+/* One Stockham pass of radix p: y[q + s(p pp + t)] = W^(t pp s) sum_r x[q + s(pp + r m)] w_p^(rt),
+ * W = exp(sign 2 pi i / h), for pp < m, q < s; element i is the B values at [i B, i B + B). */
+static void bpass(const bplan *P, int p, int m, int s, int sign, const double *restrict xr,
+                  const double *restrict xi, double *restrict yr, double *restrict yi)
+{
+  const int ts = P->ts, N = P->h * ts;
+  const double sg = sign < 0 ? 1.0 : -1.0; /* the table holds the forward (sign -1) angles */
+  int pp, q, l, r, t;
+  for (pp = 0; pp < m; pp++) {
+    for (q = 0; q < s; q++) {
+      const size_t i0 = (size_t)(q + s * pp);
+      const size_t o0 = (size_t)(q + s * p * pp);
+      if (p == 4) {
+        const double *a0r = xr + i0 * ORC_NB, *a0i = xi + i0 * ORC_NB;
+        const double *a1r = xr + (i0 + (size_t)s * m) * ORC_NB, *a1i = xi + (i0 + (size_t)s * m) * ORC_NB;
+        const double *a2r = xr + (i0 + (size_t)2 * s * m) * ORC_NB, *a2i = xi + (i0 + (size_t)2 * s * m) * ORC_NB;
+        const double *a3r = xr + (i0 + (size_t)3 * s * m) * ORC_NB, *a3i = xi + (i0 + (size_t)3 * s * m) * ORC_NB;
+        double *y0r = yr + o0 * ORC_NB, *y0i = yi + o0 * ORC_NB;
+        double *y1r = yr + (o0 + s) * ORC_NB, *y1i = yi + (o0 + s) * ORC_NB;
+        double *y2r = yr + (o0 + 2 * (size_t)s) * ORC_NB, *y2i = yi + (o0 + 2 * (size_t)s) * ORC_NB;
+        double *y3r = yr + (o0 + 3 * (size_t)s) * ORC_NB, *y3i = yi + (o0 + 3 * (size_t)s) * ORC_NB;
+        const int k1 = pp * s * ts, k2 = 2 * k1, k3 = 3 * k1;
+        const double w1r = P->wr[k1], w1i = sg * P->wi[k1], w2r = P->wr[k2], w2i = sg * P->wi[k2];
+        const double w3r = P->wr[k3], w3i = sg * P->wi[k3];
+        for (l = 0; l < ORC_NB; l++) {
+          const double t0r = a0r[l] + a2r[l], t0i = a0i[l] + a2i[l];
+          const double t1r = a0r[l] - a2r[l], t1i = a0i[l] - a2i[l];
+          const double t2r = a1r[l] + a3r[l], t2i = a1i[l] + a3i[l];
+          const double t3r = a1r[l] - a3r[l], t3i = a1i[l] - a3i[l];
+          /* b1 = t1 + sign i t3, b3 = t1 - sign i t3 */
+          const double b1r = t1r - sign * t3i, b1i = t1i + sign * t3r;
+          const double b3r = t1r + sign * t3i, b3i = t1i - sign * t3r;
+          const double b2r = t0r - t2r, b2i = t0i - t2i;
+          y0r[l] = t0r + t2r;
+          y0i[l] = t0i + t2i;
+          y1r[l] = b1r * w1r - b1i * w1i;
+          y1i[l] = b1r * w1i + b1i * w1r;
+          y2r[l] = b2r * w2r - b2i * w2i;
+          y2i[l] = b2r * w2i + b2i * w2r;
+          y3r[l] = b3r * w3r - b3i * w3i;
+          y3i[l] = b3r * w3i + b3i * w3r;
+        }
+      } else if (p == 2) {
+        const double *a0r = xr + i0 * ORC_NB, *a0i = xi + i0 * ORC_NB;
+        const double *a1r = xr + (i0 + (size_t)s * m) * ORC_NB, *a1i = xi + (i0 + (size_t)s * m) * ORC_NB;
+        double *y0r = yr + o0 * ORC_NB, *y0i = yi + o0 * ORC_NB;
+        double *y1r = yr + (o0 + s) * ORC_NB, *y1i = yi + (o0 + s) * ORC_NB;
+        const int k1 = pp * s * ts;
+        const double w1r = P->wr[k1], w1i = sg * P->wi[k1];
+        for (l = 0; l < ORC_NB; l++) {
+          const double br = a0r[l] - a1r[l], bi = a0i[l] - a1i[l];
+          y0r[l] = a0r[l] + a1r[l];
+          y0i[l] = a0i[l] + a1i[l];
+          y1r[l] = br * w1r - bi * w1i;
+          y1i[l] = br * w1i + bi * w1r;
+        }
+      } else if (p == 3) {
+        const double c3 = -0.5, s3 = (double)(sign * 0.866025403784438646763723170752936183L);
+        const double *a0r = xr + i0 * ORC_NB, *a0i = xi + i0 * ORC_NB;
+        const double *a1r = xr + (i0 + (size_t)s * m) * ORC_NB, *a1i = xi + (i0 + (size_t)s * m) * ORC_NB;
+        const double *a2r = xr + (i0 + (size_t)2 * s * m) * ORC_NB, *a2i = xi + (i0 + (size_t)2 * s * m) * ORC_NB;
+        double *y0r = yr + o0 * ORC_NB, *y0i = yi + o0 * ORC_NB;
+        double *y1r = yr + (o0 + s) * ORC_NB, *y1i = yi + (o0 + s) * ORC_NB;
+        double *y2r = yr + (o0 + 2 * (size_t)s) * ORC_NB, *y2i = yi + (o0 + 2 * (size_t)s) * ORC_NB;
+        const int k1 = pp * s * ts, k2 = 2 * k1;
+        const double w1r = P->wr[k1], w1i = sg * P->wi[k1], w2r = P->wr[k2], w2i = sg * P->wi[k2];
+        for (l = 0; l < ORC_NB; l++) {
+          const double t1r = a1r[l] + a2r[l], t1i = a1i[l] + a2i[l];
+          const double t2r = a1r[l] - a2r[l], t2i = a1i[l] - a2i[l];
+          const double mr = a0r[l] + c3 * t1r, mi = a0i[l] + c3 * t1i;
+          const double nr = -s3 * t2i, ni = s3 * t2r; /* i sign (sqrt3/2) t2 */
+          const double b1r = mr + nr, b1i = mi + ni, b2r = mr - nr, b2i = mi - ni;
+          y0r[l] = a0r[l] + t1r;
+          y0i[l] = a0i[l] + t1i;
+          y1r[l] = b1r * w1r - b1i * w1i;
+          y1i[l] = b1r * w1i + b1i * w1r;
+          y2r[l] = b2r * w2r - b2i * w2i;
+          y2i[l] = b2r * w2i + b2i * w2r;
+        }
+      } else { /* direct DFT of length p */
+        const int Np = N / p;
+        for (t = 0; t < p; t++) {
+          double *ytr = yr + (o0 + (size_t)t * s) * ORC_NB, *yti = yi + (o0 + (size_t)t * s) * ORC_NB;
+          const int kt = t * pp * s * ts;
+          const double wtr = P->wr[kt], wti = sg * P->wi[kt];
+          double accr[ORC_NB], acci[ORC_NB];
+          for (l = 0; l < ORC_NB; l++) accr[l] = acci[l] = 0.0;
+          for (r = 0; r < p; r++) {
+            const double *arr = xr + (i0 + (size_t)r * s * m) * ORC_NB, *ari = xi + (i0 + (size_t)r * s * m) * ORC_NB;
+            const int kr = ((r * t) % p) * Np;
+            const double cr = P->wr[kr], ci = sg * P->wi[kr];
+            for (l = 0; l < ORC_NB; l++) {
+              accr[l] += arr[l] * cr - ari[l] * ci;
+              acci[l] += arr[l] * ci + ari[l] * cr;
+            }
+          }
+          for (l = 0; l < ORC_NB; l++) {
+            ytr[l] = accr[l] * wtr - acci[l] * wti;
+            yti[l] = accr[l] * wti + acci[l] * wtr;
+          }
+        }
+      }
+    }
+  }
+}
+
+/* FFT of length P->h of the B lines in (*xr, *xi), using (*yr, *yi) as the second buffer; on
+ * return *xr / *xi point at the result. */
+static void bfft(const bplan *P, int sign, double **xr, double **xi, double **yr, double **yi)
+{
+  int f, s = 1, m = P->h;
+  for (f = 0; f < P->nf; f++) {
+    const int p = P->fac[f];
+    double *t;
+    m /= p;
+    bpass(P, p, m, s, sign, *xr, *xi, *yr, *yi);
+    t = *xr; *xr = *yr; *yr = t;
+    t = *xi; *xi = *yi; *yi = t;
+    s *= p;
+  }
+}
+
+/* compute_deriv_loc (deriv_line) on B lines of M complex values */
+static void deriv_lines(double *xr, double *xi, int M, int r2c)
+{
+  int g = r2c ? (M - 1) * 2 : M, mid = g / 2, i, l;
+  for (i = 0; i < M; i++) {
+    double *pr = xr + (size_t)i * ORC_NB, *pi = xi + (size_t)i * ORC_NB;
+    if (i == mid) {
+      for (l = 0; l < ORC_NB; l++) pr[l] = pi[l] = 0.0;
+      continue;
+    }
+    {
+      const double k = (double)(i < mid ? i : i - g);
+      for (l = 0; l < ORC_NB; l++) {
+        const double re = pr[l], im = pi[l];
+        pr[l] = -k * im;
+        pi[l] = k * re;
+      }
+    }
+  }
+}
+
+/* Whether a stage runs on the batched engine: C2C of any length, R2C / C2R of even length. */
+static int batched_ok(int kind, int nlog)
+{
+  if (kind == ORC_K_C2C_FWD || kind == ORC_K_C2C_BWD) return nlog >= 1;
+  if (kind == ORC_K_R2C || kind == ORC_K_C2R) return nlog >= 2 && nlog % 2 == 0;
+  return 0;
+}
+
+static void exec_stage_batched(int kind, int dt1, int dt2, int nin, int nout, int nlog, const long long s1[3],
+                               const long long s2[3], int L, int u, int v, long long nu, long long line0,
+                               long long lend, const double *in, double *out, int deriv, int nthreads)
+{
+  const int half = (kind == ORC_K_R2C || kind == ORC_K_C2R);
+  const int h = half ? nlog / 2 : nlog;
+  bplan P;
+  const long long nblk = (lend - line0 + ORC_NB - 1) / ORC_NB;
+  bplan_init(&P, h, half ? 2 : 1);
+#pragma omp parallel num_threads(nthreads)
+  {
+    const size_t cap = (size_t)((nin > nout ? nin : nout) + 2) * ORC_NB;
+    double *buf = (double *)malloc(sizeof(double) * 4 * cap);
+    long long blk;
+#pragma omp for schedule(static)
+    for (blk = 0; blk < nblk; blk++) {
+      double *xr = buf, *xi = buf + cap, *yr = buf + 2 * cap, *yi = buf + 3 * cap;
+      long long o1[ORC_NB], o2[ORC_NB];
+      const long long l0 = line0 + blk * ORC_NB;
+      const int nl = (int)(lend - l0 < ORC_NB ? lend - l0 : ORC_NB);
+      int l, j, k;
+      for (l = 0; l < ORC_NB; l++) {
+        const long long ln = l0 + (l < nl ? l : 0), iu = ln % nu, iv = ln / nu;
+        o1[l] = iu * s1[u] + iv * s1[v];
+        o2[l] = iu * s2[u] + iv * s2[v];
+      }
+      /* gather */
+      if (kind == ORC_K_R2C) {
+        for (j = 0; j < h; j++)
+          for (l = 0; l < ORC_NB; l++) {
+            xr[(size_t)j * ORC_NB + l] = in[o1[l] + (2 * j) * s1[L]];
+            xi[(size_t)j * ORC_NB + l] = in[o1[l] + (2 * j + 1) * s1[L]];
+          }
+      } else {
+        for (j = 0; j < nin; j++)
+          for (l = 0; l < ORC_NB; l++) {
+            xr[(size_t)j * ORC_NB + l] = in[2 * (o1[l] + j * s1[L])];
+            xi[(size_t)j * ORC_NB + l] = in[2 * (o1[l] + j * s1[L]) + 1];
+          }
+      }
+      if (kind == ORC_K_C2C_FWD || kind == ORC_K_C2C_BWD) {
+        bfft(&P, kind == ORC_K_C2C_FWD ? -1 : 1, &xr, &xi, &yr, &yi);
+      } else if (kind == ORC_K_R2C) {
+        /* Z = FFT_h(x[2m] + i x[2m+1]); X[k] = (Z[k] + conj Z[h-k]) / 2 - (i / 2) W^k (Z[k] - conj Z[h-k]) */
+        bfft(&P, -1, &xr, &xi, &yr, &yi);
+        for (k = 0; k <= h; k++) {
+          const double *ar = xr + (size_t)(k % h) * ORC_NB, *ai = xi + (size_t)(k % h) * ORC_NB;
+          const double *cr = xr + (size_t)((h - k) % h) * ORC_NB, *ci = xi + (size_t)((h - k) % h) * ORC_NB;
+          double *Xr = yr + (size_t)k * ORC_NB, *Xi = yi + (size_t)k * ORC_NB;
+          const double wr = P.wr[k], wi = P.wi[k];
+          for (l = 0; l < ORC_NB; l++) {
+            const double fer = 0.5 * (ar[l] + cr[l]), fei = 0.5 * (ai[l] - ci[l]);
+            const double dr = ar[l] - cr[l], di = ai[l] + ci[l];
+            const double for_ = 0.5 * di, foi = -0.5 * dr;
+            Xr[l] = fer + (for_ * wr - foi * wi);
+            Xi[l] = fei + (for_ * wi + foi * wr);
+          }
+        }
+        { double *t = xr; xr = yr; yr = t; t = xi; xi = yi; yi = t; }
+      } else { /* C2R: Z[k] = (X[k] + conj X[h-k]) + i W^-k (X[k] - conj X[h-k]); z = IFFT_h(Z) */
+        for (l = 0; l < ORC_NB; l++) {
+          xi[l] = 0.0;                   /* imag of DC ignored */
+          xi[(size_t)h * ORC_NB + l] = 0.0; /* imag of Nyquist ignored */
+        }
+        for (k = 0; k < h; k++) {
+          const double *ar = xr + (size_t)k * ORC_NB, *ai = xi + (size_t)k * ORC_NB;
+          const double *cr = xr + (size_t)(h - k) * ORC_NB, *ci = xi + (size_t)(h - k) * ORC_NB;
+          double *Zr = yr + (size_t)k * ORC_NB, *Zi = yi + (size_t)k * ORC_NB;
+          const double wr = P.wr[k], wi = -P.wi[k]; /* exp(+2 pi i k / n) */
+          for (l = 0; l < ORC_NB; l++) {
+            const double fer = ar[l] + cr[l], fei = ai[l] - ci[l];
+            const double dr = ar[l] - cr[l], di = ai[l] + ci[l];
+            const double for_ = dr * wr - di * wi, foi = dr * wi + di * wr;
+            Zr[l] = fer - foi;
+            Zi[l] = fei + for_;
+          }
+        }
+        { double *t = xr; xr = yr; yr = t; t = xi; xi = yi; yi = t; }
+        bfft(&P, 1, &xr, &xi, &yr, &yi);
+      }
+      if (deriv && dt2 == 2) deriv_lines(xr, xi, nout, kind == ORC_K_R2C);
+      /* scatter */
+      if (kind == ORC_K_C2R) {
+        for (j = 0; j < h; j++)
+          for (l = 0; l < nl; l++) {
+            out[o2[l] + (2 * j) * s2[L]] = xr[(size_t)j * ORC_NB + l];
+            out[o2[l] + (2 * j + 1) * s2[L]] = xi[(size_t)j * ORC_NB + l];
+          }
+      } else {
+        for (j = 0; j < nout; j++)
+          for (l = 0; l < nl; l++) {
+            out[2 * (o2[l] + j * s2[L])] = xr[(size_t)j * ORC_NB + l];
+            out[2 * (o2[l] + j * s2[L]) + 1] = xi[(size_t)j * ORC_NB + l];
+          }
+      }
+    }
+    free(buf);
+  }
+  (void)dt1;
+  bplan_free(&P);
+}
+
+/* ------------------------------------------------------------------------------------------ */
 /* Planner, build/templ.C. */
 
 /* swap0, templ.C:816-858: next memory order that makes dim L stride-1. */
@@ -577,13 +883,21 @@ int orc_exec_stage_lines(const orc_stage *S, const double *in, double *out, int 
   strides_of(&S->g2, s2);
   na = S->g1.gdims[a];
   nb = S->g1.gdims[b];
-  lineplan_init(&LP, kind, ti.r2r, nlog);
   if (ti.dt2 != 2) deriv = 0; /* compute_deriv_loc only acts on complex output, exec.C:245-286 */
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #else
   nthreads = 1;
 #endif
+  if (g_batched && batched_ok(kind, nlog)) {
+    /* blocks of lines neighbouring along the faster of the two other dims of the input */
+    const int fast_b = s1[b] < s1[a];
+    const long long lend = (line1 < 0 || line1 > na * nb) ? na * nb : line1;
+    exec_stage_batched(kind, ti.dt1, ti.dt2, nin, nout, nlog, s1, s2, L, fast_b ? b : a, fast_b ? a : b,
+                       fast_b ? nb : na, line0, lend, in, out, deriv, nthreads);
+    return 0;
+  }
+  lineplan_init(&LP, kind, ti.r2r, nlog);
 #pragma omp parallel num_threads(nthreads)
   {
     int maxn = (nin > nout ? nin : nout) + 2;

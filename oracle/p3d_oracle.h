@@ -93,6 +93,11 @@ typedef struct {
   int ok;
 } orc_plan3d;
 
+/* 1 (default): stages of C2C lines, and R2C / C2R lines of even length, run on the batched
+ * line engine (blocks of 16 lines, vectorised butterflies); 0: line by line.  Same results to
+ * rounding. */
+void orc_set_batched(int on);
+
 /* Builds the stage list of transform3D<T1,T2>::transform3D (build/templ.C:91-420). Returns 0 on
  * success, nonzero on an error the reference would print. */
 int orc_plan3d_make(const int types[3], const orc_grid *g1, const orc_grid *g2, orc_plan3d *p);
@@ -103,7 +108,8 @@ int orc_exec3d(const orc_plan3d *p, const double *in, double *out, int idir, int
 /* One 1D stage (transplan::exec, build/exec.C:522-622) on explicit grids. */
 int orc_exec_stage(const orc_stage *s, const double *in, double *out, int deriv, int nthreads);
 /* Same, restricted to lines [line0, line1) of the stage (line = index over the two batch dims,
- * first batch dim fastest); line1 < 0 means all lines.  Used to time bounded samples. */
+ * first batch dim fastest; on the batched engine the batch dim with the smaller input stride
+ * fastest); line1 < 0 means all lines.  Used to time bounded samples. */
 int orc_exec_stage_lines(const orc_stage *s, const double *in, double *out, int deriv, int nthreads,
                          long long line0, long long line1);
 /* Standalone spectral derivative (build/deriv.C:85-184) on a complex field, along logical dim

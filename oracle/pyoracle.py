@@ -31,7 +31,7 @@ def build(force: bool = False) -> str:
             and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(src),
                                                   os.path.getmtime(os.path.join(HERE, "p3d_oracle.h")))):
         return LIB_PATH
-    base = ["gcc", "-O2", "-fPIC", "-shared", "-std=gnu99", "-o", LIB_PATH + ".tmp", src, "-lm"]
+    base = ["gcc", "-O3", "-fPIC", "-shared", "-std=gnu99", "-o", LIB_PATH + ".tmp", src, "-lm"]
     try:
         subprocess.run(base[:1] + ["-fopenmp"] + base[1:], check=True, capture_output=True)
     except subprocess.CalledProcessError:
@@ -89,6 +89,7 @@ def lib():
         _lib.orc_compute_deriv.argtypes = [ctypes.POINTER(Grid), dp, dp, ctypes.c_int]
         _lib.orc_compute_deriv_axis.argtypes = [ctypes.POINTER(Grid), dp, dp, ctypes.c_int, ctypes.c_int]
         _lib.orc_type_info_get.argtypes = [ctypes.c_int, ctypes.POINTER(TypeInfo)]
+        _lib.orc_set_batched.argtypes = [ctypes.c_int]
         _lib.orc_swap0.argtypes = [ctypes.POINTER(ctypes.c_int * 3), ctypes.POINTER(ctypes.c_int * 3), ctypes.c_int]
         _lib.orc_find_order.argtypes = [ctypes.POINTER(ctypes.c_int * 3), ctypes.POINTER(Grid),
                                         ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_int * 3)]
@@ -160,6 +161,12 @@ def storage_shape(gdims, mo):
     for i in range(3):
         sd[mo[i]] = gdims[i]
     return (sd[2], sd[1], sd[0])
+
+
+def set_batched(on: bool):
+    """Stages of C2C lines and of even-length R2C / C2R lines on the batched line engine (True,
+    the default) or line by line (False); the same results to rounding."""
+    lib().orc_set_batched(1 if on else 0)
 
 
 class OraclePlan:
