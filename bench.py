@@ -710,6 +710,9 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=16)
     ap.add_argument("--kernels-only", choices=["fp64", "fp32"], default=None,
                     help="run only the device-resident round trip of that form (profiling runs)")
+    ap.add_argument("--e2e-only", choices=["fp64", "fp32"], default=None,
+                    help="run only the round trip of that form from and to page-locked host arrays "
+                         "(profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -723,6 +726,32 @@ def main():
         res = batch_workload(p3d, p3d.lib(), args.steps, args.warmup)
         if rank == 0:
             print(json.dumps({"workload": "batched uneven round trips", **res}), flush=True)
+        return
+    if args.e2e_only:
+        import ctypes
+        import p3dfft_gb300 as p3d
+        import build_lib
+        build_lib.build()
+        L = p3d.lib()
+        prec = 8 if args.e2e_only == "fp64" else 4
+        rdt = np.float64 if prec == 8 else np.float32
+        ft, bt = (FWD, BWD) if prec == 8 else (tuple(t - 1 for t in FWD), tuple(t - 1 for t in BWD))
+        f = p3d.Transform3D(ft, GD, MO1, GD2, MO2, -1, 0)
+        b = p3d.Transform3D(bt, GD2, MO2, GD, MO1, 0, -1)
+        hin = p3d.PinnedArray(p3d.storage_shape(GD, MO1), rdt)
+        hout = p3d.PinnedArray(p3d.storage_shape(GD, MO1), rdt)
+        hin.array[...] = np.random.default_rng(512).uniform(-1.0, 1.0, hin.array.shape)
+        d_spec = p3d.DeviceArray(S_C * prec // 8)
+        vp = ctypes.c_void_p
+        for k in range(args.warmup + args.steps):
+            if k == args.warmup:
+                L.p3dfft_gb300_synchronize()
+                t0 = time.perf_counter()
+            p3d.check(L.p3dfft_gb300_exec3d(f.handle, vp(hin.ptr), vp(d_spec.ptr), IDIR, 0))
+            p3d.check(L.p3dfft_gb300_exec3d(b.handle, vp(d_spec.ptr), vp(hout.ptr), -1, 0))
+        L.p3dfft_gb300_synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps)
+        print(json.dumps({"e2e_only": args.e2e_only, "grid": list(GD), "ms_per_round_trip": ms}), flush=True)
         return
     if args.kernels_only:
         import ctypes
