@@ -982,9 +982,10 @@ def main():
             "outside_stage_kernels": modes_ms["direct_both_not_pipelined"] - link_ms - dev_ms,
             "overlapped_by_link_pipelining": modes_ms["direct_both_not_pipelined"] - e2e_ms,
             # the pipelined schedule's floor: the link-bound x stages, the z stages (they need the
-            # whole field) and one y slab in each direction outside the link time
+            # whole field) and the thin y slab (1/16 of the planes) in each direction outside the
+            # link time
             "pipelined_schedule_floor": link_ms + fwd_ms[2] + bwd_ms[0] + (fwd_ms[1] + bwd_ms[1]) / max(
-                2, min(16, int(os.environ.get("P3DFFT_GB300_PIPE_SLABS", "8")))),
+                2, int(os.environ.get("P3DFFT_GB300_LINK_TAIL", "16"))),
             "forward_stages": fwd_ms, "backward_stages": bwd_ms,
             "host_link_GBps": {"h2d_in_x_r2c": S_R / (fwd_ms[0] * 1e-3) / 1e9,
                                "d2h_in_x_c2r": S_R / (bwd_ms[-1] * 1e-3) / 1e9}}

@@ -1102,7 +1102,34 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
   int f = 1;
   while (f < 16 && ((f * u[0]) % 16 || (f * u[1]) % 16 || (f * u[2]) % 16 || (f * u[3]) % 16)) f++;
   const int len = a.g1.gdims[sd];
-  const int per = ((len + NS - 1) / NS + f - 1) / f * f;
+  // Slab starts along sd.  Staged copies: NS equal slabs.  A link stage: a few large slabs and one
+  // thin slab where the neighbour stage runs outside the link time (last for the forward, where
+  // the neighbour follows the link stage; first for the backward, where it leads), since each
+  // slab boundary stalls the link stage (its slowest CTA) and the thin slab bounds the exposed
+  // neighbour work; the thin link slab must still outlast one large neighbour slab.  Measured on
+  // the 512^3 FP64 round trip (large slabs, thin = len / TAILDIV): 3, 16: 12.65 ms; 4, 32: 12.74;
+  // 3, 32: 12.78; 5, 32: 12.79; 3, 64: 12.87; 7, 8 (8 equal slabs): 12.93; 2, 32: 13.28.
+  static int NBIG = 0, TAILDIV = 0;  // P3DFFT_GB300_LINK_SLABS (default 3), P3DFFT_GB300_LINK_TAIL (16)
+  if (!NBIG) {
+    const char *e1 = getenv("P3DFFT_GB300_LINK_SLABS"), *e2 = getenv("P3DFFT_GB300_LINK_TAIL");
+    NBIG = e1 ? std::max(1, std::min(kMaxSlabs - 1, atoi(e1))) : 3;
+    TAILDIV = e2 ? std::max(2, atoi(e2)) : 16;
+  }
+  auto up = [&](int v) { return (v + f - 1) / f * f; };
+  std::vector<int> cuts;  // slab starts (multiples of f), then len
+  const int thin = link ? up(std::max(1, len / TAILDIV)) : 0;
+  // the large slabs cover [lo, hi); the thin one [0, lo) (backward) or [hi, len) (forward)
+  const int lo = link == 2 ? thin : 0, hi = link == 1 ? (len - thin) / f * f : len;
+  if (link && thin < len && hi - lo >= NBIG * f) {
+    const int per = up((hi - lo + NBIG - 1) / NBIG);
+    if (link == 2) cuts.push_back(0);
+    for (int c = lo; c < hi; c += per) cuts.push_back(c);
+    if (link == 1) cuts.push_back(hi);
+  } else {
+    const int per = up((len + NS - 1) / NS);
+    for (int c = 0; c < len; c += per) cuts.push_back(c);
+  }
+  cuts.push_back(len);
   cudaStream_t ms = cur_stream(), ps = g_pipe_stream, cs = g_copy_stream;
   // the second stream (and the copy stream) start after everything already queued on the
   // library stream
@@ -1117,8 +1144,9 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
   const ExecCtx *ca = link == 1 ? &pc : prev, *cb = link == 1 ? prev : &pc;
   cudaStream_t sa = link == 1 ? ps : ms, sb = link == 1 ? ms : ps;
   int rc = E_OK;
-  for (int c = 0, k = 0; c < len && rc == E_OK; c += per, k++) {
-    SlabBox box{sd, c, std::min(per, len - c)};
+  for (int k = 0; k + 1 < (int)cuts.size() && rc == E_OK; k++) {
+    const int c = cuts[k];
+    SlabBox box{sd, c, cuts[k + 1] - c};
     if (host_in) {
       if (cudaMemcpyAsync(static_cast<unsigned char *>(const_cast<void *>(src)) + (size_t)c * u[0],
                           static_cast<const unsigned char *>(host_in) + (size_t)c * u[0], (size_t)box.m * u[0],

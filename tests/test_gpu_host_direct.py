@@ -167,7 +167,7 @@ def test_pinned_host_stages_pipelined_equal_device(gpu, prec, mo1, mo2, sliced):
                                               (1, (512, 96, 90), (1, 0, 2), (2, 1, 0))])
 def test_link_pipelined_ragged_slabs_and_native_fp64(gpu, arith, gd, mo1, mo2):
     """Direct host input / output with the link stages on capped persistent grids beside their
-    neighbour stages: slab counts that do not divide the slab dim (70 and 90 planes in 8 slabs),
+    neighbour stages: slab dims of 70 and 90 planes (large slabs and a thin one, ragged),
     native FP64 arithmetic (IEEE intermediates), and another memory-order pair; each equal bit for
     bit to the same round trip stage after stage (cap 0) and to device-resident arrays."""
     p3d = gpu
