@@ -211,3 +211,35 @@ def test_link_pipelined_ragged_slabs_and_native_fp64(gpu, arith, gd, mo1, mo2):
         assert np.array_equal(y, y_dev), cap
     rel = np.linalg.norm(y_dev / np.prod(gd) - x) / np.linalg.norm(x)
     assert rel < 1e-13, rel
+
+
+@pytest.mark.parametrize("side", ["in", "out"])
+def test_link_pipeline_one_side_direct(gpu, side):
+    """One host array read (or written) directly with its link stage pipelined beside the
+    neighbour stage, the other staged through HBM with per-slab copies (FP32, 50 MB fields): the
+    result equal bit for bit to device-resident arrays."""
+    p3d = gpu
+    gd = (512, 160, 160)
+    gd2 = (257, gd[1], gd[2])
+    f = p3d.Transform3D([p3d.TYPE_IDS["R2CFFT_S"], p3d.TYPE_IDS["CFFT_FORWARD_S"],
+                         p3d.TYPE_IDS["CFFT_FORWARD_S"]], gd, (0, 1, 2), gd2, (1, 2, 0), -1, 0)
+    b = p3d.Transform3D([p3d.TYPE_IDS["C2RFFT_S"], p3d.TYPE_IDS["CFFT_BACKWARD_S"],
+                         p3d.TYPE_IDS["CFFT_BACKWARD_S"]], gd2, (1, 2, 0), gd, (0, 1, 2), 0, -1)
+    x = seeded_field(f.in_shape(), seed=77, dtype=np.float32)
+    hin = p3d.PinnedArray(x.shape, np.float32)
+    hin.array[...] = x
+    hout = p3d.PinnedArray(x.shape, np.float32)
+    d_s = p3d.DeviceArray(int(np.prod(f.out_shape())) * 8)
+    try:
+        p3d.set_host_direct(side)
+        f.exec(hin.array, d_s, idir=2)
+        spec = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
+        b.exec(d_s, hout.array)
+    finally:
+        p3d.set_host_direct(True)
+    d_in, d_out = p3d.DeviceArray(x.nbytes), p3d.DeviceArray(x.nbytes)
+    d_in.upload(x)
+    f.exec(d_in, d_s, idir=2)
+    assert np.array_equal(spec, d_s.download(np.empty(f.out_shape(), f.out_dtype())))
+    b.exec(d_s, d_out)
+    assert np.array_equal(hout.array, d_out.download(np.empty_like(x)))
