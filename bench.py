@@ -924,14 +924,15 @@ def main():
     hin.array[...] = x
     n_e2e = max(3, min(args.steps, 20))
 
-    def e2e_run():
+    def e2e_run(pin=None, pout=None):
+        pin, pout = pin or hin.ptr, pout or hout.ptr
         for _ in range(2):
-            step(hin.ptr, hout.ptr)
+            step(pin, pout)
         L.p3dfft_gb300_synchronize()
         barrier()
         t0 = time.perf_counter()
         for _ in range(n_e2e):
-            step(hin.ptr, hout.ptr)  # host in (exec_deriv) and host out (exec), each call synchronous
+            step(pin, pout)  # host in (exec_deriv) and host out (exec), each call synchronous
         L.p3dfft_gb300_synchronize()
         return max_over_ranks((time.perf_counter() - t0) / n_e2e * 1e3)
 
@@ -955,6 +956,15 @@ def main():
     p3d.set_link_ctas(0)
     modes_ms["direct_both_not_pipelined"] = e2e_run()
     p3d.set_link_ctas(-1)
+    # pageable host arrays (plain numpy memory, pages already touched): staged through HBM by the
+    # copies (default), or read / written in place through the host's page tables
+    x_pg, y_pg = np.array(x), np.zeros_like(x)
+    modes_ms["pageable_staged"] = e2e_run(x_pg.ctypes.data, y_pg.ctypes.data)
+    p3d.set_pageable_direct(True)
+    if p3d.get_pageable_direct() == 1:
+        modes_ms["pageable_direct"] = e2e_run(x_pg.ctypes.data, y_pg.ctypes.data)
+    p3d.set_pageable_direct(False)
+    del x_pg, y_pg
     e2e_staged_ms = modes_ms["staged_both"]
     e2e_ms = modes_ms["direct_both"]
     e2e = {"value": ALG_BYTES * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": S_R,

@@ -56,6 +56,14 @@ int p3dfft_gb300_get_host_pipeline(void);
  * variable's), -1 for the default. */
 void p3dfft_gb300_set_link_ctas(int n);
 int p3dfft_gb300_get_link_ctas(void);
+/* 1: pageable host arrays (plain malloc / new) are read and written by the first / last stage in
+ * place, like page-locked ones, where the device accesses pageable memory through the host's
+ * page tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables, e.g. Grace with NVLink-C2C);
+ * elsewhere, and with 0 (the default), pageable arrays are staged through HBM.
+ * P3DFFT_GB300_PAGEABLE_DIRECT=1 sets 1 at start-up.  get: 1 on, 0 off, -1 not supported by the
+ * device. */
+void p3dfft_gb300_set_pageable_direct(int on);
+int p3dfft_gb300_get_pageable_direct(void);
 /* Arithmetic of FP64 stages: 1 = float-float on the FP32 pipe (default; ~48-bit significand,
  * ~1e-14 relative L2 per 3D transform), 0 = native FP64 DFMA (slow on GB300).  The initial value
  * can be set with P3DFFT_GB300_FP64_ARITH=native. */

@@ -655,8 +655,35 @@ static int host_direct_mode() {
   }
   return g_host_direct;
 }
+// Pageable host memory read / written by the kernels in place: only where the device accesses
+// pageable memory coherently through the host's page tables (address translation over
+// NVLink-C2C, as on Grace; cudaDevAttrPageableMemoryAccessUsesHostPageTables), not where access
+// would migrate pages.  -1: P3DFFT_GB300_PAGEABLE_DIRECT at first use ("0" off; default off).
+static int g_pageable_direct = -1;
+static int pageable_access_ok() {  // 1: the device reads pageable memory through the host's tables
+  static int ok = -1;
+  if (ok < 0) {
+    int dev = 0, pm = 0, hpt = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pm, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    ok = pm && hpt ? 1 : 0;
+  }
+  return ok;
+}
+static bool pageable_direct() {
+  if (g_pageable_direct < 0) {
+    const char *e = getenv("P3DFFT_GB300_PAGEABLE_DIRECT");
+    g_pageable_direct = (e && e[0] == '1') ? 1 : 0;
+  }
+  return g_pageable_direct == 1 && pageable_access_ok() == 1;
+}
 // Page-locked host memory (cudaHostAlloc / cudaHostRegister) is addressable by kernels over
-// NVLink-C2C; returns its device-side address, or nullptr for any other pointer.
+// NVLink-C2C; returns its device-side address (pageable memory: the pointer itself when
+// pageable_direct()), or nullptr for any other pointer.
 static void *mapped_host_ptr(const void *p) {
   if (!p || !host_direct_mode()) return nullptr;
   cudaPointerAttributes a;
@@ -664,7 +691,9 @@ static void *mapped_host_ptr(const void *p) {
     cudaGetLastError();
     return nullptr;
   }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  if (a.type == cudaMemoryTypeUnregistered && pageable_direct()) return const_cast<void *>(p);
+  return nullptr;
 }
 
 static bool ensure_buf(void **p, size_t *have, size_t need) {
@@ -1678,6 +1707,11 @@ void p3dfft_gb300_set_stream(void *s) { g_stream = (cudaStream_t)s; }
 void p3dfft_gb300_set_sync(int s) { g_sync = s ? 1 : 0; }
 void p3dfft_gb300_set_host_pipeline(int on) { g_host_pipe = on ? 1 : 0; }
 void p3dfft_gb300_set_link_ctas(int n) { g_link_ctas = n < 0 ? -1 : n; }
+void p3dfft_gb300_set_pageable_direct(int on) { g_pageable_direct = on ? 1 : 0; }
+int p3dfft_gb300_get_pageable_direct(void) {
+  if (!ensure_device()) return 0;
+  return pageable_direct() ? 1 : (pageable_access_ok() ? 0 : -1);
+}
 int p3dfft_gb300_get_link_ctas(void) { return link_ctas_set(); }
 int p3dfft_gb300_get_host_pipeline(void) { return pipeline_host_stages() ? 1 : 0; }
 void p3dfft_gb300_set_host_direct(int on) { g_host_direct = on == 1 ? 3 : (on == 2 ? 1 : (on == 3 ? 2 : 0)); }

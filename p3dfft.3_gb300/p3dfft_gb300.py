@@ -65,6 +65,8 @@ def lib():
         "p3dfft_gb300_get_host_pipeline": ([], ctypes.c_int),
         "p3dfft_gb300_set_link_ctas": ([ctypes.c_int], None),
         "p3dfft_gb300_get_link_ctas": ([], ctypes.c_int),
+        "p3dfft_gb300_set_pageable_direct": ([ctypes.c_int], None),
+        "p3dfft_gb300_get_pageable_direct": ([], ctypes.c_int),
         "p3dfft_gb300_set_fp64_arith": ([ctypes.c_int], None), "p3dfft_gb300_get_fp64_arith": ([], ctypes.c_int),
         "p3dfft_gb300_set_reference_compat": ([ctypes.c_int], None),
         "p3dfft_gb300_get_reference_compat": ([], ctypes.c_int),
@@ -241,6 +243,17 @@ def set_link_ctas(n: int):
 
 def get_link_ctas() -> int:
     return int(lib().p3dfft_gb300_get_link_ctas())
+
+
+def set_pageable_direct(on: bool):
+    """Pageable host arrays read / written in place by the end stages where the device walks the
+    host's page tables (True), or staged through HBM (False, the default)."""
+    lib().p3dfft_gb300_set_pageable_direct(1 if on else 0)
+
+
+def get_pageable_direct() -> int:
+    """1 on, 0 off, -1 not supported by the device."""
+    return int(lib().p3dfft_gb300_get_pageable_direct())
 
 
 def set_stream(stream_ptr: int):

@@ -243,3 +243,41 @@ def test_link_pipeline_one_side_direct(gpu, side):
     assert np.array_equal(spec, d_s.download(np.empty(f.out_shape(), f.out_dtype())))
     b.exec(d_s, d_out)
     assert np.array_equal(hout.array, d_out.download(np.empty_like(x)))
+
+
+@pytest.mark.parametrize("gd", [(64, 48, 40), (512, 128, 80)])
+def test_pageable_arrays_in_place_equal_device(gpu, gd):
+    """Pageable host arrays (plain numpy memory; the output's pages untouched before the call) read
+    and written in place by the end stages through the host's page tables, the larger field with
+    the link pipeline: equal bit for bit to device-resident arrays and to the staged path."""
+    p3d = gpu
+    p3d.set_fp64_arith(1)
+    gd2 = (gd[0] // 2 + 1, gd[1], gd[2])
+    f = p3d.Transform3D([p3d.TYPE_IDS["R2CFFT_D"], p3d.TYPE_IDS["CFFT_FORWARD_D"],
+                         p3d.TYPE_IDS["CFFT_FORWARD_D"]], gd, (0, 1, 2), gd2, (1, 2, 0), -1, 0)
+    b = p3d.Transform3D([p3d.TYPE_IDS["C2RFFT_D"], p3d.TYPE_IDS["CFFT_BACKWARD_D"],
+                         p3d.TYPE_IDS["CFFT_BACKWARD_D"]], gd2, (1, 2, 0), gd, (0, 1, 2), 0, -1)
+    x = seeded_field(f.in_shape(), seed=sum(gd) + 5)
+    d_s = p3d.DeviceArray(int(np.prod(f.out_shape())) * 16)
+    res = {}
+    try:
+        for direct in (False, True):
+            p3d.set_pageable_direct(direct)
+            if direct and p3d.get_pageable_direct() != 1:
+                pytest.skip("the device does not access pageable memory through the host's page tables")
+            y = np.empty_like(x)
+            f.exec(x, d_s, idir=2)
+            spec = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
+            b.exec(d_s, y)
+            res[direct] = (spec, y)
+    finally:
+        p3d.set_pageable_direct(False)
+    d_in, d_out = p3d.DeviceArray(x.nbytes), p3d.DeviceArray(x.nbytes)
+    d_in.upload(x)
+    f.exec(d_in, d_s, idir=2)
+    spec_dev = d_s.download(np.empty(f.out_shape(), f.out_dtype()))
+    b.exec(d_s, d_out)
+    y_dev = d_out.download(np.empty_like(x))
+    for direct, (spec, y) in res.items():
+        assert np.array_equal(spec, spec_dev), direct
+        assert np.array_equal(y, y_dev), direct
