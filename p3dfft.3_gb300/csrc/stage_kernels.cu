@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(256) k_stage(KParams p) {
   using S = typename O::S;
   using G = typename O::G;
   constexpr int SH = E::PADSH;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];  // (as declared in fast_stage.cuh)
   C *b0 = reinterpret_cast<C *>(smem_raw);
   C *b1 = b0 + (size_t)p.TB * p.nfl * p.ls;
   const int tile = blockIdx.x % p.ntile;
