@@ -917,6 +917,15 @@ def main():
     # the dominant kernel's per-point counts and DRAM traffic come from the committed ncu
     # summaries under profiles/ (one small-case capture each), not from this run
     roofline["counts_source"] = "profiles/ (committed ncu summaries: TRAFFIC, INSTR, FP32OPS lines)"
+    if n_sm and clocks.get("sm_mhz"):
+        # the step's FFT flops (2.5 V log2 V per direction) against the native FP64 pipe's peak
+        # (DFMA at the 1.75 thread instructions per SM per clock measured on this part, 2 flops
+        # each): what the float-float arithmetic delivers beyond that pipe
+        fl = 2 * 2.5 * GD[0] * GD[1] * GD[2] * np.log2(float(GD[0] * GD[1] * GD[2]))
+        pk = 2 * 1.75 * n_sm * clocks["sm_mhz"] * 1e6
+        roofline["fp64_pipe_equivalent"] = {"flops_per_step": fl, "achieved_tflops": fl / (ms_step * 1e-3) / 1e12,
+                                            "native_fp64_peak_tflops": pk / 1e12,
+                                            "ratio_to_native_peak": fl / (ms_step * 1e-3) / pk}
 
     # ---- e2e: pinned host buffers through the public API ----
     hin = p3d.PinnedArray(p3d.storage_shape(GD, MO1), np.float64)
