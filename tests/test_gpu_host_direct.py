@@ -245,20 +245,23 @@ def test_link_pipeline_one_side_direct(gpu, side):
     assert np.array_equal(hout.array, d_out.download(np.empty_like(x)))
 
 
-@pytest.mark.parametrize("gd", [(64, 48, 40), (512, 128, 80)])
-def test_pageable_arrays_in_place_equal_device(gpu, gd):
+@pytest.mark.parametrize("prec,gd,mo1,mo2", [(8, (64, 48, 40), (0, 1, 2), (1, 2, 0)),
+                                              (8, (512, 128, 80), (0, 1, 2), (1, 2, 0)),
+                                              (4, (512, 160, 128), (2, 0, 1), (0, 1, 2))])
+def test_pageable_arrays_in_place_equal_device(gpu, prec, gd, mo1, mo2):
     """Pageable host arrays (plain numpy memory; the output's pages untouched before the call) read
-    and written in place by the end stages through the host's page tables, the larger field with
+    and written in place by the end stages through the host's page tables, the larger fields with
     the link pipeline: equal bit for bit to device-resident arrays and to the staged path."""
     p3d = gpu
     p3d.set_fp64_arith(1)
     gd2 = (gd[0] // 2 + 1, gd[1], gd[2])
-    f = p3d.Transform3D([p3d.TYPE_IDS["R2CFFT_D"], p3d.TYPE_IDS["CFFT_FORWARD_D"],
-                         p3d.TYPE_IDS["CFFT_FORWARD_D"]], gd, (0, 1, 2), gd2, (1, 2, 0), -1, 0)
-    b = p3d.Transform3D([p3d.TYPE_IDS["C2RFFT_D"], p3d.TYPE_IDS["CFFT_BACKWARD_D"],
-                         p3d.TYPE_IDS["CFFT_BACKWARD_D"]], gd2, (1, 2, 0), gd, (0, 1, 2), 0, -1)
-    x = seeded_field(f.in_shape(), seed=sum(gd) + 5)
-    d_s = p3d.DeviceArray(int(np.prod(f.out_shape())) * 16)
+    S = "D" if prec == 8 else "S"
+    f = p3d.Transform3D([p3d.TYPE_IDS[f"R2CFFT_{S}"], p3d.TYPE_IDS[f"CFFT_FORWARD_{S}"],
+                         p3d.TYPE_IDS[f"CFFT_FORWARD_{S}"]], gd, mo1, gd2, mo2, -1, 0)
+    b = p3d.Transform3D([p3d.TYPE_IDS[f"C2RFFT_{S}"], p3d.TYPE_IDS[f"CFFT_BACKWARD_{S}"],
+                         p3d.TYPE_IDS[f"CFFT_BACKWARD_{S}"]], gd2, mo2, gd, mo1, 0, -1)
+    x = seeded_field(f.in_shape(), seed=sum(gd) + 5, dtype=np.float64 if prec == 8 else np.float32)
+    d_s = p3d.DeviceArray(int(np.prod(f.out_shape())) * 2 * prec)
     res = {}
     try:
         for direct in (False, True):
