@@ -647,6 +647,15 @@ static int link_ctas(int prec) {
   }
   return sms * (prec == 4 ? 2 : 1);
 }
+// Tile counters for the link stage's persistent CTAs (P3DFFT_GB300_TILE_CTR=0: fixed grid stride)
+static bool tile_ctr_on() {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = getenv("P3DFFT_GB300_TILE_CTR");
+    on = (e && e[0] == '0') ? 0 : 1;
+  }
+  return on == 1;
+}
 static int g_host_direct = -1;
 static int host_direct_mode() {
   if (g_host_direct < 0) {
@@ -765,7 +774,8 @@ static void fill_stage_desc(const Plan *P, const Stage &s, bool deriv, StageDesc
 // layouts (the strides of the whole field).
 struct SlabBox {
   int sd, c, m;
-  int ctas = 0;  // the stage's grid cap (StageDesc::max_ctas)
+  int ctas = 0;            // the stage's grid cap (StageDesc::max_ctas)
+  int *ctr = nullptr;      // and its zeroed tile counter (StageDesc::tile_ctr)
 };
 
 // engine_override >= 0 replaces the plan's tuned engine choice for this stage (0 = heuristic);
@@ -818,6 +828,7 @@ static int run_stage(const Plan *P, const Stage &s, const void *src, void *dst, 
       dst = static_cast<unsigned char *>(dst) + (size_t)box->c * d.s2[sd] * t.dt2 * P->prec;
       d.d1[sd] = d.d2[sd] = box->m;
       d.max_ctas = box->ctas;
+      d.tile_ctr = box->ctr;
       if (d.sin) d.sin += (long long)box->c * d.mi[sd];
       if (d.sout) d.sout += (long long)box->c * d.mo[sd];
     }
@@ -1172,6 +1183,15 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
   // is the link stage
   const ExecCtx *ca = link == 1 ? &pc : prev, *cb = link == 1 ? prev : &pc;
   cudaStream_t sa = link == 1 ? ps : ms, sb = link == 1 ? ms : ps;
+  // FP64: the link stage's CTAs take their tiles from a counter per slab, zeroed ahead of its
+  // slabs on its own stream, so that the CTAs of a slab finish within about one tile of each
+  // other (512^3 round trip 12.61 against 12.67 ms with a fixed grid stride; FP32, whose tiles
+  // are shorter, 6.02 against 5.95 ms, keeps the grid stride)
+  int *ctrs = (link && link_ctas > 0 && P->prec == 8 && tile_ctr_on()) ? tile_counters(g_tabs) : nullptr;
+  if (ctrs && cudaMemsetAsync(ctrs, 0, sizeof(int) * kTileCounters, ps) != cudaSuccess) {
+    cudaGetLastError();
+    ctrs = nullptr;
+  }
   int rc = E_OK;
   for (int k = 0; k + 1 < (int)cuts.size() && rc == E_OK; k++) {
     const int c = cuts[k];
@@ -1186,6 +1206,7 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
       }
     }
     box.ctas = link == 1 ? link_ctas : 0;
+    box.ctr = (link == 1 && ctrs) ? ctrs + k : nullptr;
     t_ctx = ca;
     rc = run_stage(P, a, src, mid, da, nullptr, nullptr, -1, lka, &box);
     t_ctx = prev;
@@ -1195,6 +1216,7 @@ static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void
       break;
     }
     box.ctas = link == 2 ? link_ctas : 0;
+    box.ctr = (link == 2 && ctrs) ? ctrs + k : nullptr;
     t_ctx = cb;
     rc = run_stage(P, b, mid, dst, db, nullptr, nullptr, -1, lkb, &box);
     t_ctx = prev;

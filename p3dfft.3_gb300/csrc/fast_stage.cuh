@@ -72,6 +72,9 @@ struct FParams {
   int tma_mode;  // 1: lines contiguous (boxes of one line's floats x TB lines); 2: tile dim
                  // contiguous (C2C: boxes of TB points' floats x rows of the line dim)
   int *status;
+  // k_fast_persist: a zeroed counter from which the CTAs take their tiles after the first (the
+  // CTA that finishes first takes the next), or nullptr for a fixed grid stride
+  int *tile_ctr;
 };
 
 // The FP32 split-twiddle policy the build instantiates: twiddle powers read from the tables
@@ -1046,9 +1049,16 @@ inline bool fast_persist_ok(int kind, int n, int ffin, int ffout) {
 template <class O, int KIND, int N, int FF = 0>
 __global__ void __launch_bounds__(FastShape<N>::BLOCK, FAST_PERSIST_MINB)
     k_fast_persist(FParams p) {
+  __shared__ int nxt;
   for (int t = blockIdx.x;;) {
     fk_tile<O, KIND, N, FF>(p, t, p.in, p.out);
-    t += gridDim.x;
+    if (p.tile_ctr) {
+      if (threadIdx.x == 0) nxt = (int)gridDim.x + atomicAdd(p.tile_ctr, 1);
+      __syncthreads();
+      t = nxt;
+    } else {
+      t += gridDim.x;
+    }
     if (t >= p.ntotal) break;
     __syncthreads();
   }

@@ -50,6 +50,7 @@ struct StageDesc {
   // specialised kernels: at most this many CTAs, each walking the tiles with a grid stride
   // (0: one CTA per tile)
   int max_ctas = 0;
+  int *tile_ctr = nullptr;  // with max_ctas: a zeroed counter for dynamic tile assignment
   // Float-float intermediate fields (float-float arithmetic, specialised C2C / R2C / C2R kernels
   // only; other launches with these set fail with E_UNSUPPORTED).  ffin: the input field holds
   // packed float-float values scaled per stored line; the scale of the value at logical
@@ -97,6 +98,9 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
 // Whether the stage runs on a specialised kernel that honours StageDesc::max_ctas (nothing is
 // launched; the stage's tables are loaded into `tabs`).
 bool stage_cap_ok(const StageDesc &d, const void *in, void *out, int arith, DeviceTables *tabs);
+// Device counters for capped launches (StageDesc::tile_ctr), kTileCounters of them, or nullptr.
+constexpr int kTileCounters = 16;
+int *tile_counters(DeviceTables *tabs);
 
 // ---- grouped launches (batch runtime) ----
 // One stage of one transform with its buffers, as the executor would launch it.

@@ -699,9 +699,11 @@ struct DeviceTables {
   // key: (N, format + 8 pass) format 0 = double, 1 = float, 2 = float-float, 3 = packed float-float
   std::map<std::pair<int, int>, void *> tabs;
   int *status = nullptr;  // device status word: nonzero after a kernel's bounded wait ran out
+  int *ctrs = nullptr;    // kTileCounters tile counters of capped launches
   ~DeviceTables() {
     for (auto &kv : tabs) cudaFree(kv.second);
     if (status) cudaFree(status);
+    if (ctrs) cudaFree(ctrs);
   }
   // pass = 1: the specialised kernels' per-pass twiddle rows of FFT length N; pass = 2: the
   // Bluestein engine's tables for length N
@@ -740,6 +742,16 @@ DeviceTables *tables_create() {
   return t;
 }
 void tables_destroy(DeviceTables *t) { delete t; }
+int *tile_counters(DeviceTables *t) {
+  if (!t) return nullptr;
+  std::lock_guard<std::mutex> g(t->mu);
+  if (!t->ctrs && cudaMalloc(&t->ctrs, sizeof(int) * kTileCounters) != cudaSuccess) {
+    cudaGetLastError();
+    t->ctrs = nullptr;
+  }
+  return t->ctrs;
+}
+
 int device_status(DeviceTables *t, bool clear) {
   if (!t || !t->status) return 0;
   int v = 0;
@@ -1223,6 +1235,7 @@ int launch_stage(const StageDesc &d, const void *in, void *out, int arith, cudaS
     q.tma_mode = 0;
     q.tma_store = 0;
     q.status = nullptr;
+    q.tile_ctr = d.max_ctas > 0 ? d.tile_ctr : nullptr;
     fa.tma = 0;
     if (fast_prep) {
       *fast_prep = fa;
