@@ -65,3 +65,31 @@ def test_c2r_to_real_length_one_is_rejected_at_plan_time(p3d):
     with pytest.raises(p3d.P3DFFTError, match="PLAN"):
         p3d.Transform3D([p3d.C2RFFT_D, p3d.CFFT_BACKWARD_D, p3d.CFFT_BACKWARD_D], (1, 4, 4), (0, 1, 2),
                         (1, 4, 4), (0, 1, 2), 0, -1)
+
+
+def test_host_io_switches_round_trip(p3d, monkeypatch):
+    """The host-I/O switches hold what they are set to: the link-stage CTA cap (-1 back to the
+    default, which the environment variable overrides) and the host pipeline; the pageable switch
+    reports "not on" without a device."""
+    import torch
+    monkeypatch.delenv("P3DFFT_GB300_LINK_CTAS", raising=False)
+    try:
+        p3d.set_link_ctas(37)
+        assert p3d.get_link_ctas() == 37
+        p3d.set_link_ctas(0)
+        assert p3d.get_link_ctas() == 0
+        p3d.set_link_ctas(-1)
+        assert p3d.get_link_ctas() == -1
+        monkeypatch.setenv("P3DFFT_GB300_LINK_CTAS", "200")
+        assert p3d.get_link_ctas() == 200
+        p3d.set_host_pipeline(False)
+        assert p3d.get_host_pipeline() is False
+    finally:
+        p3d.set_link_ctas(-1)
+        p3d.set_host_pipeline(True)
+    if not torch.cuda.is_available():
+        p3d.set_pageable_direct(True)
+        try:
+            assert p3d.get_pageable_direct() != 1
+        finally:
+            p3d.set_pageable_direct(False)
