@@ -617,7 +617,7 @@ static bool pipeline_host_stages() {
   }
   return g_host_pipe == 1;
 }
-// Grid cap of an end stage that reads / writes a page-locked host array directly while its
+// Grid cap of an end stage that reads / writes a host array in place while its
 // neighbour stage runs beside it slab by slab (0: no such pipelining).  -1 (default): from
 // P3DFFT_GB300_LINK_CTAS when set, else one CTA per SM for FP64 stages and two for FP32.
 // Measured on the 512^3 round trip (forward / backward ms, +-0.05 between runs): FP64 38 CTAs
@@ -1103,7 +1103,8 @@ static cudaEvent_t g_pipe_ev[kMaxSlabs + 1];  // one per slab, and the fork / jo
 // host_out slab by slab as stage b finishes each (sd the slowest dim of that layout, so each slab
 // is one contiguous copy).
 static int ensure_copy_stream();
-// link 1: stage a reads a page-locked host array directly, link 2: stage b writes one; that stage
+// link 1: stage a reads a host array in place (page-locked, or pageable with in-place access),
+// link 2: stage b writes one; that stage
 // bounds the pair, so it runs on the priority stream with its grid capped at link_ctas persistent
 // CTAs (enough to keep the host link busy) and the other stage's slabs take the remaining SM time.
 static int run_pair_slabs(const Plan *P, int s, const void *src, void *mid, void *dst, int idir, const FFLink *lka,
